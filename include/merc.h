@@ -1,0 +1,151 @@
+/*
+ * merc.h - C ABI of the GB300 Mercurius integrator (libmerc.so).
+ *
+ * The reference (at2005/p9-integrator) has no library interface: its only
+ * boundary is the `mint` executable, which launches one CUDA kernel per batch
+ * of steps:
+ *   mercurius_solver(double* omega, M, e, a, i, Omega, double* m,
+ *                    double3* out_pos, int Nm, int batch, double dt)
+ *     src/sim.cuh:615-625, launched from src/mercurius.cu:184-196.
+ * Every entry point below replaces one piece of that launch sequence so the
+ * drop-in `mint` CLI (and any FFI caller: ctypes, cgo, JNI) drives the GPU
+ * through plain pointers and sizes.  No torch or CUDA types cross this ABI.
+ *
+ * Conventions
+ *  - Every function returns an int status: MERC_OK (0) or a MERC_ERR_* code;
+ *    merc_last_error(ctx) returns a message for the last failure.
+ *  - Host buffers are owned by the caller and only read/written during the
+ *    call.  Device buffers are owned by the context.
+ *  - One context per host thread; a context is bound to one GPU.
+ *  - Units: G = 1, M_sun = 1 (implicit, at the origin, not in the body list),
+ *    AU, yr (reference README.md:2).  All state is IEEE binary64.
+ *  - Bodies of a system are ordered massive first; the first n_massive bodies
+ *    are the gravitating sources (reference src/mercurius.cu:4-15 counts them,
+ *    src/sim.cuh:339 loops over the first Nm).
+ *  - Arrays of a batch of systems are concatenated body-wise:
+ *    system s owns bodies [body_offset[s], body_offset[s+1]).
+ *  - Position/velocity arrays are structure-of-arrays, component-major:
+ *    pos[c * n_total + j] for component c in {x, y, z} of body j.
+ */
+#ifndef MERC_H
+#define MERC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MERC_OK 0
+#define MERC_ERR_CONFIG 1   /* invalid argument, size or parameter */
+#define MERC_ERR_CUDA 2     /* CUDA runtime error (message has details) */
+#define MERC_ERR_TIMEOUT 3  /* a bounded device wait gave up */
+#define MERC_ERR_NONCONV 4  /* a Kepler solve hit its iteration cap */
+#define MERC_ERR_STATE 5    /* call out of order (e.g. step before load) */
+
+/* drift formulations */
+#define MERC_DRIFT_ELEMENTS 0  /* reference: cartesian->elements, M += n dt, Danby, back */
+#define MERC_DRIFT_UNIVERSAL 1 /* universal-variable (Stumpff) f and g solve */
+
+/* warm start of the universal-variable solve */
+#define MERC_WARM_PLAIN 0 /* s0 = dt / r0 */
+#define MERC_WARM_MLP 1   /* FP32 MLP guess, then the same FP64 Newton */
+
+/* per-body flags (uint32) */
+#define MERC_FLAG_CE_LAST 1u   /* close encounter detected in the most recent step */
+#define MERC_FLAG_CE_EVER 2u   /* close encounter detected in any step since load */
+#define MERC_FLAG_EJECTED 4u   /* heliocentric distance exceeded eject_r (sticky) */
+#define MERC_FLAG_NONFINITE 8u /* position or velocity became NaN/inf (sticky) */
+
+/* Integration parameters.  Defaults (merc_default_params) are the
+ * reference's compile-time constants (src/constants.cuh:4-11) and its
+ * hard-coded dt (src/mercurius.cu:43). */
+typedef struct merc_params {
+  double dt;            /* step, yr                          (ref 0.8219) */
+  double softening2;    /* epsilon^2 of the pair/Sun forces  (ref 1e-8, constants.cuh:8) */
+  double hill_factor;   /* r_crit = hill_factor * Hill radius of the source (ref 1) */
+  double kepler_tol;    /* universal solve: stop when |ds| <= tol*|s| (ref CUTOFF 1e-13) */
+  double eject_r;       /* flag bodies beyond this distance; 0 = off */
+  int32_t kepler_iters; /* Danby iterations, element drift (ref 8, constants.cuh:4) */
+  int32_t bs_rows;      /* Richardson rows of the encounter sub-stepper (ref 3, constants.cuh:10), 1..4 */
+  int32_t compat_block; /* 0: a body excludes itself by its index in the system.
+                           B > 0: reproduce the reference, which compares the source
+                           index with threadIdx.x = index % B (sim.cuh:172-175,364,608) */
+  int32_t drift;        /* MERC_DRIFT_* */
+  int32_t kepler_max_iter; /* universal solve iteration cap (>= 1) */
+  int32_t warm_start;   /* MERC_WARM_* */
+} merc_params;
+
+typedef struct merc_stats {
+  int64_t steps_done;        /* steps integrated since load */
+  int64_t ce_body_steps;     /* sum over steps of bodies in close encounter */
+  int64_t kepler_iterations; /* universal drift: Newton iterations summed over bodies */
+  int64_t kepler_solves;     /* universal drift: number of solves */
+  int64_t kepler_nonconverged; /* universal drift: solves that hit the cap */
+  int64_t n_bodies;          /* total bodies loaded (all systems) */
+  int64_t n_systems;
+  double last_step_ms;       /* device time of the last merc_step call */
+} merc_stats;
+
+typedef struct merc_ctx merc_ctx;
+
+/* Fill *p with the reference defaults. */
+void merc_default_params(merc_params* p);
+
+/* Create a context on CUDA device `device`.  Replaces cudaSetDevice +
+ * launch configuration, reference src/mercurius.cu:36,45-69. */
+int merc_create(int device, const merc_params* p, merc_ctx** out);
+int merc_destroy(merc_ctx* ctx);
+const char* merc_last_error(const merc_ctx* ctx);
+int merc_set_params(merc_ctx* ctx, const merc_params* p);
+
+/* Load systems from orbital elements.  Replaces the host staging of the
+ * element arrays (src/mercurius.cu:73-164) and the kernel prologue that turns
+ * them into heliocentric positions and democratic-heliocentric velocities
+ * (src/sim.cuh:654-677).  elements: 6 arrays of n_total doubles, in the order
+ * inclination, longitude of ascending node, argument of perihelion, mean
+ * anomaly, eccentricity, semi-major axis: elements[k * n_total + j]. */
+int merc_load_elements(merc_ctx* ctx, int32_t n_systems, const int64_t* body_offset,
+                       const int32_t* n_massive, const double* mass, const double* elements);
+
+/* Load systems from heliocentric positions and democratic-heliocentric
+ * velocities directly.  a_lag (may be NULL) is the semi-major axis the element
+ * drift uses for its first mean motion (src/sim.cuh:692); NULL derives it from
+ * the state. */
+int merc_load_state(merc_ctx* ctx, int32_t n_systems, const int64_t* body_offset,
+                    const int32_t* n_massive, const double* mass, const double* pos,
+                    const double* vel, const double* a_lag);
+
+/* Integrate n_steps Mercurius steps of every loaded system.  Replaces the
+ * step loop of mercurius_solver (src/sim.cuh:679-742). */
+int merc_step(merc_ctx* ctx, int64_t n_steps);
+
+/* Batch boundary of the reference: reverse democratic-heliocentric
+ * conversion, cartesian -> elements, then elements -> cartesian and forward
+ * conversion (src/sim.cuh:744-765 then :654-677).  Updates a_lag. */
+int merc_roundtrip(merc_ctx* ctx);
+
+/* Copy state out.  pos: heliocentric positions (3*n_total), vel: democratic-
+ * heliocentric velocities (3*n_total), flags: n_total.  Any pointer may be NULL.
+ * Replaces the output D2H copy of src/mercurius.cu:203-206. */
+int merc_get_state(merc_ctx* ctx, double* pos, double* vel, uint32_t* flags);
+int merc_get_a_lag(merc_ctx* ctx, double* a_lag);
+
+/* Orbital elements of the current state (reverse DH conversion, then
+ * cartesian -> elements; src/sim.cuh:748-758).  Layout as merc_load_elements. */
+int merc_get_elements(merc_ctx* ctx, double* elements);
+
+int merc_get_stats(merc_ctx* ctx, merc_stats* out);
+
+/* Energy of each system (massive bodies, Sun included, unsoftened), for
+ * conservation checks.  energy: n_systems doubles. */
+int merc_energy(merc_ctx* ctx, double* energy);
+
+/* Number of kernel launches issued by this context since creation. */
+int64_t merc_launch_count(const merc_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MERC_H */

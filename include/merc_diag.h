@@ -1,0 +1,36 @@
+/*
+ * merc_diag.h - diagnostic entry points of libmerc.so (no reference
+ * counterpart: the reference exposes no library).  They let a caller check the
+ * device math library against a host evaluation, measure the FP64 FMA peak
+ * of the GPU for roofline fractions, and time the kick kernels inside the
+ * captured step graph.
+ */
+#ifndef MERC_DIAG_H
+#define MERC_DIAG_H
+
+#include <stdint.h>
+
+#include "merc.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Evaluate a merc_math function on the GPU for n inputs: fn 0 sin, 1 cos,
+ * 2 atan2(x, y), 3 acos, 4 log, 5 sinh, 6 cosh, 7 cbrt, 8 exp. */
+int merc_diag_math(int device, int fn, int64_t n, const double* x, const double* y, double* out);
+
+/* FP64 FMA throughput of the device in TFLOP/s (2 flops per FMA), best of
+ * three runs of a register-resident FMA loop over 4 blocks per SM. */
+int merc_diag_fp64_peak(int device, double* tflops);
+
+/* on != 0: record CUDA events around each kick kernel when the step graph is
+ * next captured.  merc_diag_kick_ms returns the mean kick duration of the
+ * most recent graph replay and the number of kick launches it averaged. */
+int merc_diag_time_kicks(merc_ctx* ctx, int on);
+int merc_diag_kick_ms(merc_ctx* ctx, double* avg_ms, int32_t* n_launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MERC_DIAG_H */

@@ -1,0 +1,386 @@
+// merc_device.cuh - per-body device physics of the Mercurius step.
+//
+// Each function is the GPU form of one stage of the reference step
+// (at2005/p9-integrator src/sim.cuh); the cited lines give the formula.  The
+// translation unit is compiled with -fmad=false so that a*b+c is never fused
+// implicitly: the explicit fma() calls below are exactly those of the
+// reference, and together with merc_math.h every stage evaluates to the same
+// bits as the CPU check of the same algorithm.
+#pragma once
+#include <stdint.h>
+
+#include "merc_math.h"
+
+namespace merc {
+
+struct d3 {
+  double x, y, z;
+};
+
+__device__ __forceinline__ double mag2(const d3& a) { return fma(a.x, a.x, fma(a.y, a.y, a.z * a.z)); }
+__device__ __forceinline__ double stable_div(double x, double y) {  // sim.cuh:81-87
+  double etz = (double)(y == 0.0), netz = (double)(y != 0.0);
+  return (netz * x) / (y + etz);
+}
+__device__ __forceinline__ double stable_sqrt(double x) { return sqrt(x * (double)(x >= 0.0)); }  // :35-40
+__device__ __forceinline__ double stable_log(double x) {                                         // :57-62
+  return mm::log(x * (double)(x > 0.0) + (double)(x <= 0.0));
+}
+__device__ __forceinline__ double stable_acos(double x) {  // :64-72
+  double alto = (double)(fabs(x) <= 1.0);
+  return mm::acos(fma(x, alto, copysign(1.0 - alto, x)));
+}
+__device__ __forceinline__ double rsqrt_ieee(double x) { return 1.0 / sqrt(x); }
+
+// Changeover radius of a source: hill_factor x Hill radius, a from h and e
+// (sim.cuh:133-164).
+__device__ __forceinline__ double rcrit(const d3& r, const d3& v, double m, double hill) {
+  d3 h = {fma(r.y, v.z, -r.z * v.y), fma(r.z, v.x, -r.x * v.z), fma(r.x, v.y, -r.y * v.x)};
+  double h2 = mag2(h);
+  double rmag = sqrt(mag2(r));
+  double v2 = mag2(v);
+  double rdv = fma(r.x, v.x, fma(r.y, v.y, r.z * v.z));
+  double factor = v2 - 1.0 / rmag;
+  d3 ev = {fma(factor, r.x, -rdv * v.x), fma(factor, r.y, -rdv * v.y), fma(factor, r.z, -rdv * v.z)};
+  double e2 = mag2(ev);
+  double a = h2 / (1.0 - e2);
+  return a * (mm::cbrt(m / 3.0) * hill);
+}
+
+// Changeover weight K(y), y = (r_ij - 0.1 rc) / (0.9 rc) (sim.cuh:176-183).
+// The common cases y > 1 (K = 1) and y < 0 (K = 0) give the same bits as the
+// branch-free formula; everything else takes the formula.
+__device__ __forceinline__ double changeover_K(double y) {
+  if (y > 1.0 && y < 1.7976931348623157e308) return 1.0;
+  if (y < 0.0 && y > -1.7976931348623157e308) return 0.0;
+  double K = y * y / (2.0 * y * y - 2.0 * y + 1.0);
+  double gtz = (double)(y > 0.0), gto = (double)(y > 1.0), valid = (double)(y <= 1.0 && y >= 0.0);
+  return K * gtz * valid + gto;
+}
+
+// Sources of one system as seen by the kicks: positions, mass and the two
+// changeover products 0.1 rc, 0.9 rc, plus rc itself.
+struct SrcView {
+  const double* x;
+  const double* y;
+  const double* z;
+  const double* m;
+  const double* rc;  // rc, 0.1 rc, 0.9 rc interleaved: rc[3*i + k]
+};
+
+// K-weighted kick of one body over the system's sources in the reference's
+// order (body_interaction_kick, sim.cuh:327-382).  BS selects the encounter
+// weighting (1 - K inside r_crit, sim.cuh:357-361).
+template <bool BS>
+__device__ __forceinline__ d3 kick_exact(const d3& pos, d3 vel, int self, const SrcView& S, int nm, double dt,
+                                         double soft2) {
+  d3 acc = {0.0, 0.0, 0.0};
+  for (int i = 0; i < nm; i++) {
+    d3 d = {S.x[i] - pos.x, S.y[i] - pos.y, S.z[i] - pos.z};
+    double r_sq = mag2(d);
+    double r = stable_sqrt(r_sq);
+    double rc = S.rc[3 * i], rc01 = S.rc[3 * i + 1], rc09 = S.rc[3 * i + 2];
+    double notself = (double)(self != i);
+    double r_ij = notself * r;  // norm3d of d is the same sqrt of the same fma chain
+    double K = changeover_K((r_ij - rc01) / rc09);
+    double w = K;
+    if (BS) w = (double)(r <= rc) * (1.0 - K) + (double)(r > rc) * K;
+    r_sq += notself * soft2;
+    double denom = r_sq * r;
+    double wa = w * stable_div(S.m[i], denom);
+    acc.x = fma(wa, d.x, acc.x);
+    acc.y = fma(wa, d.y, acc.y);
+    acc.z = fma(wa, d.z, acc.z);
+  }
+  vel.x = fma(acc.x, dt, vel.x);
+  vel.y = fma(acc.y, dt, vel.y);
+  vel.z = fma(acc.z, dt, vel.z);
+  return vel;
+}
+
+// close_encounter_p, sim.cuh:589-613
+__device__ __forceinline__ bool close_encounter(const d3& pos, int self, const SrcView& S, int nm) {
+  bool ce = false;
+  for (int i = 0; i < nm; i++) {
+    d3 d = {S.x[i] - pos.x, S.y[i] - pos.y, S.z[i] - pos.z};
+    double mag = sqrt(mag2(d));
+    ce = ce || ((mag < S.rc[3 * i]) && (self != i));
+  }
+  return ce;
+}
+
+// ---- Kepler's equation, Danby/Burkardt, fixed iterations: sim.cuh:90-126 ----
+__device__ __forceinline__ double danby(double M, double e, int iters) {
+  double E = M;
+  const double lt1 = (double)(e < 1.0), gt1 = (double)(e > 1.0);
+  const double sign = copysign(1.0, e - 1.0);
+  for (int i = 0; i < iters; i++) {
+    double s, c;
+    mm::sincos(E, &s, &c);
+    // The reference blends both branches (sim.cuh:100-101).  For e < 1 and a
+    // finite sinh the hyperbolic terms enter as exact zeros, so they are only
+    // evaluated when they can matter.
+    double sh = 0.0, ch = 0.0;
+    if (gt1 != 0.0 || !(fabs(E) < 700.0)) {
+      sh = mm::sinh(E);
+      ch = mm::cosh(E);
+    }
+    s = lt1 * s + gt1 * sh;
+    c = lt1 * c + gt1 * ch;
+    double esin = e * s;
+    double f = (sign * M) - esin + E;
+    double ecos = e * c;
+    double fp = 1.0 - ecos;
+    double dE = -f / fp;
+    if (i > iters - 2) {
+      dE = -f / (fp + dE * esin / 2.0);
+      dE = -f / ((fp + dE * esin / 2.0) + (dE * dE * ecos / 6.0));
+      dE = -f / ((fp + dE * esin / 2.0) + (dE * dE * ecos / 6.0) - (dE * dE * dE * esin / 24.0));
+    }
+    E += dE;
+  }
+  return E;
+}
+
+struct PV {
+  d3 pos, vel;
+};
+
+// ---- elements -> cartesian, mu = 1: sim.cuh:188-239 ----
+__device__ __forceinline__ PV cart_from_elem(double inc, double node, double peri, double M, double e, double a,
+                                             int iters) {
+  double si, ci, so, co, sa, ca;
+  mm::sincos(inc, &si, &ci);
+  mm::sincos(node, &so, &co);
+  mm::sincos(peri, &sa, &ca);
+  double z1 = ca * co, z2 = ca * so, z3 = sa * co, z4 = sa * so;
+  double d11 = fma(-z4, ci, z1), d12 = fma(z3, ci, z2), d13 = sa * si;
+  double d21 = fma(-z2, ci, -z3), d22 = fma(z1, ci, -z4), d23 = ca * si;
+  double romes = stable_sqrt(copysign(1.0, e - 1.0) * fma(e, e, -1.0));
+  double gt1 = (double)(e > 1.0), lt1 = (double)(e < 1.0);
+  double E = danby(M, e, iters);
+  double sE, cE;
+  mm::sincos(E, &sE, &cE);
+  double shE = 0.0, chE = 0.0;
+  if (gt1 != 0.0 || !(fabs(E) < 700.0)) {
+    shE = mm::sinh(E);
+    chE = mm::cosh(E);
+  }
+  sE = fma(lt1, sE, gt1 * shE);
+  cE = fma(lt1, cE, gt1 * chE);
+  z1 = a * (cE - e);
+  z2 = copysign(1.0, 1.0 - e) * a * romes * sE;
+  double q = stable_div(stable_sqrt(stable_div(1.0, fabs(a))), copysign(1.0, 1.0 - e) * (fma(-e, cE, 1.0)));
+  z3 = -sE * q;
+  z4 = romes * cE * q;
+  PV r;
+  r.pos = {fma(d11, z1, d21 * z2), fma(d12, z1, d22 * z2), fma(d13, z1, d23 * z2)};
+  r.vel = {fma(d11, z3, d21 * z4), fma(d12, z3, d22 * z4), fma(d13, z3, d23 * z4)};
+  return r;
+}
+
+struct Elem {
+  double inc, node, peri, M, e, a;
+};
+
+// ---- cartesian -> elements, mu = 1: sim.cuh:241-324 ----
+__device__ __forceinline__ Elem elem_from_cart(const d3& p, const d3& v) {
+  const double tp = 6.283185307179586476925286766559005768394338798750211641949;
+  d3 h = {fma(p.y, v.z, -p.z * v.y), fma(p.z, v.x, -p.x * v.z), fma(p.x, v.y, -p.y * v.x)};
+  double h_sq = mag2(h) + 1e-8;
+  double inc = stable_acos(h.z * rsqrt_ieee(h_sq));
+  double node = mm::atan2(h.x, -h.y);
+  double r_v = fma(p.x, v.x, fma(p.y, v.y, (p.z * v.z)));
+  double v_sq = mag2(v);
+  double r = sqrt(mag2(p));
+  double s = h_sq;
+  double e = stable_sqrt(fma(s, v_sq - (2.0 / r), 1.0));
+  double q = s / (1.0 + e);
+  double cos_i = mm::cos(inc);
+  double to = stable_div(-h.x, h.y);
+  double temp = (1.0 - cos_i) * to;
+  double etz = (double)(h.y == 0.0), netz = (double)(h.y != 0.0);
+  double temp2 = fma(netz, to * to, etz);
+  double true_long = mm::atan2((fma(p.y, fma(temp2, cos_i, (netz * 1.0)), -p.x * temp)),
+                               fma(p.x, fma(netz, cos_i, temp2), -p.y * temp));
+  etz = (double)(e == 0.0);
+  netz = (double)(e != 0.0);
+  double cosE = stable_div(fma(v_sq, r, -1.0), e);
+  double E = stable_acos(cosE);
+  double rv_lt0 = (double)(r_v < 0.0);
+  E = fma(rv_lt0, tp, copysign(E, r_v));
+  double Ma = netz * fma(-e, mm::sin(E), E) + etz * true_long;
+  double gt1 = (double)(e > 1.0), lt1 = (double)(e < 1.0);
+  if (gt1 != 0.0 || !(e < 1.0)) {  // hyperbolic (or degenerate) branch of sim.cuh:297-299
+    E = fma(gt1, stable_log(cosE + stable_sqrt(fma(cosE, cosE, -1.0))), lt1 * E);
+    E = fma(gt1, copysign(E, r_v), lt1 * E);
+    Ma = fma(gt1, fma(e, mm::sinh(E), -E), lt1 * Ma);
+  }
+  double cos_f = stable_div((s - r), (e * r));
+  double f = stable_acos(cos_f);
+  f = fma(rv_lt0, tp, copysign(f, r_v));
+  double pp = true_long - f;
+  pp = netz * fmod(pp + tp + tp, tp);
+  double M_lt0 = (double)(Ma < 0.0);
+  Ma = fma(M_lt0, tp, Ma);
+  Ma = fmod(Ma, tp);
+  Elem out;
+  out.inc = inc;
+  out.node = node;
+  out.peri = pp - node;
+  out.M = Ma;
+  out.e = e;
+  out.a = q / (1.0 - e);
+  return out;
+}
+
+// ---- encounter sub-stepper: sim.cuh:410-551 ----
+__device__ __forceinline__ d3 vel_total(const d3& pos, const d3& vel, int self, const SrcView& S, int nm, double dt,
+                                        double soft2) {
+  d3 nv = kick_exact<true>(pos, vel, self, S, nm, dt, soft2);
+  double r_sq = mag2(pos);
+  double r = stable_sqrt(r_sq);
+  r_sq += soft2;
+  double denom = r_sq * r;
+  d3 rv = {pos.x / denom, pos.y / denom, pos.z / denom};
+  nv.x = fma(-rv.x, dt, nv.x);
+  nv.y = fma(-rv.y, dt, nv.y);
+  nv.z = fma(-rv.z, dt, nv.z);
+  return nv;
+}
+
+__device__ __forceinline__ PV mod_midpoint(PV c, int self, const SrcView& S, int nm, double dt, int N,
+                                           double soft2) {
+  double h = dt / (double)N;
+  d3 z1 = c.pos;
+  z1.x = fma(c.vel.x, h, z1.x);
+  z1.y = fma(c.vel.y, h, z1.y);
+  z1.z = fma(c.vel.z, h, z1.z);
+  double h2 = 2.0 * h;
+  d3 z0 = c.pos;
+  c.pos = z1;
+  c.vel = vel_total(c.pos, c.vel, self, S, nm, h, soft2);
+  for (int i = 1; i < N; i++) {
+    d3 t = {fma(h2, c.vel.x, z0.x), fma(h2, c.vel.y, z0.y), fma(h2, c.vel.z, z0.z)};
+    z0 = z1;
+    z1 = t;
+    c.pos = z1;
+    c.vel = vel_total(c.pos, c.vel, self, S, nm, h, soft2);
+  }
+  PV res;
+  res.pos = {0.5 * (z1.x + fma(c.vel.x, h, z0.x)), 0.5 * (z1.y + fma(c.vel.y, h, z0.y)),
+             0.5 * (z1.z + fma(c.vel.z, h, z0.z))};
+  res.vel = c.vel;
+  return res;
+}
+
+__device__ __forceinline__ void rich_combine(PV& o, const PV& a, const PV& q, double p4) {
+  double den = p4 - 1.0;
+  o.pos = {fma(p4, a.pos.x, -q.pos.x) / den, fma(p4, a.pos.y, -q.pos.y) / den, fma(p4, a.pos.z, -q.pos.z) / den};
+  o.vel = {fma(p4, a.vel.x, -q.vel.x) / den, fma(p4, a.vel.y, -q.vel.y) / den, fma(p4, a.vel.z, -q.vel.z) / den};
+}
+
+// Richardson extrapolation over modified-midpoint steps N = 1, 2, 4, ...
+// (sim.cuh:502-551); rows <= 4.  The tableau is kept row by row.
+__device__ __forceinline__ PV richardson(const PV& c, int self, const SrcView& S, int nm, double dt, int rows,
+                                         double soft2) {
+  PV prev[4], cur[4];
+  int N = 1;
+  prev[0] = mod_midpoint(c, self, S, nm, dt, N, soft2);
+  for (int i = 1; i < rows; i++) {
+    N <<= 1;
+    cur[0] = mod_midpoint(c, self, S, nm, dt, N, soft2);
+    double p4 = 1.0;
+    for (int j = 1; j <= i; j++) {
+      p4 *= 4.0;  // pow(4, j), exact
+      rich_combine(cur[j], cur[j - 1], prev[j - 1], p4);
+    }
+    for (int j = 0; j <= i; j++) prev[j] = cur[j];
+  }
+  return prev[rows - 1];
+}
+
+// ---- universal-variable drift (new formulation, no reference counterpart) ----
+// Stumpff functions by quartering and doubling, Horner-form Taylor series.
+__device__ __forceinline__ void stumpff(double z, double* c0, double* c1, double* c2, double* c3) {
+  int k = 0;
+  while (fabs(z) > 0.1 && k < 60) {
+    z = z * 0.25;
+    k++;
+  }
+  double s3 = fma(z, fma(z, fma(z, fma(z, fma(z, fma(z, 1.0 / 1307674368000.0, -1.0 / 6227020800.0),
+                                                  1.0 / 39916800.0), -1.0 / 362880.0), 1.0 / 5040.0),
+                         -1.0 / 120.0), 1.0 / 6.0);
+  double s2 = fma(z, fma(z, fma(z, fma(z, fma(z, fma(z, 1.0 / 87178291200.0, -1.0 / 479001600.0),
+                                                  1.0 / 3628800.0), -1.0 / 40320.0), 1.0 / 720.0),
+                         -1.0 / 24.0), 0.5);
+  double s1 = fma(-z, s3, 1.0);
+  double s0 = fma(-z, s2, 1.0);
+  for (; k > 0; k--) {
+    double n3 = fma(s0, s3, s2) * 0.25;
+    double n2 = s1 * s1 * 0.5;
+    double n1 = s0 * s1;
+    double n0 = fma(2.0 * s0, s0, -1.0);
+    s0 = n0;
+    s1 = n1;
+    s2 = n2;
+    s3 = n3;
+  }
+  *c0 = s0;
+  *c1 = s1;
+  *c2 = s2;
+  *c3 = s3;
+}
+
+struct UD {
+  PV out;
+  int iters;
+  bool converged;
+};
+
+// Universal Kepler drift with mu = 1 from initial guess s0: Newton on
+// r0 s + eta G2 + zeta G3 = dt, stop when |ds| <= tol |s|, f and g at the final s.
+__device__ __forceinline__ UD universal_drift(const d3& x0, const d3& v0, double dt, double s0, double tol,
+                                              int max_iter) {
+  double r0 = sqrt(mag2(x0));
+  double ir0 = 1.0 / r0;
+  double eta = fma(x0.x, v0.x, fma(x0.y, v0.y, x0.z * v0.z));
+  double v2 = mag2(v0);
+  double alpha = fma(2.0, ir0, -v2);
+  double zeta = fma(-alpha, r0, 1.0);
+  double s = s0;
+  int it = 0;
+  bool conv = false;
+  double c0, c1, c2, c3;
+  while (it < max_iter) {
+    double s2 = s * s;
+    stumpff(alpha * s2, &c0, &c1, &c2, &c3);
+    double G1 = s * c1, G2 = s2 * c2, G3 = s2 * s * c3;
+    double f = fma(r0, s, fma(eta, G2, fma(zeta, G3, -dt)));
+    double fp = fma(eta, G1, fma(zeta, G2, r0));
+    double ds = -f / fp;
+    s = s + ds;
+    it++;
+    if (fabs(ds) <= tol * fabs(s)) {
+      conv = true;
+      break;
+    }
+  }
+  double s2 = s * s;
+  stumpff(alpha * s2, &c0, &c1, &c2, &c3);
+  double G1 = s * c1, G2 = s2 * c2, G3 = s2 * s * c3;
+  double r = fma(eta, G1, fma(zeta, G2, r0));
+  double ir = 1.0 / r;
+  double f = fma(-G2, ir0, 1.0);
+  double g = dt - G3;
+  double fd = -G1 * ir0 * ir;
+  double gd = fma(-G2, ir, 1.0);
+  UD u;
+  u.out.pos = {fma(f, x0.x, g * v0.x), fma(f, x0.y, g * v0.y), fma(f, x0.z, g * v0.z)};
+  u.out.vel = {fma(fd, x0.x, gd * v0.x), fma(fd, x0.y, gd * v0.y), fma(fd, x0.z, gd * v0.z)};
+  u.iters = it;
+  u.converged = conv;
+  return u;
+}
+
+}  // namespace merc

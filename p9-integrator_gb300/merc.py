@@ -1,0 +1,258 @@
+"""Python binding of libmerc.so, the GB300 Mercurius integrator (C ABI in
+include/merc.h).
+
+This is a thin ctypes layer: every call goes to the CUDA library.  There is no
+CPU path; if libmerc.so has not been built the import of :class:`Integrator`
+fails with an error that says how to build it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmerc.so")
+
+MERC_OK = 0
+MERC_ERR_CONFIG = 1
+MERC_ERR_CUDA = 2
+MERC_ERR_TIMEOUT = 3
+MERC_ERR_NONCONV = 4
+MERC_ERR_STATE = 5
+
+DRIFT_ELEMENTS = 0
+DRIFT_UNIVERSAL = 1
+WARM_PLAIN = 0
+WARM_MLP = 1
+
+FLAG_CE_LAST = 1
+FLAG_CE_EVER = 2
+FLAG_EJECTED = 4
+FLAG_NONFINITE = 8
+
+_i64p = C.POINTER(C.c_int64)
+_i32p = C.POINTER(C.c_int32)
+_u32p = C.POINTER(C.c_uint32)
+_f64p = C.POINTER(C.c_double)
+
+
+class MercParams(C.Structure):
+    """``merc_params`` of include/merc.h."""
+
+    _fields_ = [
+        ("dt", C.c_double),
+        ("softening2", C.c_double),
+        ("hill_factor", C.c_double),
+        ("kepler_tol", C.c_double),
+        ("eject_r", C.c_double),
+        ("kepler_iters", C.c_int32),
+        ("bs_rows", C.c_int32),
+        ("compat_block", C.c_int32),
+        ("drift", C.c_int32),
+        ("kepler_max_iter", C.c_int32),
+        ("warm_start", C.c_int32),
+    ]
+
+
+class MercStats(C.Structure):
+    _fields_ = [
+        ("steps_done", C.c_int64),
+        ("ce_body_steps", C.c_int64),
+        ("kepler_iterations", C.c_int64),
+        ("kepler_solves", C.c_int64),
+        ("kepler_nonconverged", C.c_int64),
+        ("n_bodies", C.c_int64),
+        ("n_systems", C.c_int64),
+        ("last_step_ms", C.c_double),
+    ]
+
+
+class MercError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"merc error {code}: {msg}")
+        self.code = code
+
+
+_LIB = None
+
+
+def lib() -> C.CDLL:
+    """Load libmerc.so (once).  Raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    L.merc_default_params.argtypes = [C.POINTER(MercParams)]
+    L.merc_default_params.restype = None
+    L.merc_create.argtypes = [C.c_int, C.POINTER(MercParams), C.POINTER(vp)]
+    L.merc_destroy.argtypes = [vp]
+    L.merc_last_error.argtypes = [vp]
+    L.merc_last_error.restype = C.c_char_p
+    L.merc_set_params.argtypes = [vp, C.POINTER(MercParams)]
+    L.merc_load_elements.argtypes = [vp, C.c_int32, _i64p, _i32p, _f64p, _f64p]
+    L.merc_load_state.argtypes = [vp, C.c_int32, _i64p, _i32p, _f64p, _f64p, _f64p, _f64p]
+    L.merc_step.argtypes = [vp, C.c_int64]
+    L.merc_roundtrip.argtypes = [vp]
+    L.merc_get_state.argtypes = [vp, _f64p, _f64p, _u32p]
+    L.merc_get_a_lag.argtypes = [vp, _f64p]
+    L.merc_get_elements.argtypes = [vp, _f64p]
+    L.merc_get_stats.argtypes = [vp, C.POINTER(MercStats)]
+    L.merc_energy.argtypes = [vp, _f64p]
+    L.merc_launch_count.argtypes = [vp]
+    L.merc_launch_count.restype = C.c_int64
+    L.merc_diag_math.argtypes = [C.c_int, C.c_int, C.c_int64, _f64p, _f64p, _f64p]
+    L.merc_diag_fp64_peak.argtypes = [C.c_int, _f64p]
+    L.merc_diag_time_kicks.argtypes = [vp, C.c_int]
+    L.merc_diag_kick_ms.argtypes = [vp, _f64p, _i32p]
+    _LIB = L
+    return L
+
+
+def default_params(**kw) -> MercParams:
+    p = MercParams()
+    lib().merc_default_params(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+@dataclass
+class State:
+    pos: np.ndarray  # 3 x n (component-major, flattened)
+    vel: np.ndarray
+    flags: np.ndarray
+
+
+class Integrator:
+    """One integrator context on one GPU (merc_create ... merc_destroy)."""
+
+    def __init__(self, params: MercParams | None = None, device: int = 0):
+        self.L = lib()
+        self.h = C.c_void_p()
+        self.params = params if params is not None else default_params()
+        st = self.L.merc_create(device, C.byref(self.params), C.byref(self.h))
+        if st:
+            raise MercError(st, "merc_create failed (no CUDA device or invalid parameters)")
+        self.n = 0
+        self.nsys = 0
+
+    def _check(self, st):
+        if st:
+            raise MercError(st, self.L.merc_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.L.merc_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params: MercParams):
+        self._check(self.L.merc_set_params(self.h, C.byref(params)))
+        self.params = params
+
+    def load_elements(self, body_offset, n_massive, mass, elements):
+        off = np.ascontiguousarray(body_offset, np.int64)
+        nm = np.ascontiguousarray(n_massive, np.int32)
+        self._check(self.L.merc_load_elements(self.h, len(nm), _p(off, _i64p), _p(nm, _i32p), _p(_f64(mass), _f64p),
+                                              _p(_f64(elements), _f64p)))
+        self.n, self.nsys = int(off[-1]), len(nm)
+
+    def load_systems(self, sysm):
+        """Load a systems.Systems batch from its elements."""
+        self.load_elements(sysm.body_offset, sysm.n_massive, sysm.mass, sysm.elements)
+
+    def load_state(self, body_offset, n_massive, mass, pos, vel, a_lag=None):
+        off = np.ascontiguousarray(body_offset, np.int64)
+        nm = np.ascontiguousarray(n_massive, np.int32)
+        al = _f64(a_lag) if a_lag is not None else None
+        self._check(self.L.merc_load_state(self.h, len(nm), _p(off, _i64p), _p(nm, _i32p), _p(_f64(mass), _f64p),
+                                           _p(_f64(pos), _f64p), _p(_f64(vel), _f64p), _p(al, _f64p)))
+        self.n, self.nsys = int(off[-1]), len(nm)
+
+    def step(self, n_steps: int = 1):
+        self._check(self.L.merc_step(self.h, int(n_steps)))
+
+    def roundtrip(self):
+        self._check(self.L.merc_roundtrip(self.h))
+
+    def state(self) -> State:
+        pos = np.empty(3 * self.n)
+        vel = np.empty(3 * self.n)
+        flags = np.empty(self.n, np.uint32)
+        self._check(self.L.merc_get_state(self.h, _p(pos, _f64p), _p(vel, _f64p), _p(flags, _u32p)))
+        return State(pos, vel, flags)
+
+    def a_lag(self) -> np.ndarray:
+        a = np.empty(self.n)
+        self._check(self.L.merc_get_a_lag(self.h, _p(a, _f64p)))
+        return a
+
+    def elements(self) -> np.ndarray:
+        el = np.empty(6 * self.n)
+        self._check(self.L.merc_get_elements(self.h, _p(el, _f64p)))
+        return el
+
+    def stats(self) -> MercStats:
+        s = MercStats()
+        self._check(self.L.merc_get_stats(self.h, C.byref(s)))
+        return s
+
+    def energy(self) -> np.ndarray:
+        e = np.empty(self.nsys)
+        self._check(self.L.merc_energy(self.h, _p(e, _f64p)))
+        return e
+
+    def launch_count(self) -> int:
+        return int(self.L.merc_launch_count(self.h))
+
+    def time_kicks(self, on: bool = True):
+        self._check(self.L.merc_diag_time_kicks(self.h, 1 if on else 0))
+
+    def kick_ms(self):
+        ms = C.c_double()
+        cnt = C.c_int32()
+        self._check(self.L.merc_diag_kick_ms(self.h, C.byref(ms), C.byref(cnt)))
+        return ms.value, cnt.value
+
+
+MM_FUNCS = {"sin": 0, "cos": 1, "atan2": 2, "acos": 3, "log": 4, "sinh": 5, "cosh": 6, "cbrt": 7, "exp": 8}
+
+
+def device_math(fn: str, x, y=None, device: int = 0) -> np.ndarray:
+    """Evaluate a merc_math function on the GPU (diagnostic)."""
+    L = lib()
+    x = _f64(x)
+    yy = _f64(y) if y is not None else None
+    out = np.empty_like(x)
+    st = L.merc_diag_math(device, MM_FUNCS[fn], x.size, _p(x, _f64p), _p(yy, _f64p), _p(out, _f64p))
+    if st:
+        raise MercError(st, "merc_diag_math failed")
+    return out
+
+
+def fp64_peak_tflops(device: int = 0) -> float:
+    L = lib()
+    t = C.c_double()
+    st = L.merc_diag_fp64_peak(device, C.byref(t))
+    if st:
+        raise MercError(st, "merc_diag_fp64_peak failed")
+    return t.value
