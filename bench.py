@@ -1,0 +1,315 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Mercurius integrator.
+
+Metric: FP64 body-steps/s (bodies excluding the Sun x steps / second) of the
+planetary-embryo disk (Sun + Jupiter/Saturn analogues + 2000 embryos, all
+massive, dt 0.01 yr, changeover 3 Hill radii) integrated with the
+universal-variable drift.  Synthetic, seeded initial conditions.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours:       K timed steps on the GPU through libmerc.so, one CUDA-graph step per
+            timed iteration with the L2 flushed (512 MB write) in between;
+            `value` is device time (CUDA events), `e2e` is host wall time of the
+            public C-ABI call sequence set_state (H2D, pinned) -> step -> get_state
+            (D2H) per step.  Also reported: kick-kernel roofline against the
+            measured FP64 FMA peak, the CPU oracle on the host cores, and the
+            element-drift (reference-compat) path.
+reference:  the CPU restatement of the reference step (oracle/, OpenMP over all
+            host cores), same workload and metric; the reference itself is CUDA
+            only and ships no CPU path.
+N > 1 runs N independent replicas (one per GPU, no collective; weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "p9-integrator_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import systems  # noqa: E402
+
+METRIC = "FP64 body-steps/s (N=2000 embryo disk)"
+UNIT = "body-steps/s"
+FLOPS_PER_PAIR = 27  # kick work per pair: FMA = 2, sqrt and divide = 1 each
+
+
+def workload():
+    return systems.embryo_disk()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        return world, rank, local, dist
+    return 1, 0, 0, None
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax = float(f[1])
+            except ValueError:
+                continue
+            for name, val in zip(names, f[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def cpu_baseline(sysm, params_kw, budget_s=12.0):
+    """The oracle on this host's cores, timed on a bounded number of steps."""
+    from oracle import Oracle
+    from oracle import default_params as oparams
+
+    O = Oracle()
+    p = oparams(**params_kw)
+    pos, vel, alag = O.load_elements(p, sysm.body_offset, sysm.n_massive, sysm.mass, sysm.elements)
+    t0 = time.perf_counter()
+    pos, vel, alag, fl, _ = O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag, steps=1)
+    one = time.perf_counter() - t0
+    steps = int(max(1, min(200, budget_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag, flags=fl, steps=steps)
+    dt = time.perf_counter() - t0
+    return {"value": sysm.n_total * steps / dt, "unit": UNIT, "cores": O.threads(), "kind": "port",
+            "sample": f"{steps} steps of the full {sysm.n_total}-body workload ({dt:.1f} s)"}
+
+
+def run_reference(args, world, rank, dist):
+    if rank != 0:
+        return
+    from oracle import Oracle
+    from oracle import default_params as oparams
+
+    sysm = workload()
+    kw = dict(dt=sysm.dt, hill_factor=sysm.hill_factor, drift=1)
+    O = Oracle()
+    p = oparams(**kw)
+    pos, vel, alag = O.load_elements(p, sysm.body_offset, sysm.n_massive, sysm.mass, sysm.elements)
+    pos, vel, alag, fl, _ = O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag,
+                                  steps=args.warmup)
+    t0 = time.perf_counter()
+    O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag, flags=fl, steps=args.steps)
+    dt = time.perf_counter() - t0
+    value = sysm.n_total * args.steps / dt
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": sysm.label, "bodies": sysm.n_total, "dt": sysm.dt, "drift": "universal",
+                       "hill_factor": sysm.hill_factor},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.threads(), "kind": "port",
+                             "sample": f"{args.steps} full steps after {args.warmup} warm-up steps"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "CPU restatement of the reference step (the reference ships CUDA only)"}
+    print(json.dumps(line), flush=True)
+
+
+def load_traffic():
+    path = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def run_ours(args, world, rank, local, dist):
+    import merc
+
+    sysm = workload()
+    n = sysm.n_total
+    kw = dict(dt=sysm.dt, hill_factor=sysm.hill_factor, drift=merc.DRIFT_UNIVERSAL)
+    g = merc.Integrator(merc.default_params(**kw), device=local)
+    g.load_systems(sysm)
+    g.time_kicks(True)
+    peak = merc.fp64_peak_tflops(local)
+    g.step(args.warmup)
+    l0 = g.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    if dist is not None:
+        dist.barrier()
+    step_ms, kick_ms, kick_n = [], 0.0, 0
+    for _ in range(args.steps):
+        g.flush_l2(512 << 20)
+        g.step(1)
+        step_ms.append(g.stats().last_step_ms)
+        km, kc = g.kick_ms()
+        kick_ms += km * kc
+        kick_n += kc
+    if dist is not None:
+        dist.barrier()
+    ck = clocks.stop()
+    launches = g.launch_count() - l0
+    total_ms = max_over_ranks(dist, float(np.sum(step_ms)))
+    value = sum_over_ranks(dist, float(n * args.steps)) / (total_ms / 1e3)
+    kick_avg_ms = kick_ms / max(kick_n, 1)
+    nm = int(sysm.n_massive[0])
+    pairs_per_kick = nm * (nm - 1) + (n - nm) * nm
+    achieved = FLOPS_PER_PAIR * pairs_per_kick / (kick_avg_ms * 1e-3) / 1e12
+    traffic = load_traffic().get("kick_bytes_per_launch")
+    st = g.stats()
+
+    # end to end through the C ABI with host buffers (pinned) and copies
+    e2e_steps = max(3, min(args.steps, 20))
+    host = g.state()
+    alag = g.a_lag()
+    try:
+        import torch
+
+        pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+        pos_h, vel_h, alag_h = pin(host.pos.copy()), pin(host.vel.copy()), pin(alag.copy())
+    except Exception:
+        pos_h, vel_h, alag_h = host.pos.copy(), host.vel.copy(), alag.copy()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        g.set_state(pos_h, vel_h, alag_h)
+        g.step(1)
+        out = g.state()
+        pos_h[:] = out.pos
+        vel_h[:] = out.vel
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e_value = sum_over_ranks(dist, float(n * e2e_steps)) / e2e_s
+
+    # element-drift (reference-compat, bitwise-checked) path, same workload
+    compat = None
+    if not args.skip_compat:
+        gc = merc.Integrator(merc.default_params(dt=sysm.dt, hill_factor=sysm.hill_factor,
+                                                 drift=merc.DRIFT_ELEMENTS))
+        gc.load_systems(sysm)
+        gc.step(2)
+        cs = max(2, min(args.steps, 10))
+        gc.step(cs)
+        compat = {"value": n * cs / (gc.stats().last_step_ms / 1e3), "steps": cs, "drift": "elements"}
+        gc.close()
+    g.close()
+
+    if rank != 0:
+        return
+    cpu = cpu_baseline(sysm, kw) if not args.skip_cpu else None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded embryo disk)",
+        "config": {"workload": sysm.label, "bodies": n, "n_massive": nm, "dt": sysm.dt, "drift": "universal",
+                   "hill_factor": sysm.hill_factor, "l2": "flushed (512 MB write) between timed steps",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "fp64", "kernel": "k_kick", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "measured FP64 FMA loop on this GPU (merc_diag_fp64_peak)",
+                     "kick_ms": kick_avg_ms, "kick_launches": kick_n, "pairs_per_launch": pairs_per_kick,
+                     "flops_per_pair": FLOPS_PER_PAIR},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 7 * 8 * n,
+                "d2h_bytes_per_step": 6 * 8 * n + 4 * n, "steps": e2e_steps},
+        "gpu_launches": int(launches),
+        "clocks": ck,
+        "close_encounter_body_steps": int(st.ce_body_steps),
+        "kepler_mean_iterations": (st.kepler_iterations / st.kepler_solves) if st.kepler_solves else None,
+        "compat_elements_path": compat,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-compat", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        # the CPU reference runs on rank 0 only; other ranks have no work
+        if int(os.environ.get("RANK", "0")) == 0:
+            run_reference(args, int(os.environ.get("WORLD_SIZE", "1")), 0, None)
+        return
+    world, rank, local, dist = dist_setup()
+    if True:
+        run_ours(args, world, rank, local, dist)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -117,6 +117,11 @@ int merc_load_state(merc_ctx* ctx, int32_t n_systems, const int64_t* body_offset
                     const int32_t* n_massive, const double* mass, const double* pos,
                     const double* vel, const double* a_lag);
 
+/* Overwrite the state of the loaded systems (same layout and sizes as the
+ * load) from host buffers; a NULL pointer keeps that part.  Used to stream new
+ * initial conditions through a loaded context without reallocation. */
+int merc_set_state(merc_ctx* ctx, const double* pos, const double* vel, const double* a_lag);
+
 /* Integrate n_steps Mercurius steps of every loaded system.  Replaces the
  * step loop of mercurius_solver (src/sim.cuh:679-742). */
 int merc_step(merc_ctx* ctx, int64_t n_steps);

@@ -24,6 +24,10 @@ int merc_diag_math(int device, int fn, int64_t n, const double* x, const double*
  * three runs of a register-resident FMA loop over 4 blocks per SM. */
 int merc_diag_fp64_peak(int device, double* tflops);
 
+/* Write `bytes` of a scratch buffer on the context's stream (evicts L2 between
+ * timed steps) and wait for it. */
+int merc_diag_flush_l2(merc_ctx* ctx, int64_t bytes);
+
 /* on != 0: record CUDA events around each kick kernel when the step graph is
  * next captured.  merc_diag_kick_ms returns the mean kick duration of the
  * most recent graph replay and the number of kick launches it averaged. */

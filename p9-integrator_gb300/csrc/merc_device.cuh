@@ -65,7 +65,7 @@ struct SrcView {
   const double* y;
   const double* z;
   const double* m;
-  const double* rc;  // rc, 0.1 rc, 0.9 rc interleaved: rc[3*i + k]
+  const double* rc;  // rc, 0.1 rc, 0.9 rc, fast-path threshold: rc[4*i + k]
 };
 
 // K-weighted kick of one body over the system's sources in the reference's
@@ -79,7 +79,7 @@ __device__ __forceinline__ d3 kick_exact(const d3& pos, d3 vel, int self, const 
     d3 d = {S.x[i] - pos.x, S.y[i] - pos.y, S.z[i] - pos.z};
     double r_sq = mag2(d);
     double r = stable_sqrt(r_sq);
-    double rc = S.rc[3 * i], rc01 = S.rc[3 * i + 1], rc09 = S.rc[3 * i + 2];
+    double rc = S.rc[4 * i], rc01 = S.rc[4 * i + 1], rc09 = S.rc[4 * i + 2];
     double notself = (double)(self != i);
     double r_ij = notself * r;  // norm3d of d is the same sqrt of the same fma chain
     double K = changeover_K((r_ij - rc01) / rc09);
@@ -104,7 +104,7 @@ __device__ __forceinline__ bool close_encounter(const d3& pos, int self, const S
   for (int i = 0; i < nm; i++) {
     d3 d = {S.x[i] - pos.x, S.y[i] - pos.y, S.z[i] - pos.z};
     double mag = sqrt(mag2(d));
-    ce = ce || ((mag < S.rc[3 * i]) && (self != i));
+    ce = ce || ((mag < S.rc[4 * i]) && (self != i));
   }
   return ce;
 }
@@ -235,22 +235,30 @@ __device__ __forceinline__ Elem elem_from_cart(const d3& p, const d3& v) {
 }
 
 // ---- encounter sub-stepper: sim.cuh:410-551 ----
-__device__ __forceinline__ d3 vel_total(const d3& pos, const d3& vel, int self, const SrcView& S, int nm, double dt,
-                                        double soft2) {
-  d3 nv = kick_exact<true>(pos, vel, self, S, nm, dt, soft2);
-  double r_sq = mag2(pos);
-  double r = stable_sqrt(r_sq);
-  r_sq += soft2;
-  double denom = r_sq * r;
-  d3 rv = {pos.x / denom, pos.y / denom, pos.z / denom};
-  nv.x = fma(-rv.x, dt, nv.x);
-  nv.y = fma(-rv.y, dt, nv.y);
-  nv.z = fma(-rv.z, dt, nv.z);
-  return nv;
-}
+// The velocity update of one sub-step (update_my_velocity_total, sim.cuh:410-
+// 443) is a functor so the same Richardson scheme runs with the exact pair
+// sum of the reference order (ExactVelTotal) or with the parallel fast sums of
+// the universal path.
+struct ExactVelTotal {
+  const SrcView* S;
+  int nm, self;
+  double soft2;
+  __device__ __forceinline__ d3 operator()(const d3& pos, const d3& vel, double dt) const {
+    d3 nv = kick_exact<true>(pos, vel, self, *S, nm, dt, soft2);
+    double r_sq = mag2(pos);
+    double r = stable_sqrt(r_sq);
+    r_sq += soft2;
+    double denom = r_sq * r;
+    d3 rv = {pos.x / denom, pos.y / denom, pos.z / denom};
+    nv.x = fma(-rv.x, dt, nv.x);
+    nv.y = fma(-rv.y, dt, nv.y);
+    nv.z = fma(-rv.z, dt, nv.z);
+    return nv;
+  }
+};
 
-__device__ __forceinline__ PV mod_midpoint(PV c, int self, const SrcView& S, int nm, double dt, int N,
-                                           double soft2) {
+template <class VT>
+__device__ __forceinline__ PV mod_midpoint(PV c, const VT& vt, double dt, int N) {
   double h = dt / (double)N;
   d3 z1 = c.pos;
   z1.x = fma(c.vel.x, h, z1.x);
@@ -259,13 +267,13 @@ __device__ __forceinline__ PV mod_midpoint(PV c, int self, const SrcView& S, int
   double h2 = 2.0 * h;
   d3 z0 = c.pos;
   c.pos = z1;
-  c.vel = vel_total(c.pos, c.vel, self, S, nm, h, soft2);
+  c.vel = vt(c.pos, c.vel, h);
   for (int i = 1; i < N; i++) {
     d3 t = {fma(h2, c.vel.x, z0.x), fma(h2, c.vel.y, z0.y), fma(h2, c.vel.z, z0.z)};
     z0 = z1;
     z1 = t;
     c.pos = z1;
-    c.vel = vel_total(c.pos, c.vel, self, S, nm, h, soft2);
+    c.vel = vt(c.pos, c.vel, h);
   }
   PV res;
   res.pos = {0.5 * (z1.x + fma(c.vel.x, h, z0.x)), 0.5 * (z1.y + fma(c.vel.y, h, z0.y)),
@@ -282,14 +290,14 @@ __device__ __forceinline__ void rich_combine(PV& o, const PV& a, const PV& q, do
 
 // Richardson extrapolation over modified-midpoint steps N = 1, 2, 4, ...
 // (sim.cuh:502-551); rows <= 4.  The tableau is kept row by row.
-__device__ __forceinline__ PV richardson(const PV& c, int self, const SrcView& S, int nm, double dt, int rows,
-                                         double soft2) {
+template <class VT>
+__device__ __forceinline__ PV richardson(const PV& c, const VT& vt, double dt, int rows) {
   PV prev[4], cur[4];
   int N = 1;
-  prev[0] = mod_midpoint(c, self, S, nm, dt, N, soft2);
+  prev[0] = mod_midpoint(c, vt, dt, N);
   for (int i = 1; i < rows; i++) {
     N <<= 1;
-    cur[0] = mod_midpoint(c, self, S, nm, dt, N, soft2);
+    cur[0] = mod_midpoint(c, vt, dt, N);
     double p4 = 1.0;
     for (int j = 1; j <= i; j++) {
       p4 *= 4.0;  // pow(4, j), exact

@@ -36,349 +36,11 @@
 #include "../../include/merc.h"
 #include "../../include/merc_diag.h"
 #include "merc_device.cuh"
+#include "merc_fast.cuh"
 
 using namespace merc;
 
-namespace {
-
-constexpr int kThreads = 128;
-
-struct Dev {
-  int n = 0;     // bodies, all systems
-  int nsys = 0;  // systems
-  const int* off = nullptr;
-  const int* nm = nullptr;
-  const int* sys = nullptr;  // system of each body
-  double* x = nullptr;       // 3 n
-  double* v = nullptr;       // 3 n
-  double* xo = nullptr;      // 3 n, drift output
-  double* vo = nullptr;      // 3 n
-  const double* m = nullptr;
-  double* alag = nullptr;
-  uint32_t* flags = nullptr;
-  unsigned char* ce = nullptr;  // encounter flag of the current step
-  double* rc[2] = {nullptr, nullptr};  // 3 per body: rc, 0.1 rc, 0.9 rc (massive bodies only)
-  double* P = nullptr;               // 3 per system
-  int* ce_list = nullptr;
-  int* ce_count = nullptr;
-  unsigned long long* counters = nullptr;  // CE body-steps, Kepler iterations, solves, non-converged
-};
-
-__device__ __forceinline__ SrcView src_view(const Dev& D, const double* rc, int b0) {
-  SrcView S;
-  S.x = D.x + b0;
-  S.y = D.x + D.n + b0;
-  S.z = D.x + 2 * D.n + b0;
-  S.m = D.m + b0;
-  S.rc = rc + 3 * (size_t)b0;
-  return S;
-}
-
-__device__ __forceinline__ d3 load3(const double* a, int n, int j) { return {a[j], a[n + j], a[2 * n + j]}; }
-__device__ __forceinline__ void store3(double* a, int n, int j, const d3& v) {
-  a[j] = v.x;
-  a[n + j] = v.y;
-  a[2 * n + j] = v.z;
-}
-__device__ __forceinline__ int self_index(int local, int compat_block) {
-  return compat_block > 0 ? local % compat_block : local;
-}
-
-__device__ __forceinline__ void write_rc(double* rc, int j, const d3& x, const d3& v, double m, double hill) {
-  double r = rcrit(x, v, m, hill);
-  rc[3 * (size_t)j] = r;
-  rc[3 * (size_t)j + 1] = 0.1 * r;
-  rc[3 * (size_t)j + 2] = 0.9 * r;
-}
-
-// ---------------------------------------------------------------------------
-// prologue / epilogue kernels (sim.cuh:654-677 and :744-765)
-// ---------------------------------------------------------------------------
-__global__ void k_from_elements(Dev D, const double* __restrict__ el, int iters) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= D.n) return;
-  const int n = D.n;
-  PV pv = cart_from_elem(el[j], el[n + j], el[2 * n + j], el[3 * n + j], el[4 * n + j], el[5 * n + j], iters);
-  store3(D.x, n, j, pv.pos);
-  store3(D.v, n, j, pv.vel);
-  D.alag[j] = el[5 * n + j];
-}
-
-__global__ void k_to_elements(Dev D, double* __restrict__ el) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= D.n) return;
-  const int n = D.n;
-  Elem e = elem_from_cart(load3(D.x, n, j), load3(D.v, n, j));
-  el[j] = e.inc;
-  el[n + j] = e.node;
-  el[2 * n + j] = e.peri;
-  el[3 * n + j] = e.M;
-  el[4 * n + j] = e.e;
-  el[5 * n + j] = e.a;
-}
-
-// democratic_heliocentric_conversion (sim.cuh:555-587): per-system sums in the
-// reference order, then every body of the system is shifted.
-__global__ void k_dh_sums(Dev D, bool reverse) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= D.nsys) return;
-  const int b0 = D.off[s], nm = D.nm[s], n = D.n;
-  double total = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
-  for (int i = 0; i < nm; i++) {
-    double mi = D.m[b0 + i];
-    total += mi;
-    mx = fma(mi, D.v[b0 + i], mx);
-    my = fma(mi, D.v[n + b0 + i], my);
-    mz = fma(mi, D.v[2 * n + b0 + i], mz);
-  }
-  double not_rev = reverse ? 0.0 : 1.0;
-  double scale = 1.0 / fma(not_rev, total, 1.0);
-  D.P[3 * s] = mx * scale;
-  D.P[3 * s + 1] = my * scale;
-  D.P[3 * s + 2] = mz * scale;
-}
-
-__global__ void k_dh_apply(Dev D, double sgn) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= D.n) return;
-  const int s = D.sys[j], n = D.n;
-  D.v[j] = fma(sgn, D.P[3 * s], D.v[j]);
-  D.v[n + j] = fma(sgn, D.P[3 * s + 1], D.v[n + j]);
-  D.v[2 * n + j] = fma(sgn, D.P[3 * s + 2], D.v[2 * n + j]);
-}
-
-__global__ void k_rc(Dev D, double* rc_out, double hill) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= D.n) return;
-  const int s = D.sys[j];
-  if (j - D.off[s] >= D.nm[s]) return;
-  write_rc(rc_out, j, load3(D.x, D.n, j), load3(D.v, D.n, j), D.m[j], hill);
-}
-
-// ---------------------------------------------------------------------------
-// step kernels
-// ---------------------------------------------------------------------------
-// Half kick of every body (sim.cuh:683-685, 739-741).  When rc_out is given,
-// each massive body also writes the changeover radius of its new state for
-// the next phase; when `last` is set the step's flags are updated.
-__global__ void k_kick(Dev D, const double* __restrict__ rc_in, double* __restrict__ rc_out, double hdt,
-                       double soft2, int compat_block, double hill, double eject_r2, int last) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= D.n) return;
-  const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
-  const int local = j - b0;
-  SrcView S = src_view(D, rc_in, b0);
-  d3 pos = load3(D.x, n, j);
-  d3 vel = kick_exact<false>(pos, load3(D.v, n, j), self_index(local, compat_block), S, nm, hdt, soft2);
-  store3(D.v, n, j, vel);
-  if (rc_out && local < nm) write_rc(rc_out, j, pos, vel, D.m[j], hill);
-  if (last) {
-    uint32_t f = D.flags[j] & ~MERC_FLAG_CE_LAST;
-    if (D.ce[j]) f |= MERC_FLAG_CE_LAST | MERC_FLAG_CE_EVER;
-    if (eject_r2 > 0.0 && mag2(pos) > eject_r2) f |= MERC_FLAG_EJECTED;
-    bool fin = mm::isfinite_(pos.x) && mm::isfinite_(pos.y) && mm::isfinite_(pos.z) && mm::isfinite_(vel.x) &&
-               mm::isfinite_(vel.y) && mm::isfinite_(vel.z);
-    if (!fin) f |= MERC_FLAG_NONFINITE;
-    D.flags[j] = f;
-  }
-}
-
-// sum_i m_i v_i of each system in the reference order (main_body_kinetic,
-// sim.cuh:394-399); `vsrc` is the velocity array to sum.
-__global__ void k_momentum(Dev D, const double* __restrict__ vsrc) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= D.nsys) return;
-  const int b0 = D.off[s], nm = D.nm[s], n = D.n;
-  double px = 0.0, py = 0.0, pz = 0.0;
-  for (int i = 0; i < nm; i++) {
-    double mi = D.m[b0 + i];
-    px = fma(mi, vsrc[b0 + i], px);
-    py = fma(mi, vsrc[n + b0 + i], py);
-    pz = fma(mi, vsrc[2 * n + b0 + i], pz);
-  }
-  D.P[3 * s] = px;
-  D.P[3 * s + 1] = py;
-  D.P[3 * s + 2] = pz;
-}
-
-// Solar jump x = xsrc + dt/2 P (sim.cuh:402-404); copies vsrc -> v when the
-// drift wrote to the output buffers; massive bodies write their new r_crit.
-__global__ void k_jump(Dev D, const double* __restrict__ xsrc, const double* __restrict__ vsrc, double* rc_out,
-                       double hdt, double hill) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= D.n) return;
-  const int n = D.n, s = D.sys[j];
-  const double px = D.P[3 * s], py = D.P[3 * s + 1], pz = D.P[3 * s + 2];
-  d3 x = load3(xsrc, n, j);
-  x.x = fma(px, hdt, x.x);
-  x.y = fma(py, hdt, x.y);
-  x.z = fma(pz, hdt, x.z);
-  store3(D.x, n, j, x);
-  d3 v;
-  if (vsrc) {
-    v = load3(vsrc, n, j);
-    store3(D.v, n, j, v);
-  } else {
-    v = load3(D.v, n, j);
-  }
-  if (j - D.off[s] < D.nm[s]) write_rc(rc_out, j, x, v, D.m[j], hill);
-}
-
-// Encounter test and Kepler drift of every body (sim.cuh:692-713).  Bodies in
-// encounter are appended to the encounter list (warp ballot + prefix count);
-// the rest write their drifted state to xo/vo.  The element drift keeps the
-// reference's lagged mean motion (sim.cuh:692 uses a from the previous step).
-template <int DRIFT>
-__global__ void k_drift(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, int kep_iters,
-                        double tol, int max_iter) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = j < D.n;
-  const int lane = threadIdx.x & 31;
-  bool is_ce = false;
-  int its = 0, nonconv = 0;
-  if (active) {
-    const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
-    const int self = self_index(j - b0, compat_block);
-    SrcView S = src_view(D, rc_in, b0);
-    d3 pos = load3(D.x, n, j), vel = load3(D.v, n, j);
-    is_ce = close_encounter(pos, self, S, nm);
-    D.ce[j] = is_ce;
-    if (DRIFT == MERC_DRIFT_ELEMENTS) {
-      const double tp = 6.283185307179586476925286766559005768394338798750211641949;
-      double a = D.alag[j];
-      double nmot = rsqrt_ieee(a * a * a);
-      Elem el = elem_from_cart(pos, vel);
-      D.alag[j] = el.a;
-      double Mn = (double)(!is_ce) * fmod(fma(nmot, dt, el.M), tp) + (double)(is_ce)*el.M;
-      PV kep = cart_from_elem(el.inc, el.node, el.peri, Mn, el.e, el.a, kep_iters);
-      // for encounter bodies the Kepler result still enters the blend
-      // fma(0, kep, bs) of sim.cuh:718-730; the sub-step kernel completes it
-      store3(D.xo, n, j, kep.pos);
-      store3(D.vo, n, j, kep.vel);
-    } else if (!is_ce) {
-      double s0 = dt / sqrt(mag2(pos));
-      UD u = universal_drift(pos, vel, dt, s0, tol, max_iter);
-      store3(D.xo, n, j, u.out.pos);
-      store3(D.vo, n, j, u.out.vel);
-      its = u.iters;
-      nonconv = !u.converged;
-    }
-  }
-  // compaction of the encounter list
-  unsigned mask = __ballot_sync(0xffffffffu, is_ce);
-  if (mask) {
-    int leader = __ffs(mask) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(D.ce_count, __popc(mask));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (is_ce) D.ce_list[base + __popc(mask & ((1u << lane) - 1u))] = j;
-    if (lane == leader) atomicAdd(&D.counters[0], (unsigned long long)__popc(mask));
-  }
-  if (DRIFT == MERC_DRIFT_UNIVERSAL) {
-    int wits = __reduce_add_sync(0xffffffffu, its);
-    int wsol = __reduce_add_sync(0xffffffffu, (active && !is_ce) ? 1 : 0);
-    int wnc = __reduce_add_sync(0xffffffffu, nonconv);
-    if (lane == 0 && wsol) {
-      atomicAdd(&D.counters[1], (unsigned long long)wits);
-      atomicAdd(&D.counters[2], (unsigned long long)wsol);
-      if (wnc) atomicAdd(&D.counters[3], (unsigned long long)wnc);
-    }
-  }
-}
-
-// Encounter sub-step (Richardson extrapolation of modified-midpoint steps
-// against sources frozen at the start of the drift, sim.cuh:701-702) of every
-// body on the encounter list; grid-stride over the list.
-template <int DRIFT>
-__global__ void k_encounter(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, int rows,
-                            double soft2) {
-  const int count = *D.ce_count;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
-    const int j = D.ce_list[k];
-    const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
-    SrcView S = src_view(D, rc_in, b0);
-    PV c = {load3(D.x, n, j), load3(D.v, n, j)};
-    PV bs = richardson(c, self_index(j - b0, compat_block), S, nm, dt, rows, soft2);
-    if (DRIFT == MERC_DRIFT_ELEMENTS) {
-      d3 kp = load3(D.xo, n, j), kv = load3(D.vo, n, j);
-      bs.pos = {fma(0.0, kp.x, bs.pos.x), fma(0.0, kp.y, bs.pos.y), fma(0.0, kp.z, bs.pos.z)};
-      bs.vel = {fma(0.0, kv.x, bs.vel.x), fma(0.0, kv.y, bs.vel.y), fma(0.0, kv.z, bs.vel.z)};
-    }
-    store3(D.xo, n, j, bs.pos);
-    store3(D.vo, n, j, bs.vel);
-  }
-}
-
-// Energy of each system's massive bodies with the Sun (unsoftened, DH
-// variables): one block per system, compensated block sums.
-__global__ void k_energy(Dev D, double* out) {
-  const int s = blockIdx.x;
-  const int b0 = D.off[s], nm = D.nm[s], n = D.n;
-  __shared__ double red[kThreads];
-  double e = 0.0;
-  for (int i = threadIdx.x; i < nm; i += blockDim.x) {
-    int g = b0 + i;
-    d3 x = load3(D.x, n, g), v = load3(D.v, n, g);
-    double mi = D.m[g];
-    e += 0.5 * mi * mag2(v) - mi / sqrt(mag2(x));
-    for (int k = i + 1; k < nm; k++) {
-      d3 y = load3(D.x, n, b0 + k);
-      d3 d = {x.x - y.x, x.y - y.y, x.z - y.z};
-      e -= mi * D.m[b0 + k] / sqrt(mag2(d));
-    }
-  }
-  red[threadIdx.x] = e;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    double px = 0, py = 0, pz = 0;
-    for (int i = 0; i < nm; i++) {
-      double mi = D.m[b0 + i];
-      px += mi * D.v[b0 + i];
-      py += mi * D.v[n + b0 + i];
-      pz += mi * D.v[2 * n + b0 + i];
-    }
-    out[s] = red[0] + 0.5 * (px * px + py * py + pz * pz);
-  }
-}
-
-// ---- diagnostics ----
-__global__ void k_mm_eval(int fn, int n, const double* x, const double* y, double* out) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double a = x[i];
-  double r;
-  switch (fn) {
-    case 0: r = mm::sin(a); break;
-    case 1: r = mm::cos(a); break;
-    case 2: r = mm::atan2(a, y[i]); break;
-    case 3: r = mm::acos(a); break;
-    case 4: r = mm::log(a); break;
-    case 5: r = mm::sinh(a); break;
-    case 6: r = mm::cosh(a); break;
-    case 7: r = mm::cbrt(a); break;
-    default: r = mm::exp(a); break;
-  }
-  out[i] = r;
-}
-
-// FP64 FMA throughput probe: 8 independent fma chains per thread.
-__global__ void k_dfma_probe(double* out, int iters, double a, double b) {
-  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
-         x7 = x0 + 7;
-  for (int i = 0; i < iters; i++) {
-    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
-    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
-  }
-  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
-}
-
-inline unsigned blocks_for(int n) { return (unsigned)((n + kThreads - 1) / kThreads); }
-
-}  // namespace
+#include "merc_kernels.cuh"
 
 // ---------------------------------------------------------------------------
 // context
@@ -393,19 +55,29 @@ struct merc_ctx {
   int* d_nm = nullptr;
   int* d_sys = nullptr;
   double* d_m = nullptr;
+  unsigned char* d_big = nullptr;
+  int* d_nchunk = nullptr;
+  Work* d_work = nullptr;
+  int* d_big_ids = nullptr;
+  int n_work = 0, n_big = 0;
+  bool has_small = false, has_big = false, any_multi = false;
   std::vector<void*> allocs;
   std::vector<int> h_off, h_nm;
   bool loaded = false;
   int rc_cur = 0;  // buffer holding r_crit for the next first kick
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph = nullptr;  // kGraphSteps steps
+  cudaGraphExec_t graph1 = nullptr;  // one step
   int graph_steps = 0;
+  int last_graph_steps = 0;  // steps of the graph replayed last
+  double* flush_buf = nullptr;
+  size_t flush_bytes = 0;
   int enc_blocks = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<cudaEvent_t> kick_ev;  // start/end pairs recorded around kicks inside the graph
   bool time_kicks = false;
   int64_t steps_done = 0;
   int64_t launches = 0;
-  int64_t graph_launch_kernels = 0;
+  int kernels_per_step = 0;
   double last_ms = 0.0;
 };
 
@@ -443,10 +115,17 @@ int check_params(merc_ctx* ctx, const merc_params* p) {
   return MERC_OK;
 }
 
-void free_all(merc_ctx* ctx) {
+void drop_graphs(merc_ctx* ctx) {
+  ctx->last_graph_steps = 0;
   if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+  if (ctx->graph1) cudaGraphExecDestroy(ctx->graph1);
   ctx->graph = nullptr;
+  ctx->graph1 = nullptr;
   ctx->graph_steps = 0;
+}
+
+void free_all(merc_ctx* ctx) {
+  drop_graphs(ctx);
   for (void* a : ctx->allocs) cudaFree(a);
   ctx->allocs.clear();
   ctx->D = Dev();
@@ -486,36 +165,89 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
     ctx->h_off[s + 1] = (int)off[s + 1];
     for (int64_t j = off[s]; j < off[s + 1]; j++) sys[j] = s;
   }
+  // classification: systems with more than kSmallNm sources use the tiled
+  // kernels; their work items split targets into kTile tiles and sources
+  // into chunks so that about four blocks per SM are in flight
+  int dev_sms = 0;
+  cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  dev_sms = std::max(1, dev_sms);
+  std::vector<unsigned char> big(n_systems, 0);
+  std::vector<int> nchunk(n_systems, 0), big_ids;
+  std::vector<Work> work;
+  int64_t total_tiles = 0;
+  for (int s = 0; s < n_systems; s++) {
+    if (nm[s] > kSmallNm) {
+      big[s] = 1;
+      big_ids.push_back(s);
+      total_tiles += (off[s + 1] - off[s] + kTile - 1) / kTile;
+    }
+  }
+  const int64_t target_blocks = 4 * (int64_t)dev_sms;
+  int max_chunks = 1;
+  for (int s : big_ids) {
+    int ns = (int)(off[s + 1] - off[s]);
+    int64_t want = (target_blocks + total_tiles - 1) / std::max<int64_t>(total_tiles, 1);
+    int C = (int)std::max<int64_t>(1, std::min<int64_t>(want, (nm[s] + 15) / 16));
+    nchunk[s] = C;
+    max_chunks = std::max(max_chunks, C);
+    for (int t0 = 0; t0 < ns; t0 += kTile)
+      for (int c = 0; c < C; c++) {
+        Work w;
+        w.sys = s;
+        w.t0 = (int)off[s] + t0;
+        w.c0 = (int)((int64_t)c * nm[s] / C);
+        w.c1 = (int)((int64_t)(c + 1) * nm[s] / C);
+        w.chunk = c;
+        work.push_back(w);
+      }
+  }
+  ctx->n_work = (int)work.size();
+  ctx->n_big = (int)big_ids.size();
+  ctx->has_big = !big_ids.empty();
+  ctx->has_small = (int)big_ids.size() < n_systems;
+  ctx->any_multi = max_chunks > 1;
   Dev& D = ctx->D;
   D.n = n;
   D.nsys = n_systems;
   int st;
+  if ((st = dalloc(ctx, &ctx->d_big, n_systems)) || (st = dalloc(ctx, &ctx->d_nchunk, n_systems)) ||
+      (st = dalloc(ctx, &ctx->d_work, std::max(1, ctx->n_work))) ||
+      (st = dalloc(ctx, &ctx->d_big_ids, std::max(1, ctx->n_big))) ||
+      (st = dalloc(ctx, &D.part, ctx->any_multi ? (size_t)max_chunks * 3 * n : 1)) ||
+      (st = dalloc(ctx, &D.ce_list_big, n)))
+    return st;
   if ((st = dalloc(ctx, &ctx->d_off, n_systems + 1)) || (st = dalloc(ctx, &ctx->d_nm, n_systems)) ||
       (st = dalloc(ctx, &ctx->d_sys, n)) || (st = dalloc(ctx, &ctx->d_m, n)) || (st = dalloc(ctx, &D.x, 3 * (size_t)n)) ||
       (st = dalloc(ctx, &D.v, 3 * (size_t)n)) || (st = dalloc(ctx, &D.xo, 3 * (size_t)n)) ||
       (st = dalloc(ctx, &D.vo, 3 * (size_t)n)) || (st = dalloc(ctx, &D.alag, n)) || (st = dalloc(ctx, &D.flags, n)) ||
-      (st = dalloc(ctx, &D.ce, n)) || (st = dalloc(ctx, &D.rc[0], 3 * (size_t)n)) ||
-      (st = dalloc(ctx, &D.rc[1], 3 * (size_t)n)) || (st = dalloc(ctx, &D.P, 3 * (size_t)n_systems)) ||
-      (st = dalloc(ctx, &D.ce_list, n)) || (st = dalloc(ctx, &D.ce_count, 1)) || (st = dalloc(ctx, &D.counters, 4)))
+      (st = dalloc(ctx, &D.ce, n)) || (st = dalloc(ctx, &D.rc[0], 4 * (size_t)n)) ||
+      (st = dalloc(ctx, &D.rc[1], 4 * (size_t)n)) || (st = dalloc(ctx, &D.P, 3 * (size_t)n_systems)) ||
+      (st = dalloc(ctx, &D.ce_list, n)) || (st = dalloc(ctx, &D.ce_count, 2)) || (st = dalloc(ctx, &D.counters, 4)))
     return st;
   D.off = ctx->d_off;
   D.nm = ctx->d_nm;
   D.sys = ctx->d_sys;
   D.m = ctx->d_m;
+  D.big = ctx->d_big;
+  D.nchunk = ctx->d_nchunk;
   cudaStream_t s = ctx->stream;
   CK(cudaMemcpyAsync(ctx->d_off, ctx->h_off.data(), sizeof(int) * (n_systems + 1), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(ctx->d_nm, nm, sizeof(int) * n_systems, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(ctx->d_sys, sys.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(ctx->d_m, mass, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ctx->d_big, big.data(), n_systems, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ctx->d_nchunk, nchunk.data(), sizeof(int) * n_systems, cudaMemcpyHostToDevice, s));
+  if (ctx->n_work)
+    CK(cudaMemcpyAsync(ctx->d_work, work.data(), sizeof(Work) * ctx->n_work, cudaMemcpyHostToDevice, s));
+  if (ctx->n_big)
+    CK(cudaMemcpyAsync(ctx->d_big_ids, big_ids.data(), sizeof(int) * ctx->n_big, cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(D.flags, 0, sizeof(uint32_t) * n, s));
   CK(cudaMemsetAsync(D.ce, 0, n, s));
   CK(cudaMemsetAsync(D.counters, 0, sizeof(unsigned long long) * 4, s));
-  CK(cudaMemsetAsync(D.rc[0], 0, sizeof(double) * 3 * n, s));
-  CK(cudaMemsetAsync(D.rc[1], 0, sizeof(double) * 3 * n, s));
+  CK(cudaMemsetAsync(D.rc[0], 0, sizeof(double) * 4 * n, s));
+  CK(cudaMemsetAsync(D.rc[1], 0, sizeof(double) * 4 * n, s));
   CK(cudaStreamSynchronize(s));  // the host vectors above are temporaries
-  int dev_sms = 0;
-  cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
-  ctx->enc_blocks = std::max(1, dev_sms) * 4;
+  ctx->enc_blocks = dev_sms * 4;
   ctx->steps_done = 0;
   return MERC_OK;
 }
@@ -538,8 +270,9 @@ int dh_convert(merc_ctx* ctx, bool reverse) {
   return MERC_OK;
 }
 
-// Enqueue one step on the stream (also used while capturing the graph).
-int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph) {
+// Enqueue one step on the stream (also used while capturing the graph);
+// returns the number of kernels it launched through *kernels.
+int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int* kernels) {
   Dev& D = ctx->D;
   const merc_params& p = ctx->p;
   cudaStream_t s = ctx->stream;
@@ -548,65 +281,129 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph) {
   const double ej2 = p.eject_r > 0 ? p.eject_r * p.eject_r : 0.0;
   double* rcA = D.rc[ctx->rc_cur];
   double* rcB = D.rc[ctx->rc_cur ^ 1];
+  int nk = 0;
   auto kick_ev = [&](int k) {
-    if (record_kick_events) CK(cudaEventRecord(ctx->kick_ev[4 * step_in_graph + k], s));
+    if (record_kick_events)
+      CK(cudaEventRecordWithFlags(ctx->kick_ev[4 * (size_t)step_in_graph + k], s, cudaEventRecordExternal));
     return MERC_OK;
   };
   int st;
-  if ((st = kick_ev(0))) return st;
-  k_kick<<<nb, kThreads, 0, s>>>(D, rcA, nullptr, hdt, p.softening2, p.compat_block, p.hill_factor, ej2, 0);
-  if ((st = kick_ev(1))) return st;
-  k_momentum<<<sb, kThreads, 0, s>>>(D, D.v);
-  k_jump<<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt, p.hill_factor);
-  CK(cudaMemsetAsync(D.ce_count, 0, sizeof(int), s));
   if (p.drift == MERC_DRIFT_ELEMENTS) {
-    k_drift<MERC_DRIFT_ELEMENTS><<<nb, kThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.kepler_iters,
-                                                         p.kepler_tol, p.kepler_max_iter);
-    k_encounter<MERC_DRIFT_ELEMENTS><<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
-                                                                    p.softening2);
+    // exact path: the reference operation order for every system
+    if ((st = kick_ev(0))) return st;
+    k_kick<<<nb, kThreads, 0, s>>>(D, rcA, nullptr, hdt, p.softening2, p.compat_block, p.hill_factor, ej2, 0);
+    if ((st = kick_ev(1))) return st;
+    k_momentum<<<sb, kThreads, 0, s>>>(D, D.v, 0);
+    k_jump<<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt, p.hill_factor);
+    CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
+    k_drift_elements<<<nb, kThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.kepler_iters);
+    k_encounter_elements<<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2);
+    k_momentum<<<sb, kThreads, 0, s>>>(D, D.vo, 0);
+    k_jump<<<nb, kThreads, 0, s>>>(D, D.xo, D.vo, rcB, hdt, p.hill_factor);
+    if ((st = kick_ev(2))) return st;
+    k_kick<<<nb, kThreads, 0, s>>>(D, rcB, rcA, hdt, p.softening2, p.compat_block, p.hill_factor, ej2, 1);
+    if ((st = kick_ev(3))) return st;
+    nk = 8;
   } else {
-    k_drift<MERC_DRIFT_UNIVERSAL><<<nb, kThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.kepler_iters,
-                                                          p.kepler_tol, p.kepler_max_iter);
-    k_encounter<MERC_DRIFT_UNIVERSAL><<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
-                                                                     p.softening2);
+    auto kick = [&](const double* rc_in, double* rc_out, int last, int ev) {
+      int st2;
+      if ((st2 = kick_ev(ev))) return st2;
+      if (ctx->has_small) {
+        k_kick_small<<<nb, kThreads, 0, s>>>(D, rc_in, rc_out, hdt, p.softening2, p.compat_block, p.hill_factor,
+                                             ej2, last);
+        nk++;
+      }
+      if (ctx->has_big) {
+        k_kick_tiled<<<ctx->n_work, kTile, 0, s>>>(D, ctx->d_work, rc_in, rc_out, hdt, p.softening2, p.compat_block,
+                                                   p.hill_factor, ej2, last);
+        nk++;
+        if (ctx->any_multi) {
+          k_kick_reduce<<<nb, kThreads, 0, s>>>(D, rc_out, hdt, p.hill_factor, ej2, last);
+          nk++;
+        }
+      }
+      return kick_ev(ev + 1);
+    };
+    auto momentum = [&](const double* vsrc) {
+      if (ctx->has_small) {
+        k_momentum<<<sb, kThreads, 0, s>>>(D, vsrc, 1);
+        nk++;
+      }
+      if (ctx->has_big) {
+        k_momentum_big<<<ctx->n_big, kThreads, 0, s>>>(D, ctx->d_big_ids, vsrc);
+        nk++;
+      }
+    };
+    if ((st = kick(rcA, nullptr, 0, 0))) return st;
+    momentum(D.v);
+    k_jump<<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt, p.hill_factor);
+    nk++;
+    if (ctx->has_big) {
+      CK(cudaMemsetAsync(D.ce, 0, D.n, s));
+      k_ce_tiled<<<ctx->n_work, kTile, 0, s>>>(D, ctx->d_work, rcB, p.compat_block);
+      nk++;
+    }
+    CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
+    k_drift_universal<<<nb, kThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.kepler_tol, p.kepler_max_iter);
+    nk++;
+    if (ctx->has_small) {
+      k_encounter_small<<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2);
+      nk++;
+    }
+    if (ctx->has_big) {
+      k_encounter_big<<<ctx->enc_blocks, kEncThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
+                                                               p.softening2);
+      nk++;
+    }
+    momentum(D.vo);
+    k_jump<<<nb, kThreads, 0, s>>>(D, D.xo, D.vo, rcB, hdt, p.hill_factor);
+    nk++;
+    if ((st = kick(rcB, rcA, 1, 2))) return st;
   }
-  k_momentum<<<sb, kThreads, 0, s>>>(D, D.vo);
-  k_jump<<<nb, kThreads, 0, s>>>(D, D.xo, D.vo, rcB, hdt, p.hill_factor);
-  if ((st = kick_ev(2))) return st;
-  k_kick<<<nb, kThreads, 0, s>>>(D, rcB, rcA, hdt, p.softening2, p.compat_block, p.hill_factor, ej2, 1);
-  if ((st = kick_ev(3))) return st;
   CK(cudaGetLastError());
+  if (kernels) *kernels = nk;
   return MERC_OK;
 }
-constexpr int kKernelsPerStep = 8;
 
-int build_graph(merc_ctx* ctx, int steps) {
-  if (ctx->graph) {
-    cudaGraphExecDestroy(ctx->graph);
-    ctx->graph = nullptr;
+// Capture `steps` steps; with timing on, kick events use slots first_slot..
+int capture(merc_ctx* ctx, int steps, bool timed, int first_slot, cudaGraphExec_t* out) {
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < steps; k++) {
+    int nk = 0;
+    int st = enqueue_step(ctx, timed, first_slot + k, &nk);
+    ctx->kernels_per_step = nk;
+    if (st) {
+      cudaStreamEndCapture(ctx->stream, &g);
+      cudaGraphDestroy(g);
+      return st;
+    }
   }
+  CK(cudaStreamEndCapture(ctx->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(ctx, MERC_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+  return MERC_OK;
+}
+
+constexpr int kGraphSteps = 8;
+
+// The step graphs: kGraphSteps steps (kick events recorded when timing is on)
+// and a single step.
+int build_graphs(merc_ctx* ctx) {
+  drop_graphs(ctx);
   if (ctx->time_kicks) {
-    size_t need = 4 * (size_t)steps;
+    size_t need = 4 * (size_t)(kGraphSteps + 1);
     while (ctx->kick_ev.size() < need) {
       cudaEvent_t e;
       CK(cudaEventCreate(&e));
       ctx->kick_ev.push_back(e);
     }
   }
-  cudaGraph_t g;
-  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  for (int k = 0; k < steps; k++) {
-    int st = enqueue_step(ctx, ctx->time_kicks, k);
-    if (st) {
-      cudaStreamEndCapture(ctx->stream, &g);
-      return st;
-    }
-  }
-  CK(cudaStreamEndCapture(ctx->stream, &g));
-  cudaError_t e = cudaGraphInstantiate(&ctx->graph, g, 0);
-  cudaGraphDestroy(g);
-  if (e != cudaSuccess) return fail(ctx, MERC_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
-  ctx->graph_steps = steps;
+  int st;
+  if ((st = capture(ctx, kGraphSteps, ctx->time_kicks, 0, &ctx->graph))) return st;
+  if ((st = capture(ctx, 1, ctx->time_kicks, kGraphSteps, &ctx->graph1))) return st;
+  ctx->graph_steps = kGraphSteps;
   return MERC_OK;
 }
 
@@ -663,6 +460,7 @@ int merc_destroy(merc_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   free_all(ctx);
+  if (ctx->flush_buf) cudaFree(ctx->flush_buf);
   for (cudaEvent_t e : ctx->kick_ev) cudaEventDestroy(e);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -678,11 +476,7 @@ int merc_set_params(merc_ctx* ctx, const merc_params* p) {
   int st = check_params(ctx, p);
   if (st) return st;
   ctx->p = *p;
-  if (ctx->graph) {
-    cudaGraphExecDestroy(ctx->graph);
-    ctx->graph = nullptr;
-    ctx->graph_steps = 0;
-  }
+  drop_graphs(ctx);
   if (ctx->loaded) {
     CK(cudaSetDevice(ctx->device));
     return compute_rc(ctx);  // r_crit depends on hill_factor
@@ -742,28 +536,36 @@ int merc_load_state(merc_ctx* ctx, int32_t n_systems, const int64_t* body_offset
   return MERC_OK;
 }
 
+int merc_set_state(merc_ctx* ctx, const double* pos, const double* vel, const double* a_lag) {
+  if (!ctx) return MERC_ERR_CONFIG;
+  if (!ctx->loaded) return fail(ctx, MERC_ERR_STATE, "merc_set_state before a load");
+  CK(cudaSetDevice(ctx->device));
+  const int n = ctx->D.n;
+  if (pos) CK(cudaMemcpyAsync(ctx->D.x, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  if (vel) CK(cudaMemcpyAsync(ctx->D.v, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, ctx->stream));
+  if (a_lag) CK(cudaMemcpyAsync(ctx->D.alag, a_lag, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  int st = compute_rc(ctx);
+  if (st) return st;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return MERC_OK;
+}
+
 int merc_step(merc_ctx* ctx, int64_t n_steps) {
   if (!ctx) return MERC_ERR_CONFIG;
   if (!ctx->loaded) return fail(ctx, MERC_ERR_STATE, "merc_step before a load");
   if (n_steps < 0) return fail(ctx, MERC_ERR_CONFIG, "n_steps < 0");
   if (n_steps == 0) return MERC_OK;
   CK(cudaSetDevice(ctx->device));
-  const int G = 8;
-  if (!ctx->graph || ctx->graph_steps != G) {
-    int st = build_graph(ctx, G);
+  if (!ctx->graph) {
+    int st = build_graphs(ctx);
     if (st) return st;
   }
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  int64_t full = n_steps / G, rest = n_steps % G;
-  for (int64_t k = 0; k < full; k++) {
-    CK(cudaGraphLaunch(ctx->graph, ctx->stream));
-    ctx->launches += (int64_t)G * kKernelsPerStep;
-  }
-  for (int64_t k = 0; k < rest; k++) {
-    int st = enqueue_step(ctx, false, 0);
-    if (st) return st;
-    ctx->launches += kKernelsPerStep;
-  }
+  const int64_t full = n_steps / kGraphSteps, rest = n_steps % kGraphSteps;
+  for (int64_t k = 0; k < full; k++) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+  for (int64_t k = 0; k < rest; k++) CK(cudaGraphLaunch(ctx->graph1, ctx->stream));
+  ctx->last_graph_steps = rest > 0 ? 1 : kGraphSteps;
+  ctx->launches += n_steps * ctx->kernels_per_step;
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   CK(cudaEventSynchronize(ctx->ev1));
   float ms = 0.f;
@@ -927,25 +729,39 @@ int merc_diag_fp64_peak(int device, double* tflops) {
   return MERC_OK;
 }
 
+int merc_diag_flush_l2(merc_ctx* ctx, int64_t bytes) {
+  if (!ctx || bytes <= 0) return MERC_ERR_CONFIG;
+  CK(cudaSetDevice(ctx->device));
+  if (ctx->flush_bytes < (size_t)bytes) {
+    if (ctx->flush_buf) cudaFree(ctx->flush_buf);
+    ctx->flush_buf = nullptr;
+    ctx->flush_bytes = 0;
+    CK(cudaMalloc(&ctx->flush_buf, (size_t)bytes));
+    ctx->flush_bytes = (size_t)bytes;
+  }
+  CK(cudaMemsetAsync(ctx->flush_buf, (int)(ctx->steps_done & 0xff), (size_t)bytes, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return MERC_OK;
+}
+
 int merc_diag_time_kicks(merc_ctx* ctx, int on) {
   if (!ctx) return MERC_ERR_CONFIG;
   ctx->time_kicks = on != 0;
-  if (ctx->graph) {
-    cudaGraphExecDestroy(ctx->graph);
-    ctx->graph = nullptr;
-    ctx->graph_steps = 0;
-  }
+  drop_graphs(ctx);
   return MERC_OK;
 }
 
 int merc_diag_kick_ms(merc_ctx* ctx, double* avg_ms, int32_t* n_launches) {
   if (!ctx || !avg_ms) return MERC_ERR_CONFIG;
-  if (!ctx->time_kicks || ctx->graph_steps == 0) return fail(ctx, MERC_ERR_STATE, "kick timing is off");
+  if (!ctx->time_kicks || ctx->graph_steps == 0 || ctx->last_graph_steps == 0)
+    return fail(ctx, MERC_ERR_STATE, "kick timing is off or no step ran since it was turned on");
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   double sum = 0.0;
   int cnt = 0;
-  for (int k = 0; k < ctx->graph_steps; k++) {
+  const int first = ctx->last_graph_steps == 1 ? kGraphSteps : 0;
+  const int steps = ctx->last_graph_steps == 1 ? 1 : kGraphSteps;
+  for (int k = first; k < first + steps; k++) {
     for (int h = 0; h < 2; h++) {
       float ms = 0.f;
       CK(cudaEventElapsedTime(&ms, ctx->kick_ev[4 * k + 2 * h], ctx->kick_ev[4 * k + 2 * h + 1]));

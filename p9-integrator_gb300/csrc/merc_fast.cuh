@@ -1,0 +1,115 @@
+// merc_fast.cuh - pair arithmetic of the universal-drift path.
+//
+// FP64 is the bottleneck of this integrator on GB300 (one FP64 FMA per
+// SM per clock cycle pair, 1/58 of the FP32 rate), so the pair kernels count
+// FP64 instructions.  The common pair (source outside its changeover radius,
+// K = 1, not the body itself) costs 18 FP64 operations:
+//   d = x_i - x_j (3), r^2 (3), q = (r^2 + eps^2)^2 r^2 (3),
+//   u = q^(-1/2) from an FP32 MUFU seed refined by one Halley step (5),
+//   w = m u (1), acc += w d (3),
+// i.e. u = 1 / ((r^2 + eps^2) r) to ~1 ulp.  Every other pair (inside the
+// changeover radius, the body's own index, degenerate radii, distances
+// outside the FP32 range of the seed) takes the reference formula
+// (sim.cuh:339-375).  The decision "r > r_crit" is made on the high 32 bits of
+// r^2 and r_crit^2 (integer compare on positive doubles), with a margin so
+// that the fast branch is only taken where the reference's y > 1.
+#pragma once
+#include "merc_device.cuh"
+
+namespace merc {
+
+// A source of the fast path: position, mass, changeover radius and its
+// products, and the high word threshold of r_crit^2 (INT_MAX when r_crit is
+// not a positive finite number, which sends every pair to the exact branch).
+struct FastSrc {
+  double x, y, z, m, rc, rc01, rc09;
+  int rc2_hi;
+};
+
+__device__ __forceinline__ int hi_word(double x) { return __double2hiint(x); }
+
+// high-word threshold: r^2 hi word above this means r > r_crit with margin
+__device__ __forceinline__ int rc2_threshold(double rc) {
+  if (!(rc > 0.0) || !(rc < 1e150)) return 0x7fffffff;
+  return hi_word(rc * rc) + 1;
+}
+
+// 1 / ((r2 + eps2) sqrt(r2)) from an FP32 seed and one Halley step; valid
+// when (r2 + eps2)^2 r2 is a normal FP32 number (checked by the caller).
+__device__ __forceinline__ double inv_softened_r3(double r2, double s) {
+  double q = s * s;
+  q = q * r2;
+  double u = (double)rsqrtf((float)q);
+  double t = q * u;
+  double e = fma(-t, u, 1.0);
+  double c = fma(0.375, e, 0.5);
+  double ue = u * e;
+  return fma(ue, c, u);
+}
+
+// is q = (r2 + eps2)^2 r2 inside the FP32 normal range of the seed?
+__device__ __forceinline__ bool seed_in_range(double r2) {
+  // r2 in [1e-24, 1e12] keeps q in [~1e-40 .. 1e36] only if eps2 > 0 keeps
+  // s away from zero; the bounds below are conservative for eps2 >= 0.
+  return r2 > 1e-11 && r2 < 1e12;
+}
+
+// Exact pair of the reference (sim.cuh:344-374): weight K or the encounter
+// weighting, self exclusion, softening except for "self".
+template <bool BS>
+__device__ __forceinline__ void pair_exact(const d3& pos, int self, int i, const FastSrc& S, double soft2, d3& acc) {
+  d3 d = {S.x - pos.x, S.y - pos.y, S.z - pos.z};
+  double r_sq = mag2(d);
+  double r = stable_sqrt(r_sq);
+  double notself = (double)(self != i);
+  double K = changeover_K((notself * r - S.rc01) / S.rc09);
+  double w = K;
+  if (BS) w = (double)(r <= S.rc) * (1.0 - K) + (double)(r > S.rc) * K;
+  r_sq += notself * soft2;
+  double wa = w * stable_div(S.m, r_sq * r);
+  acc.x = fma(wa, d.x, acc.x);
+  acc.y = fma(wa, d.y, acc.y);
+  acc.z = fma(wa, d.z, acc.z);
+}
+
+// One pair on the fast path when possible.
+template <bool BS>
+__device__ __forceinline__ void pair_fast(const d3& pos, int self, int i, const FastSrc& S, double soft2, d3& acc) {
+  double dx = S.x - pos.x, dy = S.y - pos.y, dz = S.z - pos.z;
+  double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+  if (hi_word(r2) > S.rc2_hi && i != self && seed_in_range(r2)) {
+    double w = S.m * inv_softened_r3(r2, r2 + soft2);
+    acc.x = fma(w, dx, acc.x);
+    acc.y = fma(w, dy, acc.y);
+    acc.z = fma(w, dz, acc.z);
+  } else if (BS || i != self || r2 != 0.0) {
+    // (in the plain kick a body's own entry, at distance zero, contributes
+    // exactly zero: K = 0 and the guarded division returns 0)
+    pair_exact<BS>(pos, self, i, S, soft2, acc);
+  }
+}
+
+// Sun pull of the encounter sub-stepper: -pos / ((r^2 + eps^2) r)
+// (sim.cuh:431-441), fast where the seed range allows.
+__device__ __forceinline__ d3 sun_accel(const d3& pos, double soft2) {
+  double r2 = mag2(pos);
+  double s = r2 + soft2;
+  if (seed_in_range(r2)) {
+    double u = inv_softened_r3(r2, s);
+    return {-pos.x * u, -pos.y * u, -pos.z * u};
+  }
+  double r = stable_sqrt(r2);
+  double denom = s * r;
+  return {-(pos.x / denom), -(pos.y / denom), -(pos.z / denom)};
+}
+
+// Encounter test of one pair, exact: sqrt(r^2) < r_crit and not self
+// (sim.cuh:602-609); the sqrt is skipped when r^2 is clearly above r_crit^2.
+__device__ __forceinline__ bool pair_ce(const d3& pos, int self, int i, const FastSrc& S) {
+  double dx = S.x - pos.x, dy = S.y - pos.y, dz = S.z - pos.z;
+  double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+  if (hi_word(r2) > S.rc2_hi) return false;
+  return (sqrt(r2) < S.rc) && (self != i);
+}
+
+}  // namespace merc

@@ -1,0 +1,637 @@
+// merc_kernels.cuh - kernels of the Mercurius step (included by merc_engine.cu).
+//
+// Systems are classified at load time:
+//  - small systems (n_massive <= kSmallNm) are served one thread per body,
+//    each thread looping over its system's few sources (read-only cache
+//    broadcasts); the encounter sub-step is one thread per encounter body;
+//  - big systems (more sources) are served by work items of kTile targets x a
+//    chunk of sources, so a single system of ~2000 bodies fills all SMs; the
+//    per-chunk partial sums go to a scratch buffer and are added in chunk
+//    order (deterministic); the encounter sub-step gives each encounter body
+//    one block whose threads split the sources.
+// The element-drift path always uses the exact per-body kernels (reference
+// operation order); the universal path uses the classified fast kernels.
+#pragma once
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kTile = 128;       // targets per work item (one per thread)
+constexpr int kSrcTile = 256;    // sources staged in shared memory per pass
+constexpr int kSmallNm = 32;     // systems with more sources use the tiled kernels
+constexpr int kEncThreads = 128; // threads per encounter body of a big system
+
+struct Work {
+  int sys, t0, c0, c1, chunk;
+};
+
+struct Dev {
+  int n = 0;     // bodies, all systems
+  int nsys = 0;  // systems
+  const int* off = nullptr;
+  const int* nm = nullptr;
+  const int* sys = nullptr;  // system of each body
+  const unsigned char* big = nullptr;  // per system: served by the tiled kernels
+  const int* nchunk = nullptr;         // per system: source chunks of the tiled kick
+  double* x = nullptr;       // 3 n
+  double* v = nullptr;       // 3 n
+  double* xo = nullptr;      // 3 n, drift output
+  double* vo = nullptr;      // 3 n
+  const double* m = nullptr;
+  double* alag = nullptr;
+  uint32_t* flags = nullptr;
+  unsigned char* ce = nullptr;  // encounter flag of the current step
+  double* rc[2] = {nullptr, nullptr};  // 4 per body: rc, 0.1 rc, 0.9 rc, fast threshold (massive bodies)
+  double* P = nullptr;               // 3 per system
+  double* part = nullptr;            // kick partial sums [chunk][3][n]
+  int* ce_list = nullptr;            // encounter bodies of small systems
+  int* ce_list_big = nullptr;        // encounter bodies of big systems
+  int* ce_count = nullptr;           // [0] small list, [1] big list
+  unsigned long long* counters = nullptr;  // CE body-steps, Kepler iterations, solves, non-converged
+};
+
+__device__ __forceinline__ SrcView src_view(const Dev& D, const double* rc, int b0) {
+  SrcView S;
+  S.x = D.x + b0;
+  S.y = D.x + D.n + b0;
+  S.z = D.x + 2 * D.n + b0;
+  S.m = D.m + b0;
+  S.rc = rc + 4 * (size_t)b0;
+  return S;
+}
+
+__device__ __forceinline__ d3 load3(const double* a, int n, int j) { return {a[j], a[n + j], a[2 * n + j]}; }
+__device__ __forceinline__ void store3(double* a, int n, int j, const d3& v) {
+  a[j] = v.x;
+  a[n + j] = v.y;
+  a[2 * n + j] = v.z;
+}
+__device__ __forceinline__ int self_index(int local, int compat_block) {
+  return compat_block > 0 ? local % compat_block : local;
+}
+
+__device__ __forceinline__ void write_rc(double* rc, int j, const d3& x, const d3& v, double m, double hill) {
+  double r = rcrit(x, v, m, hill);
+  rc[4 * (size_t)j] = r;
+  rc[4 * (size_t)j + 1] = 0.1 * r;
+  rc[4 * (size_t)j + 2] = 0.9 * r;
+  rc[4 * (size_t)j + 3] = (double)rc2_threshold(r);
+}
+
+__device__ __forceinline__ FastSrc load_src(const Dev& D, const double* __restrict__ rc, int g) {
+  FastSrc S;
+  S.x = __ldg(D.x + g);
+  S.y = __ldg(D.x + D.n + g);
+  S.z = __ldg(D.x + 2 * D.n + g);
+  S.m = __ldg(D.m + g);
+  S.rc = __ldg(rc + 4 * (size_t)g);
+  S.rc01 = __ldg(rc + 4 * (size_t)g + 1);
+  S.rc09 = __ldg(rc + 4 * (size_t)g + 2);
+  S.rc2_hi = (int)__ldg(rc + 4 * (size_t)g + 3);
+  return S;
+}
+
+// after a kick: store v, r_crit of the new state for massive bodies, flags
+__device__ __forceinline__ void kick_epilogue(const Dev& D, int j, int local, int nm, const d3& pos, const d3& vel,
+                                              double* rc_out, double hill, double eject_r2, int last) {
+  store3(D.v, D.n, j, vel);
+  if (rc_out && local < nm) write_rc(rc_out, j, pos, vel, D.m[j], hill);
+  if (last) {
+    uint32_t f = D.flags[j] & ~MERC_FLAG_CE_LAST;
+    if (D.ce[j]) f |= MERC_FLAG_CE_LAST | MERC_FLAG_CE_EVER;
+    if (eject_r2 > 0.0 && mag2(pos) > eject_r2) f |= MERC_FLAG_EJECTED;
+    bool fin = mm::isfinite_(pos.x) && mm::isfinite_(pos.y) && mm::isfinite_(pos.z) && mm::isfinite_(vel.x) &&
+               mm::isfinite_(vel.y) && mm::isfinite_(vel.z);
+    if (!fin) f |= MERC_FLAG_NONFINITE;
+    D.flags[j] = f;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// prologue / epilogue kernels (sim.cuh:654-677 and :744-765)
+// ---------------------------------------------------------------------------
+__global__ void k_from_elements(Dev D, const double* __restrict__ el, int iters) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= D.n) return;
+  const int n = D.n;
+  PV pv = cart_from_elem(el[j], el[n + j], el[2 * n + j], el[3 * n + j], el[4 * n + j], el[5 * n + j], iters);
+  store3(D.x, n, j, pv.pos);
+  store3(D.v, n, j, pv.vel);
+  D.alag[j] = el[5 * n + j];
+}
+
+__global__ void k_to_elements(Dev D, double* __restrict__ el) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= D.n) return;
+  const int n = D.n;
+  Elem e = elem_from_cart(load3(D.x, n, j), load3(D.v, n, j));
+  el[j] = e.inc;
+  el[n + j] = e.node;
+  el[2 * n + j] = e.peri;
+  el[3 * n + j] = e.M;
+  el[4 * n + j] = e.e;
+  el[5 * n + j] = e.a;
+}
+
+// democratic_heliocentric_conversion (sim.cuh:555-587): per-system sums in the
+// reference order, then every body of the system is shifted.
+__global__ void k_dh_sums(Dev D, bool reverse) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.nsys) return;
+  const int b0 = D.off[s], nm = D.nm[s], n = D.n;
+  double total = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
+  for (int i = 0; i < nm; i++) {
+    double mi = D.m[b0 + i];
+    total += mi;
+    mx = fma(mi, D.v[b0 + i], mx);
+    my = fma(mi, D.v[n + b0 + i], my);
+    mz = fma(mi, D.v[2 * n + b0 + i], mz);
+  }
+  double not_rev = reverse ? 0.0 : 1.0;
+  double scale = 1.0 / fma(not_rev, total, 1.0);
+  D.P[3 * s] = mx * scale;
+  D.P[3 * s + 1] = my * scale;
+  D.P[3 * s + 2] = mz * scale;
+}
+
+__global__ void k_dh_apply(Dev D, double sgn) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= D.n) return;
+  const int s = D.sys[j], n = D.n;
+  D.v[j] = fma(sgn, D.P[3 * s], D.v[j]);
+  D.v[n + j] = fma(sgn, D.P[3 * s + 1], D.v[n + j]);
+  D.v[2 * n + j] = fma(sgn, D.P[3 * s + 2], D.v[2 * n + j]);
+}
+
+__global__ void k_rc(Dev D, double* rc_out, double hill) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= D.n) return;
+  const int s = D.sys[j];
+  if (j - D.off[s] >= D.nm[s]) return;
+  write_rc(rc_out, j, load3(D.x, D.n, j), load3(D.v, D.n, j), D.m[j], hill);
+}
+
+// ---------------------------------------------------------------------------
+// exact path (element drift): reference operation order
+// ---------------------------------------------------------------------------
+// Half kick of every body (sim.cuh:683-685, 739-741).
+__global__ void k_kick(Dev D, const double* __restrict__ rc_in, double* __restrict__ rc_out, double hdt,
+                       double soft2, int compat_block, double hill, double eject_r2, int last) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= D.n) return;
+  const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
+  const int local = j - b0;
+  SrcView S = src_view(D, rc_in, b0);
+  d3 pos = load3(D.x, n, j);
+  d3 vel = kick_exact<false>(pos, load3(D.v, n, j), self_index(local, compat_block), S, nm, hdt, soft2);
+  kick_epilogue(D, j, local, nm, pos, vel, rc_out, hill, eject_r2, last);
+}
+
+// sum_i m_i v_i of each system in the reference order (main_body_kinetic,
+// sim.cuh:394-399); `vsrc` is the velocity array to sum.  skip_big leaves the
+// big systems to k_momentum_big.
+__global__ void k_momentum(Dev D, const double* __restrict__ vsrc, int skip_big) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.nsys) return;
+  if (skip_big && D.big[s]) return;
+  const int b0 = D.off[s], nm = D.nm[s], n = D.n;
+  double px = 0.0, py = 0.0, pz = 0.0;
+  for (int i = 0; i < nm; i++) {
+    double mi = D.m[b0 + i];
+    px = fma(mi, vsrc[b0 + i], px);
+    py = fma(mi, vsrc[n + b0 + i], py);
+    pz = fma(mi, vsrc[2 * n + b0 + i], pz);
+  }
+  D.P[3 * s] = px;
+  D.P[3 * s + 1] = py;
+  D.P[3 * s + 2] = pz;
+}
+
+// Solar jump x = xsrc + dt/2 P (sim.cuh:402-404); copies vsrc -> v when the
+// drift wrote to the output buffers; massive bodies write their new r_crit.
+__global__ void k_jump(Dev D, const double* __restrict__ xsrc, const double* __restrict__ vsrc, double* rc_out,
+                       double hdt, double hill) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= D.n) return;
+  const int n = D.n, s = D.sys[j];
+  const double px = D.P[3 * s], py = D.P[3 * s + 1], pz = D.P[3 * s + 2];
+  d3 x = load3(xsrc, n, j);
+  x.x = fma(px, hdt, x.x);
+  x.y = fma(py, hdt, x.y);
+  x.z = fma(pz, hdt, x.z);
+  store3(D.x, n, j, x);
+  d3 v;
+  if (vsrc) {
+    v = load3(vsrc, n, j);
+    store3(D.v, n, j, v);
+  } else {
+    v = load3(D.v, n, j);
+  }
+  if (j - D.off[s] < D.nm[s]) write_rc(rc_out, j, x, v, D.m[j], hill);
+}
+
+// warp-aggregated append to an encounter list (ballot + prefix count)
+__device__ __forceinline__ void append_ce(bool flag, int j, int* list, int* count, unsigned long long* tally) {
+  const int lane = threadIdx.x & 31;
+  unsigned mask = __ballot_sync(0xffffffffu, flag);
+  if (mask) {
+    int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (flag) list[base + __popc(mask & ((1u << lane) - 1u))] = j;
+    if (lane == leader) atomicAdd(tally, (unsigned long long)__popc(mask));
+  }
+}
+
+// Encounter test and element drift of every body, reference order
+// (sim.cuh:692-713).  Bodies in encounter are appended to the encounter list;
+// every body writes its Kepler result to xo/vo (for encounter bodies it enters
+// the blend fma(0, kep, bs) of sim.cuh:718-730, completed by k_encounter).
+__global__ void k_drift_elements(Dev D, const double* __restrict__ rc_in, double dt, int compat_block,
+                                 int kep_iters) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  bool is_ce = false;
+  if (j < D.n) {
+    const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
+    const int self = self_index(j - b0, compat_block);
+    SrcView S = src_view(D, rc_in, b0);
+    d3 pos = load3(D.x, n, j), vel = load3(D.v, n, j);
+    is_ce = close_encounter(pos, self, S, nm);
+    D.ce[j] = is_ce;
+    const double tp = 6.283185307179586476925286766559005768394338798750211641949;
+    double a = D.alag[j];
+    double nmot = rsqrt_ieee(a * a * a);  // mean motion of the previous elements (sim.cuh:692)
+    Elem el = elem_from_cart(pos, vel);
+    D.alag[j] = el.a;
+    double Mn = (double)(!is_ce) * fmod(fma(nmot, dt, el.M), tp) + (double)(is_ce)*el.M;
+    PV kep = cart_from_elem(el.inc, el.node, el.peri, Mn, el.e, el.a, kep_iters);
+    store3(D.xo, n, j, kep.pos);
+    store3(D.vo, n, j, kep.vel);
+  }
+  append_ce(is_ce, j, D.ce_list, &D.ce_count[0], &D.counters[0]);
+}
+
+// Encounter sub-step (Richardson extrapolation of modified-midpoint steps
+// against sources frozen at the start of the drift, sim.cuh:701-702) in the
+// reference order; one thread per listed body, grid-stride.
+__global__ void k_encounter_elements(Dev D, const double* __restrict__ rc_in, double dt, int compat_block,
+                                     int rows, double soft2) {
+  const int count = D.ce_count[0];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+    const int j = D.ce_list[k];
+    const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
+    SrcView S = src_view(D, rc_in, b0);
+    ExactVelTotal vt{&S, nm, self_index(j - b0, compat_block), soft2};
+    PV c = {load3(D.x, n, j), load3(D.v, n, j)};
+    PV bs = richardson(c, vt, dt, rows);
+    d3 kp = load3(D.xo, n, j), kv = load3(D.vo, n, j);
+    bs.pos = {fma(0.0, kp.x, bs.pos.x), fma(0.0, kp.y, bs.pos.y), fma(0.0, kp.z, bs.pos.z)};
+    bs.vel = {fma(0.0, kv.x, bs.vel.x), fma(0.0, kv.y, bs.vel.y), fma(0.0, kv.z, bs.vel.z)};
+    store3(D.xo, n, j, bs.pos);
+    store3(D.vo, n, j, bs.vel);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// fast path (universal drift)
+// ---------------------------------------------------------------------------
+// Half kick of the bodies of small systems.
+__global__ void k_kick_small(Dev D, const double* __restrict__ rc_in, double* __restrict__ rc_out, double hdt,
+                             double soft2, int compat_block, double hill, double eject_r2, int last) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= D.n) return;
+  const int n = D.n, s = D.sys[j];
+  if (D.big[s]) return;
+  const int b0 = D.off[s], nm = D.nm[s], local = j - b0, self = self_index(local, compat_block);
+  d3 pos = load3(D.x, n, j);
+  d3 acc = {0.0, 0.0, 0.0};
+  for (int i = 0; i < nm; i++) pair_fast<false>(pos, self, i, load_src(D, rc_in, b0 + i), soft2, acc);
+  d3 vel = load3(D.v, n, j);
+  vel.x = fma(acc.x, hdt, vel.x);
+  vel.y = fma(acc.y, hdt, vel.y);
+  vel.z = fma(acc.z, hdt, vel.z);
+  kick_epilogue(D, j, local, nm, pos, vel, rc_out, hill, eject_r2, last);
+}
+
+// stage sources [c, c + cnt) of system starting at b0 into shared memory
+__device__ __forceinline__ void stage_sources(const Dev& D, const double* __restrict__ rc, int b0, int c, int cnt,
+                                              FastSrc* tile) {
+  for (int k = threadIdx.x; k < cnt; k += blockDim.x) tile[k] = load_src(D, rc, b0 + c + k);
+}
+
+// Tiled half kick of the big systems: block = work item (kTile targets x a
+// chunk of sources).  One chunk: finish the kick; several: write the partial.
+__global__ void __launch_bounds__(kTile) k_kick_tiled(Dev D, const Work* __restrict__ work,
+                                                      const double* __restrict__ rc_in, double* __restrict__ rc_out,
+                                                      double hdt, double soft2, int compat_block, double hill,
+                                                      double eject_r2, int last) {
+  __shared__ FastSrc tile[kSrcTile];
+  const Work W = work[blockIdx.x];
+  const int n = D.n, s = W.sys, b0 = D.off[s], b1 = D.off[s + 1], nm = D.nm[s];
+  const int j = W.t0 + threadIdx.x;
+  const bool active = j < b1;
+  const int local = j - b0, self = self_index(local, compat_block);
+  d3 pos = active ? load3(D.x, n, j) : d3{0.0, 0.0, 0.0};
+  d3 acc = {0.0, 0.0, 0.0};
+  for (int c = W.c0; c < W.c1; c += kSrcTile) {
+    const int cnt = min(kSrcTile, W.c1 - c);
+    __syncthreads();
+    stage_sources(D, rc_in, b0, c, cnt, tile);
+    __syncthreads();
+    if (active)
+      for (int k = 0; k < cnt; k++) pair_fast<false>(pos, self, c + k, tile[k], soft2, acc);
+  }
+  if (!active) return;
+  if (D.nchunk[s] == 1) {
+    d3 vel = load3(D.v, n, j);
+    vel.x = fma(acc.x, hdt, vel.x);
+    vel.y = fma(acc.y, hdt, vel.y);
+    vel.z = fma(acc.z, hdt, vel.z);
+    kick_epilogue(D, j, local, nm, pos, vel, rc_out, hill, eject_r2, last);
+  } else {
+    double* p = D.part + (size_t)W.chunk * 3 * n;
+    store3(p, n, j, acc);
+  }
+}
+
+// Sum of the chunk partials in chunk order, then the kick of big-system bodies
+// with more than one chunk.
+__global__ void k_kick_reduce(Dev D, double* __restrict__ rc_out, double hdt, double hill, double eject_r2,
+                              int last) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= D.n) return;
+  const int n = D.n, s = D.sys[j], C = D.nchunk[s];
+  if (!D.big[s] || C <= 1) return;
+  d3 acc = {0.0, 0.0, 0.0};
+  for (int c = 0; c < C; c++) {
+    const double* p = D.part + (size_t)c * 3 * n;
+    acc.x += p[j];
+    acc.y += p[n + j];
+    acc.z += p[2 * n + j];
+  }
+  d3 pos = load3(D.x, n, j), vel = load3(D.v, n, j);
+  vel.x = fma(acc.x, hdt, vel.x);
+  vel.y = fma(acc.y, hdt, vel.y);
+  vel.z = fma(acc.z, hdt, vel.z);
+  kick_epilogue(D, j, j - D.off[s], D.nm[s], pos, vel, rc_out, hill, eject_r2, last);
+}
+
+// Tiled encounter test of the big systems: any source of the chunk within
+// r_crit sets ce[j] (the flags were cleared before the launch).
+__global__ void __launch_bounds__(kTile) k_ce_tiled(Dev D, const Work* __restrict__ work,
+                                                    const double* __restrict__ rc_in, int compat_block) {
+  __shared__ FastSrc tile[kSrcTile];
+  const Work W = work[blockIdx.x];
+  const int n = D.n, s = W.sys, b0 = D.off[s], b1 = D.off[s + 1];
+  const int j = W.t0 + threadIdx.x;
+  const bool active = j < b1;
+  const int self = self_index(j - b0, compat_block);
+  d3 pos = active ? load3(D.x, n, j) : d3{0.0, 0.0, 0.0};
+  bool ce = false;
+  for (int c = W.c0; c < W.c1; c += kSrcTile) {
+    const int cnt = min(kSrcTile, W.c1 - c);
+    __syncthreads();
+    stage_sources(D, rc_in, b0, c, cnt, tile);
+    __syncthreads();
+    if (active)
+      for (int k = 0; k < cnt; k++) ce = ce || pair_ce(pos, self, c + k, tile[k]);
+  }
+  if (active && ce) D.ce[j] = 1;
+}
+
+// Momentum of each big system: block per system, strided partial sums and a
+// fixed-order tree (deterministic).
+__global__ void k_momentum_big(Dev D, const int* __restrict__ big_ids, const double* __restrict__ vsrc) {
+  const int s = big_ids[blockIdx.x];
+  const int b0 = D.off[s], nm = D.nm[s], n = D.n;
+  __shared__ double red[3][kThreads];
+  double px = 0.0, py = 0.0, pz = 0.0;
+  for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+    double mi = D.m[b0 + i];
+    px = fma(mi, vsrc[b0 + i], px);
+    py = fma(mi, vsrc[n + b0 + i], py);
+    pz = fma(mi, vsrc[2 * n + b0 + i], pz);
+  }
+  red[0][threadIdx.x] = px;
+  red[1][threadIdx.x] = py;
+  red[2][threadIdx.x] = pz;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + w];
+      red[1][threadIdx.x] += red[1][threadIdx.x + w];
+      red[2][threadIdx.x] += red[2][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    D.P[3 * s] = red[0][0];
+    D.P[3 * s + 1] = red[1][0];
+    D.P[3 * s + 2] = red[2][0];
+  }
+}
+
+// Encounter test (small systems inline, big systems from ce[]) and universal
+// drift of every body not in encounter; encounter bodies go to the lists.
+__global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, double tol,
+                                  int max_iter) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  bool ce_small = false, ce_big = false;
+  int its = 0, nonconv = 0, solved = 0;
+  if (j < D.n) {
+    const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
+    d3 pos = load3(D.x, n, j);
+    bool is_ce;
+    if (D.big[s]) {
+      is_ce = D.ce[j] != 0;
+      ce_big = is_ce;
+    } else {
+      const int self = self_index(j - b0, compat_block);
+      is_ce = false;
+      for (int i = 0; i < nm; i++) is_ce = is_ce || pair_ce(pos, self, i, load_src(D, rc_in, b0 + i));
+      D.ce[j] = is_ce;
+      ce_small = is_ce;
+    }
+    if (!is_ce) {
+      d3 vel = load3(D.v, n, j);
+      double s0 = dt / sqrt(mag2(pos));
+      UD u = universal_drift(pos, vel, dt, s0, tol, max_iter);
+      store3(D.xo, n, j, u.out.pos);
+      store3(D.vo, n, j, u.out.vel);
+      its = u.iters;
+      nonconv = !u.converged;
+      solved = 1;
+    }
+  }
+  append_ce(ce_small, j, D.ce_list, &D.ce_count[0], &D.counters[0]);
+  append_ce(ce_big, j, D.ce_list_big, &D.ce_count[1], &D.counters[0]);
+  int wits = __reduce_add_sync(0xffffffffu, its);
+  int wsol = __reduce_add_sync(0xffffffffu, solved);
+  int wnc = __reduce_add_sync(0xffffffffu, nonconv);
+  if (lane == 0 && wsol) {
+    atomicAdd(&D.counters[1], (unsigned long long)wits);
+    atomicAdd(&D.counters[2], (unsigned long long)wsol);
+    if (wnc) atomicAdd(&D.counters[3], (unsigned long long)wnc);
+  }
+}
+
+// velocity update of an encounter sub-step, one thread, fast pairs
+struct FastVelTotal {
+  const Dev* D;
+  const double* rc;
+  int b0, nm, self;
+  double soft2;
+  __device__ __forceinline__ d3 operator()(const d3& pos, const d3& vel, double dt) const {
+    d3 acc = {0.0, 0.0, 0.0};
+    for (int i = 0; i < nm; i++) pair_fast<true>(pos, self, i, load_src(*D, rc, b0 + i), soft2, acc);
+    d3 sa = sun_accel(pos, soft2);
+    d3 nv;
+    nv.x = fma(sa.x, dt, fma(acc.x, dt, vel.x));
+    nv.y = fma(sa.y, dt, fma(acc.y, dt, vel.y));
+    nv.z = fma(sa.z, dt, fma(acc.z, dt, vel.z));
+    return nv;
+  }
+};
+
+__global__ void k_encounter_small(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, int rows,
+                                  double soft2) {
+  const int count = D.ce_count[0];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+    const int j = D.ce_list[k];
+    const int n = D.n, s = D.sys[j], b0 = D.off[s];
+    FastVelTotal vt{&D, rc_in, b0, D.nm[s], self_index(j - b0, compat_block), soft2};
+    PV c = {load3(D.x, n, j), load3(D.v, n, j)};
+    PV bs = richardson(c, vt, dt, rows);
+    store3(D.xo, n, j, bs.pos);
+    store3(D.vo, n, j, bs.vel);
+  }
+}
+
+// velocity update of an encounter sub-step, the threads of a block split the
+// sources; the block sum is a fixed-order tree (all threads get the result)
+struct BlockVelTotal {
+  const Dev* D;
+  const double* rc;
+  int b0, nm, self;
+  double soft2;
+  double* red;  // shared, 3 * blockDim.x
+  __device__ __forceinline__ d3 operator()(const d3& pos, const d3& vel, double dt) const {
+    d3 acc = {0.0, 0.0, 0.0};
+    for (int i = threadIdx.x; i < nm; i += blockDim.x)
+      pair_fast<true>(pos, self, i, load_src(*D, rc, b0 + i), soft2, acc);
+    const int t = threadIdx.x, B = blockDim.x;
+    __syncthreads();
+    red[t] = acc.x;
+    red[B + t] = acc.y;
+    red[2 * B + t] = acc.z;
+    __syncthreads();
+    for (int w = B / 2; w > 0; w >>= 1) {
+      if (t < w) {
+        red[t] += red[t + w];
+        red[B + t] += red[B + t + w];
+        red[2 * B + t] += red[2 * B + t + w];
+      }
+      __syncthreads();
+    }
+    acc = {red[0], red[B], red[2 * B]};
+    d3 sa = sun_accel(pos, soft2);
+    d3 nv;
+    nv.x = fma(sa.x, dt, fma(acc.x, dt, vel.x));
+    nv.y = fma(sa.y, dt, fma(acc.y, dt, vel.y));
+    nv.z = fma(sa.z, dt, fma(acc.z, dt, vel.z));
+    return nv;
+  }
+};
+
+__global__ void __launch_bounds__(kEncThreads) k_encounter_big(Dev D, const double* __restrict__ rc_in, double dt,
+                                                               int compat_block, int rows, double soft2) {
+  __shared__ double red[3 * kEncThreads];
+  const int count = D.ce_count[1];
+  for (int k = blockIdx.x; k < count; k += gridDim.x) {
+    const int j = D.ce_list_big[k];
+    const int n = D.n, s = D.sys[j], b0 = D.off[s];
+    BlockVelTotal vt{&D, rc_in, b0, D.nm[s], self_index(j - b0, compat_block), soft2, red};
+    PV c = {load3(D.x, n, j), load3(D.v, n, j)};
+    PV bs = richardson(c, vt, dt, rows);
+    if (threadIdx.x == 0) {
+      store3(D.xo, n, j, bs.pos);
+      store3(D.vo, n, j, bs.vel);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// diagnostics
+// ---------------------------------------------------------------------------
+// Energy of each system's massive bodies with the Sun (unsoftened, DH
+// variables): one block per system.
+__global__ void k_energy(Dev D, double* out) {
+  const int s = blockIdx.x;
+  const int b0 = D.off[s], nm = D.nm[s], n = D.n;
+  __shared__ double red[kThreads];
+  double e = 0.0;
+  for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+    int g = b0 + i;
+    d3 x = load3(D.x, n, g), v = load3(D.v, n, g);
+    double mi = D.m[g];
+    e += 0.5 * mi * mag2(v) - mi / sqrt(mag2(x));
+    for (int k = i + 1; k < nm; k++) {
+      d3 y = load3(D.x, n, b0 + k);
+      d3 d = {x.x - y.x, x.y - y.y, x.z - y.z};
+      e -= mi * D.m[b0 + k] / sqrt(mag2(d));
+    }
+  }
+  red[threadIdx.x] = e;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double px = 0, py = 0, pz = 0;
+    for (int i = 0; i < nm; i++) {
+      double mi = D.m[b0 + i];
+      px += mi * D.v[b0 + i];
+      py += mi * D.v[n + b0 + i];
+      pz += mi * D.v[2 * n + b0 + i];
+    }
+    out[s] = red[0] + 0.5 * (px * px + py * py + pz * pz);
+  }
+}
+
+__global__ void k_mm_eval(int fn, int n, const double* x, const double* y, double* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double a = x[i];
+  double r;
+  switch (fn) {
+    case 0: r = mm::sin(a); break;
+    case 1: r = mm::cos(a); break;
+    case 2: r = mm::atan2(a, y[i]); break;
+    case 3: r = mm::acos(a); break;
+    case 4: r = mm::log(a); break;
+    case 5: r = mm::sinh(a); break;
+    case 6: r = mm::cosh(a); break;
+    case 7: r = mm::cbrt(a); break;
+    default: r = mm::exp(a); break;
+  }
+  out[i] = r;
+}
+
+// FP64 FMA throughput probe: 8 independent fma chains per thread.
+__global__ void k_dfma_probe(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+         x7 = x0 + 7;
+  for (int i = 0; i < iters; i++) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+inline unsigned blocks_for(int n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+
+}  // namespace

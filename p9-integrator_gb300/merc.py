@@ -98,6 +98,8 @@ def lib() -> C.CDLL:
     L.merc_load_elements.argtypes = [vp, C.c_int32, _i64p, _i32p, _f64p, _f64p]
     L.merc_load_state.argtypes = [vp, C.c_int32, _i64p, _i32p, _f64p, _f64p, _f64p, _f64p]
     L.merc_step.argtypes = [vp, C.c_int64]
+    L.merc_set_state.argtypes = [vp, _f64p, _f64p, _f64p]
+    L.merc_diag_flush_l2.argtypes = [vp, C.c_int64]
     L.merc_roundtrip.argtypes = [vp]
     L.merc_get_state.argtypes = [vp, _f64p, _f64p, _u32p]
     L.merc_get_a_lag.argtypes = [vp, _f64p]
@@ -187,6 +189,15 @@ class Integrator:
         self._check(self.L.merc_load_state(self.h, len(nm), _p(off, _i64p), _p(nm, _i32p), _p(_f64(mass), _f64p),
                                            _p(_f64(pos), _f64p), _p(_f64(vel), _f64p), _p(al, _f64p)))
         self.n, self.nsys = int(off[-1]), len(nm)
+
+    def set_state(self, pos=None, vel=None, a_lag=None):
+        """Overwrite the loaded state from host arrays (None keeps a part)."""
+        self._check(self.L.merc_set_state(self.h, _p(_f64(pos) if pos is not None else None, _f64p),
+                                          _p(_f64(vel) if vel is not None else None, _f64p),
+                                          _p(_f64(a_lag) if a_lag is not None else None, _f64p)))
+
+    def flush_l2(self, nbytes: int = 512 << 20):
+        self._check(self.L.merc_diag_flush_l2(self.h, int(nbytes)))
 
     def step(self, n_steps: int = 1):
         self._check(self.L.merc_step(self.h, int(n_steps)))
