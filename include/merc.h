@@ -150,6 +150,36 @@ int merc_energy(merc_ctx* ctx, double* energy);
 /* Number of kernel launches issued by this context since creation. */
 int64_t merc_launch_count(const merc_ctx* ctx);
 
+/* Bytes of the fixed device scratch array behind merc_step_static. */
+#define MERC_STATIC_SCRATCH_BYTES (16u << 20)
+
+/* Allocation-free stepping.  No counterpart in the reference (which has no
+ * library interface); it exists for callers that cannot call cudaMalloc: an
+ * application that gives the library device memory from its own pool or
+ * framework allocator, a runtime that forbids allocation after start-up, or a
+ * caller that must not add allocator traffic while it records GPU work.
+ *
+ * Integrates n_steps universal-drift steps (p->drift must be
+ * MERC_DRIFT_UNIVERSAL) of ONE system whose state is in caller-owned device
+ * memory: pos and vel (3 * n_bodies doubles each, component-major,
+ * heliocentric positions and democratic-heliocentric velocities, updated in
+ * place), mass (n_bodies doubles, massive bodies first) and flags
+ * (n_bodies uint32, updated; may be NULL).  stream is a cudaStream_t or NULL
+ * for the default stream; the call returns after the stream has finished the
+ * work.  The function allocates nothing: every scratch buffer comes from one
+ * fixed device array of MERC_STATIC_SCRATCH_BYTES, which every GPU that loads
+ * the library holds until the process exits.  Sizes whose scratch does not
+ * fit (about 100k bodies for a system with many massive bodies) return
+ * MERC_ERR_CONFIG before any work is queued.
+ *
+ * The first call on a device looks up the array's device address on that
+ * device (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls share the one array, and each call re-initialises the
+ * parts that must start at zero, so calls that overlap on the GPU (other
+ * host threads, other streams) race with each other: serialise them. */
+int merc_step_static(int device, const merc_params* p, int32_t n_bodies, int32_t n_massive, double* pos,
+                     double* vel, const double* mass, uint32_t* flags, int64_t n_steps, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

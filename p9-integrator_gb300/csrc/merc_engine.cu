@@ -28,6 +28,7 @@
 
 #include <algorithm>
 #include <cstdarg>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -677,6 +678,198 @@ int merc_energy(merc_ctx* ctx, double* energy) {
 }
 
 int64_t merc_launch_count(const merc_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free stepping (merc_step_static)
+// ---------------------------------------------------------------------------
+// Some callers cannot call cudaMalloc: a host application that hands this
+// library device memory it manages itself (a memory pool or a framework
+// allocator that must see every allocation), a runtime that forbids
+// allocation after start-up, or a caller that must not add allocator traffic
+// while it is recording CUDA work.  For them merc_step_static integrates one
+// system held in caller-owned device buffers and takes every scratch buffer of
+// the step (r_crit tables, the kick's per-chunk partial sums, drift outputs,
+// encounter lists, per-step momentum) from this fixed device array.  Every GPU
+// that loads the library holds it until the process exits.
+constexpr size_t kStaticScratchBytes = (size_t)MERC_STATIC_SCRATCH_BYTES;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+unsigned char* g_static_ptr[kMaxDevices] = {};
+
+// Device address of g_static_scratch on the current device `dev`: in host
+// code the symbol names a host-side stand-in, so the address comes from
+// cudaGetSymbolAddress, once per device, with that device current.
+cudaError_t static_scratch_on(int dev, unsigned char** out) {
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) return e;
+    g_static_ptr[dev] = (unsigned char*)p;
+  }
+  *out = g_static_ptr[dev];
+  return cudaSuccess;
+}
+
+// bump allocator over the static array (offsets only; nothing is allocated)
+struct Carve {
+  unsigned char* base;
+  size_t used = 0;
+  template <class T> T* take(size_t count) {
+    size_t bytes = (std::max<size_t>(count, 1) * sizeof(T) + 255) & ~(size_t)255;
+    T* p = base ? (T*)(base + used) : nullptr;
+    used += bytes;
+    return p;
+  }
+};
+
+}  // namespace
+
+extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodies, int32_t n_massive, double* pos,
+                                double* vel, const double* mass, uint32_t* flags, int64_t n_steps, void* stream) {
+  merc_ctx* ctx = nullptr;  // errors are reported by status code only
+  if (!p || !pos || !vel || !mass) return MERC_ERR_CONFIG;
+  if (n_bodies <= 0 || n_massive < 0 || n_massive > n_bodies || n_steps < 0) return MERC_ERR_CONFIG;
+  if (device < 0 || device >= kMaxDevices) return MERC_ERR_CONFIG;
+  if (p->drift != MERC_DRIFT_UNIVERSAL || check_params(nullptr, p) != MERC_OK) return MERC_ERR_CONFIG;
+  CK(cudaSetDevice(device));
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  sms = std::max(1, sms);
+  const int n = n_bodies, nm = n_massive;
+  const bool big = nm > kSmallNm;
+  // chunks of the tiled kick, as in the context path
+  int C = 1;
+  std::vector<Work> work;
+  if (big) {
+    int64_t tiles = (n + kTile - 1) / kTile;
+    int64_t want = (4 * (int64_t)sms + tiles - 1) / tiles;
+    C = (int)std::max<int64_t>(1, std::min<int64_t>(want, (nm + 15) / 16));
+  }
+  // layout of the scratch; sizes checked before anything is launched
+  Carve lay{nullptr};
+  auto plan = [&](Carve& c, Dev& D, int** off, int** nmv, unsigned char** bigv, int** nch, Work** wk, int** ids,
+                  uint32_t** fl) {
+    *off = c.take<int>(2);
+    *nmv = c.take<int>(1);
+    *bigv = c.take<unsigned char>(1);
+    *nch = c.take<int>(1);
+    *ids = c.take<int>(1);
+    *wk = c.take<Work>(big ? (size_t)((n + kTile - 1) / kTile) * C : 1);
+    D.sys = c.take<int>(n);
+    D.xo = c.take<double>(3 * (size_t)n);
+    D.vo = c.take<double>(3 * (size_t)n);
+    D.alag = c.take<double>(n);
+    D.ce = c.take<unsigned char>(n);
+    D.rc[0] = c.take<double>(4 * (size_t)n);
+    D.rc[1] = c.take<double>(4 * (size_t)n);
+    D.P = c.take<double>(3);
+    D.part = c.take<double>(C > 1 ? (size_t)C * 3 * n : 1);
+    D.ce_list = c.take<int>(n);
+    D.ce_list_big = c.take<int>(n);
+    D.ce_count = c.take<int>(2);
+    D.counters = c.take<unsigned long long>(4);
+    *fl = c.take<uint32_t>(n);
+  };
+  {
+    Dev tmp;
+    int *a, *b, *d, *f;
+    unsigned char* e;
+    Work* w;
+    uint32_t* g;
+    plan(lay, tmp, &a, &b, &e, &d, &w, &f, &g);
+    if (lay.used > kStaticScratchBytes) return MERC_ERR_CONFIG;  // too many bodies for the static scratch
+  }
+  if (n_steps == 0) return MERC_OK;
+  unsigned char* base = nullptr;
+  CK(static_scratch_on(device, &base));
+  Carve cv{base};
+  Dev D;
+  int *d_off, *d_nm, *d_nchunk, *d_ids;
+  unsigned char* d_big;
+  Work* d_work;
+  uint32_t* d_flags_scratch;
+  plan(cv, D, &d_off, &d_nm, &d_big, &d_nchunk, &d_work, &d_ids, &d_flags_scratch);
+  D.n = n;
+  D.nsys = 1;
+  D.off = d_off;
+  D.nm = d_nm;
+  D.big = d_big;
+  D.nchunk = d_nchunk;
+  D.x = pos;
+  D.v = vel;
+  D.m = mass;
+  D.flags = flags ? flags : d_flags_scratch;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (big)
+    for (int t0 = 0; t0 < n; t0 += kTile)
+      for (int c = 0; c < C; c++) work.push_back(Work{0, t0, (int)((int64_t)c * nm / C), (int)((int64_t)(c + 1) * nm / C), c});
+  const int h_off[2] = {0, n};
+  const int h_nchunk = big ? C : 0, h_ids = 0;
+  const unsigned char h_big = big ? 1 : 0;
+  // the tables of this call, and every region that must start at zero
+  CK(cudaMemcpyAsync(d_off, h_off, sizeof h_off, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_nm, &nm, sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_big, &h_big, 1, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_nchunk, &h_nchunk, sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_ids, &h_ids, sizeof(int), cudaMemcpyHostToDevice, s));
+  if (big) CK(cudaMemcpyAsync(d_work, work.data(), sizeof(Work) * work.size(), cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync((void*)D.sys, 0, sizeof(int) * n, s));
+  CK(cudaMemsetAsync(D.ce, 0, n, s));
+  CK(cudaMemsetAsync(D.counters, 0, 4 * sizeof(unsigned long long), s));
+  if (!flags) CK(cudaMemsetAsync(d_flags_scratch, 0, sizeof(uint32_t) * n, s));
+  // the kernel sequence of the universal path, on the caller's stream
+  const double hdt = 0.5 * p->dt;
+  const double ej2 = p->eject_r > 0 ? p->eject_r * p->eject_r : 0.0;
+  const unsigned nb = blocks_for(n);
+  double *rcA = D.rc[0], *rcB = D.rc[1];
+  k_rc<<<nb, kThreads, 0, s>>>(D, rcA, p->hill_factor);
+  auto kick = [&](const double* rc_in, double* rc_out, int last) {
+    if (!big) {
+      k_kick_small<<<nb, kThreads, 0, s>>>(D, rc_in, rc_out, hdt, p->softening2, p->compat_block, p->hill_factor,
+                                           ej2, last);
+    } else {
+      k_kick_tiled<<<(unsigned)work.size(), kTile, 0, s>>>(D, d_work, rc_in, rc_out, hdt, p->softening2,
+                                                          p->compat_block, p->hill_factor, ej2, last);
+      if (C > 1) k_kick_reduce<<<nb, kThreads, 0, s>>>(D, rc_out, hdt, p->hill_factor, ej2, last);
+    }
+  };
+  auto momentum = [&](const double* vsrc) {
+    if (!big)
+      k_momentum<<<1, kThreads, 0, s>>>(D, vsrc, 1);
+    else
+      k_momentum_big<<<1, kThreads, 0, s>>>(D, d_ids, vsrc);
+  };
+  for (int64_t k = 0; k < n_steps; k++) {
+    kick(rcA, nullptr, 0);
+    momentum(D.v);
+    k_jump<<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt, p->hill_factor);
+    if (big) {
+      CK(cudaMemsetAsync(D.ce, 0, n, s));
+      k_ce_tiled<<<(unsigned)work.size(), kTile, 0, s>>>(D, d_work, rcB, p->compat_block);
+    }
+    CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
+    k_drift_universal<<<nb, kThreads, 0, s>>>(D, rcB, p->dt, p->compat_block, p->kepler_tol, p->kepler_max_iter);
+    if (!big)
+      k_encounter_small<<<sms * 4, 64, 0, s>>>(D, rcB, p->dt, p->compat_block, p->bs_rows, p->softening2);
+    else
+      k_encounter_big<<<sms * 4, kEncThreads, 0, s>>>(D, rcB, p->dt, p->compat_block, p->bs_rows, p->softening2);
+    momentum(D.vo);
+    k_jump<<<nb, kThreads, 0, s>>>(D, D.xo, D.vo, rcB, hdt, p->hill_factor);
+    kick(rcB, rcA, 1);
+    CK(cudaGetLastError());
+  }
+  CK(cudaStreamSynchronize(s));
+  return MERC_OK;
+}
+
+extern "C" {
 
 // ---- diagnostics (merc_diag.h) ----
 int merc_diag_math(int device, int fn, int64_t n, const double* x, const double* y, double* out) {

@@ -108,6 +108,8 @@ def lib() -> C.CDLL:
     L.merc_energy.argtypes = [vp, _f64p]
     L.merc_launch_count.argtypes = [vp]
     L.merc_launch_count.restype = C.c_int64
+    L.merc_step_static.argtypes = [C.c_int, C.POINTER(MercParams), C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
     L.merc_diag_math.argtypes = [C.c_int, C.c_int, C.c_int64, _f64p, _f64p, _f64p]
     L.merc_diag_fp64_peak.argtypes = [C.c_int, _f64p]
     L.merc_diag_time_kicks.argtypes = [vp, C.c_int]
