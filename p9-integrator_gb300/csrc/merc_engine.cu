@@ -58,9 +58,12 @@ struct merc_ctx {
   double* d_m = nullptr;
   unsigned char* d_big = nullptr;
   int* d_nchunk = nullptr;
-  Work* d_work = nullptr;
+  Work* d_work = nullptr;     // all targets of the big systems
+  Work* d_work_tp = nullptr;  // test-particle targets of the big systems
+  SymTask* d_sym = nullptr;   // massive block pairs of the big systems
+  long long* d_sym_base = nullptr;
   int* d_big_ids = nullptr;
-  int n_work = 0, n_big = 0;
+  int n_work = 0, n_work_tp = 0, n_sym = 0, n_big = 0, max_big_nm = 0;
   bool has_small = false, has_big = false, any_multi = false;
   std::vector<void*> allocs;
   std::vector<int> h_off, h_nm;
@@ -109,6 +112,7 @@ int check_params(merc_ctx* ctx, const merc_params* p) {
   if (p->compat_block < 0) return fail(ctx, MERC_ERR_CONFIG, "compat_block < 0");
   if (p->drift != MERC_DRIFT_ELEMENTS && p->drift != MERC_DRIFT_UNIVERSAL)
     return fail(ctx, MERC_ERR_CONFIG, "unknown drift %d", p->drift);
+  if (p->softening2 > 1.0) return fail(ctx, MERC_ERR_CONFIG, "softening2 > 1 AU^2 is not supported");
   if (p->kepler_max_iter < 1 || p->kepler_max_iter > 1000)
     return fail(ctx, MERC_ERR_CONFIG, "kepler_max_iter out of 1..1000");
   if (p->warm_start != MERC_WARM_PLAIN && p->warm_start != MERC_WARM_MLP)
@@ -185,12 +189,18 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
   }
   const int64_t target_blocks = 4 * (int64_t)dev_sms;
   int max_chunks = 1;
+  std::vector<Work> work_tp;
+  std::vector<SymTask> sym;
+  std::vector<long long> sym_base(n_systems, -1);
+  long long sym_total = 0;
+  ctx->max_big_nm = 0;
   for (int s : big_ids) {
     int ns = (int)(off[s + 1] - off[s]);
     int64_t want = (target_blocks + total_tiles - 1) / std::max<int64_t>(total_tiles, 1);
     int C = (int)std::max<int64_t>(1, std::min<int64_t>(want, (nm[s] + 15) / 16));
     nchunk[s] = C;
     max_chunks = std::max(max_chunks, C);
+    ctx->max_big_nm = std::max(ctx->max_big_nm, (int)nm[s]);
     for (int t0 = 0; t0 < ns; t0 += kTile)
       for (int c = 0; c < C; c++) {
         Work w;
@@ -201,7 +211,24 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
         w.chunk = c;
         work.push_back(w);
       }
+    for (int t0 = nm[s]; t0 < ns; t0 += kTile)
+      for (int c = 0; c < C; c++) {
+        Work w;
+        w.sys = s;
+        w.t0 = (int)off[s] + t0;
+        w.c0 = (int)((int64_t)c * nm[s] / C);
+        w.c1 = (int)((int64_t)(c + 1) * nm[s] / C);
+        w.chunk = c;
+        work_tp.push_back(w);
+      }
+    const int NB = (nm[s] + 31) / 32;
+    for (int I = 0; I < NB; I++)
+      for (int J = I; J < NB; J++) sym.push_back(SymTask{s, I, J});
+    sym_base[s] = sym_total;
+    sym_total += (long long)NB * 3 * nm[s];
   }
+  ctx->n_work_tp = (int)work_tp.size();
+  ctx->n_sym = (int)sym.size();
   ctx->n_work = (int)work.size();
   ctx->n_big = (int)big_ids.size();
   ctx->has_big = !big_ids.empty();
@@ -215,7 +242,9 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
       (st = dalloc(ctx, &ctx->d_work, std::max(1, ctx->n_work))) ||
       (st = dalloc(ctx, &ctx->d_big_ids, std::max(1, ctx->n_big))) ||
       (st = dalloc(ctx, &D.part, ctx->any_multi ? (size_t)max_chunks * 3 * n : 1)) ||
-      (st = dalloc(ctx, &D.ce_list_big, n)))
+      (st = dalloc(ctx, &D.ce_list_big, n)) || (st = dalloc(ctx, &ctx->d_work_tp, std::max(1, ctx->n_work_tp))) ||
+      (st = dalloc(ctx, &ctx->d_sym, std::max(1, ctx->n_sym))) ||
+      (st = dalloc(ctx, &ctx->d_sym_base, n_systems)) || (st = dalloc(ctx, &D.part_sym, std::max<long long>(1, sym_total))))
     return st;
   if ((st = dalloc(ctx, &ctx->d_off, n_systems + 1)) || (st = dalloc(ctx, &ctx->d_nm, n_systems)) ||
       (st = dalloc(ctx, &ctx->d_sys, n)) || (st = dalloc(ctx, &ctx->d_m, n)) || (st = dalloc(ctx, &D.x, 3 * (size_t)n)) ||
@@ -231,6 +260,7 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
   D.m = ctx->d_m;
   D.big = ctx->d_big;
   D.nchunk = ctx->d_nchunk;
+  D.sym_base = ctx->d_sym_base;
   cudaStream_t s = ctx->stream;
   CK(cudaMemcpyAsync(ctx->d_off, ctx->h_off.data(), sizeof(int) * (n_systems + 1), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(ctx->d_nm, nm, sizeof(int) * n_systems, cudaMemcpyHostToDevice, s));
@@ -242,6 +272,10 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
     CK(cudaMemcpyAsync(ctx->d_work, work.data(), sizeof(Work) * ctx->n_work, cudaMemcpyHostToDevice, s));
   if (ctx->n_big)
     CK(cudaMemcpyAsync(ctx->d_big_ids, big_ids.data(), sizeof(int) * ctx->n_big, cudaMemcpyHostToDevice, s));
+  if (ctx->n_work_tp)
+    CK(cudaMemcpyAsync(ctx->d_work_tp, work_tp.data(), sizeof(Work) * ctx->n_work_tp, cudaMemcpyHostToDevice, s));
+  if (ctx->n_sym) CK(cudaMemcpyAsync(ctx->d_sym, sym.data(), sizeof(SymTask) * ctx->n_sym, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ctx->d_sym_base, sym_base.data(), sizeof(long long) * n_systems, cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(D.flags, 0, sizeof(uint32_t) * n, s));
   CK(cudaMemsetAsync(D.ce, 0, n, s));
   CK(cudaMemsetAsync(D.counters, 0, sizeof(unsigned long long) * 4, s));
@@ -306,6 +340,8 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     if ((st = kick_ev(3))) return st;
     nk = 8;
   } else {
+    // the symmetric pair kernels assume a massive body excludes exactly itself
+    const bool use_sym = p.compat_block == 0 || p.compat_block >= ctx->max_big_nm;
     auto kick = [&](const double* rc_in, double* rc_out, int last, int ev) {
       int st2;
       if ((st2 = kick_ev(ev))) return st2;
@@ -314,7 +350,18 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
                                              ej2, last);
         nk++;
       }
-      if (ctx->has_big) {
+      if (ctx->has_big && use_sym) {
+        // massive targets: symmetric block pairs; test particles: tiled
+        k_sym<true><<<ctx->n_sym, 32, 0, s>>>(D, ctx->d_sym, ctx->n_sym, rc_in, p.softening2);
+        nk++;
+        if (ctx->n_work_tp) {
+          k_kick_tiled<<<ctx->n_work_tp, kTile, 0, s>>>(D, ctx->d_work_tp, rc_in, rc_out, hdt, p.softening2,
+                                                        p.compat_block, p.hill_factor, ej2, last);
+          nk++;
+        }
+        k_kick_reduce_sym<<<nb, kThreads, 0, s>>>(D, rc_out, hdt, p.hill_factor, ej2, last);
+        nk++;
+      } else if (ctx->has_big) {
         k_kick_tiled<<<ctx->n_work, kTile, 0, s>>>(D, ctx->d_work, rc_in, rc_out, hdt, p.softening2, p.compat_block,
                                                    p.hill_factor, ej2, last);
         nk++;
@@ -341,8 +388,17 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     nk++;
     if (ctx->has_big) {
       CK(cudaMemsetAsync(D.ce, 0, D.n, s));
-      k_ce_tiled<<<ctx->n_work, kTile, 0, s>>>(D, ctx->d_work, rcB, p.compat_block);
-      nk++;
+      if (use_sym) {
+        k_sym<false><<<ctx->n_sym, 32, 0, s>>>(D, ctx->d_sym, ctx->n_sym, rcB, p.softening2);
+        nk++;
+        if (ctx->n_work_tp) {
+          k_ce_tiled<<<ctx->n_work_tp, kTile, 0, s>>>(D, ctx->d_work_tp, rcB, p.compat_block);
+          nk++;
+        }
+      } else {
+        k_ce_tiled<<<ctx->n_work, kTile, 0, s>>>(D, ctx->d_work, rcB, p.compat_block);
+        nk++;
+      }
     }
     CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
     k_drift_universal<<<nb, kThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.kepler_tol, p.kepler_max_iter);
@@ -352,8 +408,8 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       nk++;
     }
     if (ctx->has_big) {
-      k_encounter_big<<<ctx->enc_blocks, kEncThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
-                                                               p.softening2);
+      k_encounter_cluster<<<ctx->enc_blocks, kEncThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
+                                                                   p.softening2);
       nk++;
     }
     momentum(D.vo);

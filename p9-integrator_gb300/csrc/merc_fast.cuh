@@ -35,11 +35,16 @@ __device__ __forceinline__ int rc2_threshold(double rc) {
 }
 
 // 1 / ((r2 + eps2) sqrt(r2)) from an FP32 seed and one Halley step; valid
-// when (r2 + eps2)^2 r2 is a normal FP32 number (checked by the caller).
+// when (r2 + eps2)^2 r2 is a normal FP32 number (checked by the caller).  The
+// double <-> float moves of the seed are done on the integer pipes from the
+// high word (exponent rebias by 1023 - 127 = 896), so the FP64 pipe only sees
+// the 8 arithmetic operations.
 __device__ __forceinline__ double inv_softened_r3(double r2, double s) {
   double q = s * s;
   q = q * r2;
-  double u = (double)rsqrtf((float)q);
+  float qf = __int_as_float((__double2hiint(q) - 0x38000000) << 3);
+  int yb = __float_as_int(rsqrtf(qf));
+  double u = __hiloint2double((yb >> 3) + 0x38000000, yb << 29);
   double t = q * u;
   double e = fma(-t, u, 1.0);
   double c = fma(0.375, e, 0.5);
@@ -47,11 +52,12 @@ __device__ __forceinline__ double inv_softened_r3(double r2, double s) {
   return fma(ue, c, u);
 }
 
-// is q = (r2 + eps2)^2 r2 inside the FP32 normal range of the seed?
+// is q = (r2 + eps2)^2 r2 inside the FP32 normal range of the seed?  Checked
+// on the high word of r2 (integer compare, positive doubles order like their
+// bits): 2^-36 < r2 < 2^39 keeps q in [2^-108, 2^120] for eps2 <= 1.
 __device__ __forceinline__ bool seed_in_range(double r2) {
-  // r2 in [1e-24, 1e12] keeps q in [~1e-40 .. 1e36] only if eps2 > 0 keeps
-  // s away from zero; the bounds below are conservative for eps2 >= 0.
-  return r2 > 1e-11 && r2 < 1e12;
+  const int h = __double2hiint(r2);
+  return h > 0x3DB00000 && h < 0x42600000;
 }
 
 // Exact pair of the reference (sim.cuh:344-374): weight K or the encounter

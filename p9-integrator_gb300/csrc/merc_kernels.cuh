@@ -12,6 +12,7 @@
 // The element-drift path always uses the exact per-body kernels (reference
 // operation order); the universal path uses the classified fast kernels.
 #pragma once
+#include <cooperative_groups.h>
 
 namespace {
 
@@ -19,7 +20,8 @@ constexpr int kThreads = 128;
 constexpr int kTile = 128;       // targets per work item (one per thread)
 constexpr int kSrcTile = 256;    // sources staged in shared memory per pass
 constexpr int kSmallNm = 32;     // systems with more sources use the tiled kernels
-constexpr int kEncThreads = 128; // threads per encounter body of a big system
+constexpr int kEncThreads = 128; // threads per block of an encounter body of a big system
+constexpr int kEncCluster = 4;   // blocks (a thread-block cluster) per encounter body of a big system
 
 struct Work {
   int sys, t0, c0, c1, chunk;
@@ -43,7 +45,9 @@ struct Dev {
   unsigned char* ce = nullptr;  // encounter flag of the current step
   double* rc[2] = {nullptr, nullptr};  // 4 per body: rc, 0.1 rc, 0.9 rc, fast threshold (massive bodies)
   double* P = nullptr;               // 3 per system
-  double* part = nullptr;            // kick partial sums [chunk][3][n]
+  double* part = nullptr;            // kick partial sums of test-particle targets [chunk][3][n]
+  double* part_sym = nullptr;        // kick partial sums of massive targets, per system [block][3][nm]
+  const long long* sym_base = nullptr;  // per system: offset of its block partials in part_sym (-1: none)
   int* ce_list = nullptr;            // encounter bodies of small systems
   int* ce_list_big = nullptr;        // encounter bodies of big systems
   int* ce_count = nullptr;           // [0] small list, [1] big list
@@ -377,6 +381,188 @@ __global__ void k_kick_reduce(Dev D, double* __restrict__ rc_out, double hdt, do
   kick_epilogue(D, j, j - D.off[s], D.nm[s], pos, vel, rc_out, hill, eject_r2, last);
 }
 
+// ---- symmetric massive-massive interactions of the big systems ----
+// The massive bodies of a big system are cut into blocks of 32.  A warp takes
+// one unordered block pair (I, J), I <= J: lane t keeps target i = 32 I + t and
+// a rotating source j = 32 J + ((t + k) mod 32) that moves one lane per
+// iteration together with its reverse accumulator, so after 32 iterations
+// every lane has met every source and the reverse sums are back home.  Both
+// directions of a pair share d, r^2 and u = 1 / ((r^2 + eps^2) r): 22 FP64
+// operations per unordered pair instead of 2 x 18.  The diagonal block runs
+// k = 1..16 (k = 16 on lanes 0..15 only).  Pairs inside either changeover
+// radius, or outside the seed range, take the reference formula per direction.
+struct SymTask {
+  int sys, I, J;
+};
+
+struct RotSrc {
+  double x, y, z, m;
+  int thr, idx;
+};
+
+__device__ __forceinline__ void rotate(RotSrc& r, d3& acc, bool& flag) {
+  const int src = (threadIdx.x + 1) & 31;
+  r.x = __shfl_sync(0xffffffffu, r.x, src);
+  r.y = __shfl_sync(0xffffffffu, r.y, src);
+  r.z = __shfl_sync(0xffffffffu, r.z, src);
+  r.m = __shfl_sync(0xffffffffu, r.m, src);
+  r.thr = __shfl_sync(0xffffffffu, r.thr, src);
+  r.idx = __shfl_sync(0xffffffffu, r.idx, src);
+  acc.x = __shfl_sync(0xffffffffu, acc.x, src);
+  acc.y = __shfl_sync(0xffffffffu, acc.y, src);
+  acc.z = __shfl_sync(0xffffffffu, acc.z, src);
+  flag = __shfl_sync(0xffffffffu, (int)flag, src) != 0;
+}
+
+// KICK: accumulate accelerations; !KICK: encounter test flags.
+template <bool KICK>
+__global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ tasks, int ntasks,
+                                             const double* __restrict__ rc, double soft2) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= ntasks) return;  // whole warps leave together
+  const int lane = threadIdx.x & 31;
+  const SymTask T = tasks[warp];
+  const int s = T.sys, b0 = D.off[s], nm = D.nm[s];
+  const int i = 32 * T.I + lane;
+  const bool iv = i < nm;
+  RotSrc A, B;
+  A.x = iv ? D.x[b0 + i] : 0.0;
+  A.y = iv ? D.x[D.n + b0 + i] : 0.0;
+  A.z = iv ? D.x[2 * D.n + b0 + i] : 0.0;
+  A.m = iv ? D.m[b0 + i] : 0.0;
+  A.thr = iv ? (int)rc[4 * (size_t)(b0 + i) + 3] : 0x7fffffff;
+  A.idx = i;
+  const int j0 = 32 * T.J + lane;
+  const bool jv0 = j0 < nm;
+  B.x = jv0 ? D.x[b0 + j0] : 0.0;
+  B.y = jv0 ? D.x[D.n + b0 + j0] : 0.0;
+  B.z = jv0 ? D.x[2 * D.n + b0 + j0] : 0.0;
+  B.m = jv0 ? D.m[b0 + j0] : 0.0;
+  B.thr = jv0 ? (int)rc[4 * (size_t)(b0 + j0) + 3] : 0x7fffffff;
+  B.idx = jv0 ? j0 : -1;
+  d3 accA = {0.0, 0.0, 0.0}, accB = {0.0, 0.0, 0.0};
+  bool ceA = false, ceB = false;
+  const bool diag = T.I == T.J;
+  const int kbeg = diag ? 1 : 0, kend = diag ? 16 : 31;
+  int rotations = 0;
+  if (diag) {
+    rotate(B, accB, ceB);
+    rotations++;
+  }
+  for (int k = kbeg; k <= kend; k++) {
+    const bool act = iv && B.idx >= 0 && !(diag && k == 16 && lane >= 16);
+    if (act) {
+      const double dx = B.x - A.x, dy = B.y - A.y, dz = B.z - A.z;
+      const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+      const int h = __double2hiint(r2);
+      if (KICK) {
+        if (h > max(A.thr, B.thr) && seed_in_range(r2)) {
+          const double u = inv_softened_r3(r2, r2 + soft2);
+          const double wa = B.m * u, wb = A.m * u;
+          accA.x = fma(wa, dx, accA.x);
+          accA.y = fma(wa, dy, accA.y);
+          accA.z = fma(wa, dz, accA.z);
+          accB.x = fma(-wb, dx, accB.x);
+          accB.y = fma(-wb, dy, accB.y);
+          accB.z = fma(-wb, dz, accB.z);
+        } else {
+          // reference formula in each direction (self = own index here)
+          const d3 pa = {A.x, A.y, A.z}, pb = {B.x, B.y, B.z};
+          pair_exact<false>(pa, A.idx, B.idx, load_src(D, rc, b0 + B.idx), soft2, accA);
+          pair_exact<false>(pb, B.idx, A.idx, load_src(D, rc, b0 + A.idx), soft2, accB);
+        }
+      } else {
+        // encounter of i with source j uses r_crit(j), of j with i uses r_crit(i)
+        if (h <= B.thr) ceA = ceA || sqrt(r2) < rc[4 * (size_t)(b0 + B.idx)];
+        if (h <= A.thr) ceB = ceB || sqrt(r2) < rc[4 * (size_t)(b0 + A.idx)];
+      }
+    }
+    rotate(B, accB, ceB);
+    rotations++;
+  }
+  // bring the reverse accumulators home: lane t takes from lane t + 32 - R
+  {
+    const int src = (lane + 32 - (rotations & 31)) & 31;
+    accB.x = __shfl_sync(0xffffffffu, accB.x, src);
+    accB.y = __shfl_sync(0xffffffffu, accB.y, src);
+    accB.z = __shfl_sync(0xffffffffu, accB.z, src);
+    ceB = __shfl_sync(0xffffffffu, (int)ceB, src) != 0;
+  }
+  if (KICK) {
+    const size_t stride = 3 * (size_t)nm;
+    double* base = D.part_sym + D.sym_base[s];
+    if (diag) {
+      if (iv) {
+        double* p = base + (size_t)T.I * stride;
+        p[i] = accA.x + accB.x;
+        p[nm + i] = accA.y + accB.y;
+        p[2 * nm + i] = accA.z + accB.z;
+      }
+    } else {
+      if (iv) {
+        double* p = base + (size_t)T.J * stride;  // block I's slot for source block J
+        p[i] = accA.x;
+        p[nm + i] = accA.y;
+        p[2 * nm + i] = accA.z;
+      }
+      if (jv0) {
+        double* p = base + (size_t)T.I * stride;  // block J's slot for source block I
+        p[j0] = accB.x;
+        p[nm + j0] = accB.y;
+        p[2 * nm + j0] = accB.z;
+      }
+    }
+  } else {
+    if (iv && ceA) D.ce[b0 + i] = 1;
+    if (jv0 && ceB) D.ce[b0 + j0] = 1;
+  }
+}
+
+// Kick of every body of a big system whose sums are in partials: massive
+// bodies add their block partials (symmetric kernel) in block order, test
+// particles their chunk partials in chunk order (when there is more than one
+// chunk; a single chunk was applied by the tiled kernel).
+__global__ void k_kick_reduce_sym(Dev D, double* __restrict__ rc_out, double hdt, double hill, double eject_r2,
+                                  int last) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= D.n) return;
+  const int n = D.n, s = D.sys[j];
+  if (!D.big[s]) return;
+  const int b0 = D.off[s], nm = D.nm[s], local = j - b0;
+  d3 acc = {0.0, 0.0, 0.0};
+  if (local < nm) {
+    // four interleaved partial sums (blocks b = 0, 4, 8, ..., 1, 5, ...) added
+    // in a fixed order: independent load/add chains, deterministic result
+    const int NB = (nm + 31) / 32;
+    const double* base = D.part_sym + D.sym_base[s];
+    d3 q[4] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+#pragma unroll 4
+    for (int b = 0; b < NB; b++) {
+      const double* p = base + (size_t)b * 3 * nm;
+      q[b & 3].x += p[local];
+      q[b & 3].y += p[nm + local];
+      q[b & 3].z += p[2 * nm + local];
+    }
+    acc.x = (q[0].x + q[1].x) + (q[2].x + q[3].x);
+    acc.y = (q[0].y + q[1].y) + (q[2].y + q[3].y);
+    acc.z = (q[0].z + q[1].z) + (q[2].z + q[3].z);
+  } else {
+    const int C = D.nchunk[s];
+    if (C <= 1) return;
+    for (int c = 0; c < C; c++) {
+      const double* p = D.part + (size_t)c * 3 * n;
+      acc.x += p[j];
+      acc.y += p[n + j];
+      acc.z += p[2 * n + j];
+    }
+  }
+  d3 pos = load3(D.x, n, j), vel = load3(D.v, n, j);
+  vel.x = fma(acc.x, hdt, vel.x);
+  vel.y = fma(acc.y, hdt, vel.y);
+  vel.z = fma(acc.z, hdt, vel.z);
+  kick_epilogue(D, j, local, nm, pos, vel, rc_out, hill, eject_r2, last);
+}
+
 // Tiled encounter test of the big systems: any source of the chunk within
 // r_crit sets ce[j] (the flags were cleared before the launch).
 __global__ void __launch_bounds__(kTile) k_ce_tiled(Dev D, const Work* __restrict__ work,
@@ -561,6 +747,95 @@ __global__ void __launch_bounds__(kEncThreads) k_encounter_big(Dev D, const doub
     }
     __syncthreads();
   }
+}
+
+// Velocity update of an encounter sub-step split over the blocks of a
+// thread-block cluster: block `rank` sums its quarter of the sources (fixed
+// tree), publishes the partial in its shared memory, and after one cluster
+// barrier every block adds the partials of ranks 0..3 in order through
+// distributed shared memory.  The partial slots are double-buffered by the
+// evaluation parity, so one barrier per evaluation separates the writes of
+// evaluation e+1 from the reads of evaluation e-1.
+struct ClusterVelTotal {
+  const Dev* D;
+  const double* rc;
+  int b0, c0, c1, self;
+  double soft2;
+  double* red;   // shared, 3 * blockDim.x
+  double* slot;  // shared, 2 x 4 doubles (3 used)
+  int* parity;   // per-thread evaluation counter
+  __device__ __forceinline__ d3 operator()(const d3& pos, const d3& vel, double dt) const {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    d3 acc = {0.0, 0.0, 0.0};
+    for (int i = c0 + (int)threadIdx.x; i < c1; i += blockDim.x)
+      pair_fast<true>(pos, self, i, load_src(*D, rc, b0 + i), soft2, acc);
+    const int t = threadIdx.x, B = blockDim.x;
+    __syncthreads();
+    red[t] = acc.x;
+    red[B + t] = acc.y;
+    red[2 * B + t] = acc.z;
+    __syncthreads();
+    for (int w = B / 2; w > 0; w >>= 1) {
+      if (t < w) {
+        red[t] += red[t + w];
+        red[B + t] += red[B + t + w];
+        red[2 * B + t] += red[2 * B + t + w];
+      }
+      __syncthreads();
+    }
+    const int buf = *parity & 1;
+    if (t == 0) {
+      slot[4 * buf] = red[0];
+      slot[4 * buf + 1] = red[B];
+      slot[4 * buf + 2] = red[2 * B];
+    }
+    cl.sync();
+    acc = {0.0, 0.0, 0.0};
+    for (int r = 0; r < kEncCluster; r++) {
+      const double* rs = cl.map_shared_rank(slot, r) + 4 * buf;
+      acc.x += rs[0];
+      acc.y += rs[1];
+      acc.z += rs[2];
+    }
+    (*parity)++;
+    d3 sa = sun_accel(pos, soft2);
+    d3 nv;
+    nv.x = fma(sa.x, dt, fma(acc.x, dt, vel.x));
+    nv.y = fma(sa.y, dt, fma(acc.y, dt, vel.y));
+    nv.z = fma(sa.z, dt, fma(acc.z, dt, vel.z));
+    return nv;
+  }
+};
+
+// Encounter sub-step of the big systems' encounter bodies: one cluster of
+// kEncCluster blocks per body (grid-stride over the list by cluster).  Every
+// thread of the cluster runs the same Richardson scheme, so the cluster
+// barriers inside the velocity updates are reached uniformly.
+__global__ void __cluster_dims__(kEncCluster, 1, 1) __launch_bounds__(kEncThreads)
+    k_encounter_cluster(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, int rows,
+                        double soft2) {
+  namespace cg = cooperative_groups;
+  __shared__ double red[3 * kEncThreads];
+  __shared__ double slot[8];
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int cid = blockIdx.x / kEncCluster, ncl = gridDim.x / kEncCluster;
+  const int count = D.ce_count[1];
+  int parity = 0;
+  for (int k = cid; k < count; k += ncl) {
+    const int j = D.ce_list_big[k];
+    const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
+    const int c0 = (int)((int64_t)rank * nm / kEncCluster), c1 = (int)((int64_t)(rank + 1) * nm / kEncCluster);
+    ClusterVelTotal vt{&D, rc_in, b0, c0, c1, self_index(j - b0, compat_block), soft2, red, slot, &parity};
+    PV c = {load3(D.x, n, j), load3(D.v, n, j)};
+    PV bs = richardson(c, vt, dt, rows);
+    if (rank == 0 && threadIdx.x == 0) {
+      store3(D.xo, n, j, bs.pos);
+      store3(D.vo, n, j, bs.vel);
+    }
+  }
+  cl.sync();  // no block leaves while another may still read its slots
 }
 
 // ---------------------------------------------------------------------------
