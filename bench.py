@@ -189,6 +189,47 @@ def load_traffic():
         return {}
 
 
+def sweep_section(merc, args, local, dist, world, rank):
+    """Batched sweep (workload 2: 4096 uneven systems in one context, every
+    phase one launch over all systems) against the same systems launched one
+    by one (one context, load + steps per system, a timed sample of systems).
+    Replicas: each rank takes a contiguous share of the systems."""
+    full = systems.sweep()
+    share = np.array_split(np.arange(full.n_systems), world)[rank]
+    sysm = full.subset(share)
+    kw = dict(dt=sysm.dt, hill_factor=sysm.hill_factor, drift=merc.DRIFT_UNIVERSAL)
+    g = merc.Integrator(merc.default_params(**kw), device=local)
+    g.load_systems(sysm)
+    g.step(args.warmup)
+    steps = max(3, min(args.steps, 20))
+    ms = 0.0
+    for _ in range(steps):
+        g.step(1)  # state (>100 MB of SoA arrays and scratch) is larger than L2
+        ms += g.stats().last_step_ms
+    ms = max_over_ranks(dist, ms)
+    batched = sum_over_ranks(dist, float(sysm.n_total * steps)) / (ms / 1e3)
+    pairs = sysm.pairs_per_step()
+    g.close()
+    # one by one: a sample of the systems, each loaded and stepped alone
+    sample = sysm.subset(np.linspace(0, sysm.n_systems - 1, 48).astype(int))
+    g1 = merc.Integrator(merc.default_params(**kw), device=local)
+    t_ms, bodies = 0.0, 0
+    for s in range(sample.n_systems):
+        one = sample.subset([s])
+        g1.load_systems(one)
+        g1.step(2)
+        g1.step(steps)
+        t_ms += g1.stats().last_step_ms
+        bodies += one.n_total * steps
+    g1.close()
+    one_by_one = bodies / (t_ms / 1e3)
+    return {"workload": full.label, "systems": int(full.n_systems), "bodies": int(full.n_total),
+            "steps": steps, "batched_body_steps_per_s": batched, "batched_ms_per_step": ms / steps,
+            "batched_pairs_per_s": sum_over_ranks(dist, float(pairs)) * steps / (ms / 1e3),
+            "one_by_one_body_steps_per_s": one_by_one, "one_by_one_sample_systems": int(sample.n_systems),
+            "speedup_vs_one_by_one": batched / one_by_one}
+
+
 def run_ours(args, world, rank, local, dist):
     import merc
 
@@ -259,6 +300,7 @@ def run_ours(args, world, rank, local, dist):
         compat = {"value": n * cs / (gc.stats().last_step_ms / 1e3), "steps": cs, "drift": "elements"}
         gc.close()
     g.close()
+    sweep = None if args.skip_sweep else sweep_section(merc, args, local, dist, world, rank)
 
     if rank != 0:
         return
@@ -283,6 +325,7 @@ def run_ours(args, world, rank, local, dist):
         "close_encounter_body_steps": int(st.ce_body_steps),
         "kepler_mean_iterations": (st.kepler_iterations / st.kepler_solves) if st.kepler_solves else None,
         "compat_elements_path": compat,
+        "sweep": sweep,
     }
     print(json.dumps(line), flush=True)
 
@@ -295,6 +338,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-compat", action="store_true")
+    ap.add_argument("--skip-sweep", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -150,6 +150,27 @@ int merc_energy(merc_ctx* ctx, double* energy);
 /* Number of kernel launches issued by this context since creation. */
 int64_t merc_launch_count(const merc_ctx* ctx);
 
+/* ---- learned warm start of the universal-variable drift ----
+ * No counterpart in the reference (its Kepler solve starts at E = M,
+ * src/sim.cuh:93).  A 4 -> 32 -> 32 -> 1 SiLU network in FP32 predicts the
+ * universal anomaly from the drift inputs; the FP64 Newton solve that follows
+ * is unchanged.  Parameters: a blob of MERC_MLP_BLOB floats (network, input and
+ * output normalisation, feature box). */
+#define MERC_MLP_BLOB 1267
+
+/* Log (features, target) of every universal drift solve into a device buffer
+ * of `capacity` samples (0 turns logging off). */
+int merc_mlp_log(merc_ctx* ctx, int64_t capacity);
+int64_t merc_mlp_log_count(merc_ctx* ctx);
+/* Copy up to max_samples logged samples (5 floats each: x1, x2, x3, x4, target). */
+int merc_mlp_get_log(merc_ctx* ctx, float* out, int64_t max_samples);
+/* Train the network on the logged samples on the GPU (hand-written forward,
+ * backward and Adam kernels, minibatches drawn by a seeded hash), epochs x
+ * (samples / batch) steps.  loss_per_epoch (may be NULL): epochs floats. */
+int merc_mlp_train(merc_ctx* ctx, int32_t epochs, int32_t batch, float lr, uint64_t seed, float* loss_per_epoch);
+int merc_mlp_set_weights(merc_ctx* ctx, const float* blob);
+int merc_mlp_get_weights(merc_ctx* ctx, float* blob);
+
 /* Bytes of the fixed device scratch array behind merc_step_static. */
 #define MERC_STATIC_SCRATCH_BYTES (16u << 20)
 

@@ -24,6 +24,16 @@ int merc_diag_math(int device, int fn, int64_t n, const double* x, const double*
  * three runs of a register-resident FMA loop over 4 blocks per SM. */
 int merc_diag_fp64_peak(int device, double* tflops);
 
+/* Loss and gradient of the warm-start network on n samples (5 floats each,
+ * as logged) with parameter blob `blob` (MERC_MLP_BLOB floats): loss = mean of
+ * 0.5 (net - target)^2 in normalised units; grad: the 1249 network parameters. */
+int merc_diag_mlp_grad(int device, int64_t n, const float* samples, const float* blob, float* loss, float* grad);
+
+/* Warm-start guess and FP64 solve for n drift inputs (pos/vel 3 x n,
+ * component-major): blob NULL gives the plain guess dt / r0. */
+int merc_diag_warm_start(int device, int64_t n, const double* pos, const double* vel, double dt, const float* blob,
+                         double tol, int32_t max_iter, double* guess, double* solved, int32_t* iters);
+
 /* Write `bytes` of a scratch buffer on the context's stream (evicts L2 between
  * timed steps) and wait for it. */
 int merc_diag_flush_l2(merc_ctx* ctx, int64_t bytes);

@@ -364,12 +364,15 @@ template <class R> inline void stumpff(R z, R* c0, R* c1, R* c2, R* c3) {
   *c0 = s0; *c1 = s1; *c2 = s2; *c3 = s3;
 }
 
-template <class R> struct UDrift { PV<R> out; int iters; bool converged; };
+template <class R> struct UDrift { PV<R> out; int iters; bool converged; R s; };
 
 // Universal-variable Kepler drift with mu = 1: solve
 //   r0 s + eta G2(s) + zeta G3(s) = dt,  G_k = s^k c_k(alpha s^2),
-// alpha = 2/r0 - v0^2, eta = x0.v0, zeta = 1 - alpha r0, by Newton from s0,
-// stop when |ds| <= tol |s|, then the f and g functions at the final s.
+// alpha = 2/r0 - v0^2, eta = x0.v0, zeta = 1 - alpha r0, by Newton from s0.
+// Stopping rule: after the update s += ds, the Newton error estimate of the
+// new s is |f''/(2 f')| ds^2; stop when it is <= tol |s| (and |ds| <= 1e-3 |s|,
+// so the estimate is only trusted in the quadratic regime).  The f and g
+// functions are then evaluated at the final s.
 template <class R>
 UDrift<R> universal_drift(const V3<R>& x0, const V3<R>& v0, R dt, R s0, R tol, int max_iter) {
   R r0 = std::sqrt(mag2(x0));
@@ -388,10 +391,15 @@ UDrift<R> universal_drift(const V3<R>& x0, const V3<R>& v0, R dt, R s0, R tol, i
     R G1 = s * c1, G2 = s2 * c2, G3 = s2 * s * c3;
     R f = std::fma(r0, s, std::fma(eta, G2, std::fma(zeta, G3, -dt)));
     R fp = std::fma(eta, G1, std::fma(zeta, G2, r0));
+    R fpp = std::fma(eta, c0, zeta * G1);
     R ds = -f / fp;
     s = s + ds;
     it++;
-    if (std::fabs(ds) <= tol * std::fabs(s)) { conv = true; break; }
+    R as = std::fabs(s);
+    if (std::fabs(ds) <= R(1e-3) * as && std::fabs(fpp * ds * ds) <= R(2) * tol * as * std::fabs(fp)) {
+      conv = true;
+      break;
+    }
   }
   R s2 = s * s;
   stumpff(alpha * s2, &c0, &c1, &c2, &c3);
@@ -407,6 +415,7 @@ UDrift<R> universal_drift(const V3<R>& x0, const V3<R>& v0, R dt, R s0, R tol, i
   u.out.vel = {std::fma(fd, x0.x, gd * v0.x), std::fma(fd, x0.y, gd * v0.y), std::fma(fd, x0.z, gd * v0.z)};
   u.iters = it;
   u.converged = conv;
+  u.s = s;
   return u;
 }
 

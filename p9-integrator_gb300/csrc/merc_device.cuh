@@ -344,10 +344,13 @@ struct UD {
   PV out;
   int iters;
   bool converged;
+  double s;  // converged universal anomaly
 };
 
 // Universal Kepler drift with mu = 1 from initial guess s0: Newton on
-// r0 s + eta G2 + zeta G3 = dt, stop when |ds| <= tol |s|, f and g at the final s.
+// r0 s + eta G2 + zeta G3 = dt; after each update the Newton error estimate
+// |f''/(2 f')| ds^2 of the new s is compared with tol |s| (trusted once
+// |ds| <= 1e-3 |s|); f and g at the final s.
 __device__ __forceinline__ UD universal_drift(const d3& x0, const d3& v0, double dt, double s0, double tol,
                                               int max_iter) {
   double r0 = sqrt(mag2(x0));
@@ -366,10 +369,12 @@ __device__ __forceinline__ UD universal_drift(const d3& x0, const d3& v0, double
     double G1 = s * c1, G2 = s2 * c2, G3 = s2 * s * c3;
     double f = fma(r0, s, fma(eta, G2, fma(zeta, G3, -dt)));
     double fp = fma(eta, G1, fma(zeta, G2, r0));
+    double fpp = fma(eta, c0, zeta * G1);
     double ds = -f / fp;
     s = s + ds;
     it++;
-    if (fabs(ds) <= tol * fabs(s)) {
+    double as = fabs(s);
+    if (fabs(ds) <= 1e-3 * as && fabs(fpp * ds * ds) <= 2.0 * tol * as * fabs(fp)) {
       conv = true;
       break;
     }
@@ -388,6 +393,7 @@ __device__ __forceinline__ UD universal_drift(const d3& x0, const d3& v0, double
   u.out.vel = {fma(fd, x0.x, gd * v0.x), fma(fd, x0.y, gd * v0.y), fma(fd, x0.z, gd * v0.z)};
   u.iters = it;
   u.converged = conv;
+  u.s = s;
   return u;
 }
 

@@ -41,6 +41,7 @@
 
 using namespace merc;
 
+#include "merc_mlp.cuh"
 #include "merc_kernels.cuh"
 
 // ---------------------------------------------------------------------------
@@ -82,6 +83,12 @@ struct merc_ctx {
   int64_t steps_done = 0;
   int64_t launches = 0;
   int kernels_per_step = 0;
+  // learned warm start: parameter blob, drift log, training state
+  float* d_mlp = nullptr;
+  bool mlp_ready = false;
+  float* d_log = nullptr;
+  unsigned long long* d_log_count = nullptr;
+  long long log_cap = 0;
   double last_ms = 0.0;
 };
 
@@ -401,7 +408,9 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       }
     }
     CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
-    k_drift_universal<<<nb, kThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.kepler_tol, p.kepler_max_iter);
+    const float* mlp = (p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) ? ctx->d_mlp : nullptr;
+    k_drift_universal<<<nb, kThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.kepler_tol, p.kepler_max_iter, mlp,
+                                              ctx->d_log, ctx->d_log_count, ctx->log_cap);
     nk++;
     if (ctx->has_small) {
       k_encounter_small<<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2);
@@ -518,6 +527,9 @@ int merc_destroy(merc_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   free_all(ctx);
   if (ctx->flush_buf) cudaFree(ctx->flush_buf);
+  if (ctx->d_mlp) cudaFree(ctx->d_mlp);
+  if (ctx->d_log) cudaFree(ctx->d_log);
+  if (ctx->d_log_count) cudaFree(ctx->d_log_count);
   for (cudaEvent_t e : ctx->kick_ev) cudaEventDestroy(e);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -735,6 +747,269 @@ int merc_energy(merc_ctx* ctx, double* energy) {
 
 int64_t merc_launch_count(const merc_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
+// ---- learned warm start ----
+int merc_mlp_log(merc_ctx* ctx, int64_t capacity) {
+  if (!ctx || capacity < 0) return MERC_ERR_CONFIG;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->d_log) cudaFree(ctx->d_log);
+  ctx->d_log = nullptr;
+  ctx->log_cap = 0;
+  if (!ctx->d_log_count) CK(cudaMalloc(&ctx->d_log_count, sizeof(unsigned long long)));
+  CK(cudaMemset(ctx->d_log_count, 0, sizeof(unsigned long long)));
+  if (capacity > 0) {
+    CK(cudaMalloc(&ctx->d_log, sizeof(float) * 5 * (size_t)capacity));
+    ctx->log_cap = capacity;
+  }
+  drop_graphs(ctx);  // the graphs hold the log pointer
+  return MERC_OK;
+}
+
+int64_t merc_mlp_log_count(merc_ctx* ctx) {
+  if (!ctx || !ctx->d_log_count) return 0;
+  unsigned long long c = 0;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return 0;
+  cudaStreamSynchronize(ctx->stream);
+  if (cudaMemcpy(&c, ctx->d_log_count, sizeof c, cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+  return (int64_t)std::min<unsigned long long>(c, (unsigned long long)ctx->log_cap);
+}
+
+int merc_mlp_get_log(merc_ctx* ctx, float* out, int64_t max_samples) {
+  if (!ctx || !out || max_samples < 0) return MERC_ERR_CONFIG;
+  int64_t n = std::min<int64_t>(merc_mlp_log_count(ctx), max_samples);
+  if (n > 0) CK(cudaMemcpy(out, ctx->d_log, sizeof(float) * 5 * (size_t)n, cudaMemcpyDeviceToHost));
+  return MERC_OK;
+}
+
+int merc_mlp_set_weights(merc_ctx* ctx, const float* w) {
+  if (!ctx || !w) return MERC_ERR_CONFIG;
+  CK(cudaSetDevice(ctx->device));
+  if (!ctx->d_mlp) CK(cudaMalloc(&ctx->d_mlp, sizeof(float) * kBlob));
+  CK(cudaMemcpy(ctx->d_mlp, w, sizeof(float) * kBlob, cudaMemcpyHostToDevice));
+  ctx->mlp_ready = true;
+  drop_graphs(ctx);
+  return MERC_OK;
+}
+
+int merc_mlp_get_weights(merc_ctx* ctx, float* w) {
+  if (!ctx || !w) return MERC_ERR_CONFIG;
+  if (!ctx->mlp_ready) return fail(ctx, MERC_ERR_STATE, "no warm-start network: train or set weights first");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpy(w, ctx->d_mlp, sizeof(float) * kBlob, cudaMemcpyDeviceToHost));
+  return MERC_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Train the network on device data (5 floats per sample) with the
+// hand-written kernels: k_mlp_grad -> k_mlp_reduce -> k_mlp_adam per batch.
+int train_on(merc_ctx* ctx, int device, float* d_blob, const float* d_data, long long n_data, int epochs, int batch,
+             float lr, unsigned long long seed, float* loss_out) {
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const int nblocks = std::max(1, std::min(2 * sms, (batch + kMlpThreads - 1) / kMlpThreads));
+  float *part = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
+  CK(cudaMalloc(&part, sizeof(float) * (size_t)nblocks * (kNet + 1)));
+  CK(cudaMalloc(&grad, sizeof(float) * (kNet + 1)));
+  CK(cudaMalloc(&m, sizeof(float) * kNet));
+  CK(cudaMalloc(&v, sizeof(float) * kNet));
+  CK(cudaMemset(m, 0, sizeof(float) * kNet));
+  CK(cudaMemset(v, 0, sizeof(float) * kNet));
+  const long long steps_per_epoch = std::max<long long>(1, n_data / batch);
+  int step = 0;
+  float lossv = 0.f;
+  for (int ep = 0; ep < epochs; ep++) {
+    double esum = 0.0;
+    // cosine decay of the learning rate over the epochs
+    const float lr_ep = lr * 0.5f * (1.0f + cosf(3.14159265f * ep / std::max(1, epochs)));
+    for (long long st = 0; st < steps_per_epoch; st++) {
+      step++;
+      k_mlp_grad<<<nblocks, kMlpThreads, 0, ctx ? ctx->stream : 0>>>(d_blob, d_data, n_data, nullptr, batch,
+                                                                     seed + 0x632BE59BD9B4E019ull * step, part);
+      k_mlp_reduce<<<(kNet + 1 + 127) / 128, 128, 0, ctx ? ctx->stream : 0>>>(part, nblocks, batch, grad);
+      k_mlp_adam<<<(kNet + 127) / 128, 128, 0, ctx ? ctx->stream : 0>>>(d_blob, grad, m, v, lr_ep, 0.9f, 0.999f,
+                                                                        1e-8f, step);
+      if (st == steps_per_epoch - 1 || (st & 63) == 0) {
+        CK(cudaMemcpyAsync(&lossv, grad + kNet, sizeof(float), cudaMemcpyDeviceToHost, ctx ? ctx->stream : 0));
+        CK(cudaStreamSynchronize(ctx ? ctx->stream : 0));
+        esum = lossv;
+      }
+    }
+    CK(cudaGetLastError());
+    if (loss_out) loss_out[ep] = (float)esum;
+  }
+  cudaFree(part);
+  cudaFree(grad);
+  cudaFree(m);
+  cudaFree(v);
+  return MERC_OK;
+}
+
+// normalisation and feature box of a sample set (host side, double sums)
+void fit_normalisation(const std::vector<float>& h, long long n, float* blob) {
+  double mean[5] = {0, 0, 0, 0, 0}, sq[5] = {0, 0, 0, 0, 0};
+  float lo[4], hi[4];
+  for (int k = 0; k < 4; k++) {
+    lo[k] = 3.4e38f;
+    hi[k] = -3.4e38f;
+  }
+  for (long long i = 0; i < n; i++)
+    for (int k = 0; k < 5; k++) {
+      double x = h[5 * i + k];
+      mean[k] += x;
+      sq[k] += x * x;
+      if (k < 4) {
+        lo[k] = std::min(lo[k], h[5 * i + k]);
+        hi[k] = std::max(hi[k], h[5 * i + k]);
+      }
+    }
+  for (int k = 0; k < 5; k++) {
+    mean[k] /= (double)n;
+    double var = std::max(sq[k] / (double)n - mean[k] * mean[k], 1e-30);
+    double sc = 1.0 / std::sqrt(var);
+    if (k < 4) {
+      blob[kInMean + k] = (float)mean[k];
+      blob[kInScale + k] = (float)std::min(sc, 1e6);
+      blob[kBoxLo + k] = lo[k];
+      blob[kBoxHi + k] = hi[k];
+    } else {
+      blob[kOutMean] = (float)mean[k];
+      blob[kOutScale] = (float)std::min(sc, 1e12);
+    }
+  }
+  // the sign feature is +-1: keep it as it is
+  blob[kInMean + 3] = 0.0f;
+  blob[kInScale + 3] = 1.0f;
+  blob[kBoxLo + 3] = -1.0f;
+  blob[kBoxHi + 3] = 1.0f;
+}
+
+void init_weights(float* blob, unsigned long long seed) {
+  unsigned long long z = seed ^ 0x2545F4914F6CDD1Dull;
+  auto uni = [&]() {  // xorshift64*
+    z ^= z >> 12;
+    z ^= z << 25;
+    z ^= z >> 27;
+    return (double)((z * 0x2545F4914F6CDD1Dull) >> 11) * (1.0 / 9007199254740992.0);
+  };
+  auto fill = [&](int off, int count, double bound) {
+    for (int k = 0; k < count; k++) blob[off + k] = (float)((2.0 * uni() - 1.0) * bound);
+  };
+  fill(kW1, kH * 4, std::sqrt(6.0 / (4 + kH)));
+  fill(kB1, kH, 0.0);
+  fill(kW2, kH * kH, std::sqrt(6.0 / (kH + kH)));
+  fill(kB2, kH, 0.0);
+  fill(kW3, kH, std::sqrt(6.0 / (kH + 1)));
+  blob[kB3] = 0.0f;
+}
+
+}  // namespace
+
+extern "C" {
+
+int merc_mlp_train(merc_ctx* ctx, int32_t epochs, int32_t batch, float lr, uint64_t seed, float* loss_per_epoch) {
+  if (!ctx || epochs < 1 || batch < 32 || !(lr > 0.f)) return MERC_ERR_CONFIG;
+  const long long n = merc_mlp_log_count(ctx);
+  if (n < 1024) return fail(ctx, MERC_ERR_STATE, "warm-start training needs logged drifts (have %lld)", n);
+  CK(cudaSetDevice(ctx->device));
+  std::vector<float> h((size_t)5 * n);
+  CK(cudaMemcpy(h.data(), ctx->d_log, sizeof(float) * 5 * (size_t)n, cudaMemcpyDeviceToHost));
+  std::vector<float> blob(kBlob, 0.f);
+  fit_normalisation(h, n, blob.data());
+  init_weights(blob.data(), seed);
+  if (!ctx->d_mlp) CK(cudaMalloc(&ctx->d_mlp, sizeof(float) * kBlob));
+  CK(cudaMemcpy(ctx->d_mlp, blob.data(), sizeof(float) * kBlob, cudaMemcpyHostToDevice));
+  int st = train_on(ctx, ctx->device, ctx->d_mlp, ctx->d_log, n, epochs, batch, lr, seed, loss_per_epoch);
+  if (st) return st;
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->mlp_ready = true;
+  drop_graphs(ctx);
+  return MERC_OK;
+}
+
+int merc_diag_mlp_grad(int device, int64_t n, const float* samples, const float* blob, float* loss, float* grad) {
+  merc_ctx* ctx = nullptr;
+  if (n <= 0 || !samples || !blob || !grad) return MERC_ERR_CONFIG;
+  CK(cudaSetDevice(device));
+  float *d_s = nullptr, *d_b = nullptr, *d_part = nullptr, *d_g = nullptr;
+  long long* d_idx = nullptr;
+  std::vector<long long> idx(n);
+  for (int64_t i = 0; i < n; i++) idx[i] = i;
+  const int nblocks = (int)std::min<int64_t>(8, (n + kMlpThreads - 1) / kMlpThreads);
+  CK(cudaMalloc(&d_s, sizeof(float) * 5 * n));
+  CK(cudaMalloc(&d_b, sizeof(float) * kBlob));
+  CK(cudaMalloc(&d_idx, sizeof(long long) * n));
+  CK(cudaMalloc(&d_part, sizeof(float) * nblocks * (kNet + 1)));
+  CK(cudaMalloc(&d_g, sizeof(float) * (kNet + 1)));
+  CK(cudaMemcpy(d_s, samples, sizeof(float) * 5 * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_b, blob, sizeof(float) * kBlob, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_idx, idx.data(), sizeof(long long) * n, cudaMemcpyHostToDevice));
+  k_mlp_grad<<<nblocks, kMlpThreads>>>(d_b, d_s, n, d_idx, (int)n, 0, d_part);
+  k_mlp_reduce<<<(kNet + 1 + 127) / 128, 128>>>(d_part, nblocks, (int)n, d_g);
+  CK(cudaGetLastError());
+  std::vector<float> g(kNet + 1);
+  CK(cudaMemcpy(g.data(), d_g, sizeof(float) * (kNet + 1), cudaMemcpyDeviceToHost));
+  memcpy(grad, g.data(), sizeof(float) * kNet);
+  if (loss) *loss = g[kNet];
+  cudaFree(d_s);
+  cudaFree(d_b);
+  cudaFree(d_idx);
+  cudaFree(d_part);
+  cudaFree(d_g);
+  return MERC_OK;
+}
+
+// Evaluate the warm-start guess for n drift inputs on the GPU (diagnostic):
+// pos/vel 3 x n component-major, returns s_guess (n) and, if s_solved is
+// given, the converged s and iterations of the solve from that guess.
+__global__ void k_mlp_probe(int n, const double* pos, const double* vel, double dt, const float* blob, double tol,
+                            int max_iter, double* guess, double* solved, int* iters) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  d3 x = {pos[j], pos[n + j], pos[2 * n + j]}, v = {vel[j], vel[n + j], vel[2 * n + j]};
+  WarmIn w = warm_features(x, v, dt);
+  double s0 = (blob && w.f[0] >= kWarmMinX1) ? warm_guess(blob, w) : w.s0;
+  guess[j] = s0;
+  UD u = universal_drift(x, v, dt, s0, tol, max_iter);
+  solved[j] = u.s;
+  iters[j] = u.iters;
+}
+
+int merc_diag_warm_start(int device, int64_t n, const double* pos, const double* vel, double dt, const float* blob,
+                         double tol, int32_t max_iter, double* guess, double* solved, int32_t* iters) {
+  merc_ctx* ctx = nullptr;
+  if (n <= 0 || !pos || !vel || !guess || !solved || !iters) return MERC_ERR_CONFIG;
+  CK(cudaSetDevice(device));
+  double *dp, *dv, *dg, *ds;
+  int* di;
+  float* db = nullptr;
+  CK(cudaMalloc(&dp, sizeof(double) * 3 * n));
+  CK(cudaMalloc(&dv, sizeof(double) * 3 * n));
+  CK(cudaMalloc(&dg, sizeof(double) * n));
+  CK(cudaMalloc(&ds, sizeof(double) * n));
+  CK(cudaMalloc(&di, sizeof(int) * n));
+  if (blob) {
+    CK(cudaMalloc(&db, sizeof(float) * kBlob));
+    CK(cudaMemcpy(db, blob, sizeof(float) * kBlob, cudaMemcpyHostToDevice));
+  }
+  CK(cudaMemcpy(dp, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dv, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice));
+  k_mlp_probe<<<(unsigned)((n + 127) / 128), 128>>>((int)n, dp, dv, dt, db, tol, max_iter, dg, ds, di);
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(guess, dg, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(solved, ds, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(iters, di, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  cudaFree(dp);
+  cudaFree(dv);
+  cudaFree(dg);
+  cudaFree(ds);
+  cudaFree(di);
+  if (db) cudaFree(db);
+  return MERC_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -911,7 +1186,8 @@ extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodi
       k_ce_tiled<<<(unsigned)work.size(), kTile, 0, s>>>(D, d_work, rcB, p->compat_block);
     }
     CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
-    k_drift_universal<<<nb, kThreads, 0, s>>>(D, rcB, p->dt, p->compat_block, p->kepler_tol, p->kepler_max_iter);
+    k_drift_universal<<<nb, kThreads, 0, s>>>(D, rcB, p->dt, p->compat_block, p->kepler_tol, p->kepler_max_iter,
+                                              nullptr, nullptr, nullptr, 0);
     if (!big)
       k_encounter_small<<<sms * 4, 64, 0, s>>>(D, rcB, p->dt, p->compat_block, p->bs_rows, p->softening2);
     else

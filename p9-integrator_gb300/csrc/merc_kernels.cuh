@@ -620,12 +620,24 @@ __global__ void k_momentum_big(Dev D, const int* __restrict__ big_ids, const dou
 
 // Encounter test (small systems inline, big systems from ce[]) and universal
 // drift of every body not in encounter; encounter bodies go to the lists.
+// mlp != nullptr: learned warm start of the solve (merc_mlp.cuh).  log_data
+// != nullptr: every solve with x1 >= kWarmMinX1 appends its features and
+// training target (5 floats) while the log has room.
+constexpr float kWarmMinX1 = 1e-5f;
+
 __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, double tol,
-                                  int max_iter) {
+                                  int max_iter, const float* __restrict__ mlp, float* __restrict__ log_data,
+                                  unsigned long long* __restrict__ log_count, long long log_cap) {
+  __shared__ float blob[kBlob];
+  if (mlp) {
+    for (int k = threadIdx.x; k < kBlob; k += blockDim.x) blob[k] = mlp[k];
+    __syncthreads();
+  }
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
-  bool ce_small = false, ce_big = false;
+  bool ce_small = false, ce_big = false, logit = false;
   int its = 0, nonconv = 0, solved = 0;
+  float rec[5];
   if (j < D.n) {
     const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
     d3 pos = load3(D.x, n, j);
@@ -642,17 +654,39 @@ __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, doubl
     }
     if (!is_ce) {
       d3 vel = load3(D.v, n, j);
-      double s0 = dt / sqrt(mag2(pos));
+      WarmIn w = warm_features(pos, vel, dt);
+      double s0 = w.s0;
+      if (mlp && w.f[0] >= kWarmMinX1) s0 = warm_guess(blob, w);
       UD u = universal_drift(pos, vel, dt, s0, tol, max_iter);
       store3(D.xo, n, j, u.out.pos);
       store3(D.vo, n, j, u.out.vel);
       its = u.iters;
       nonconv = !u.converged;
       solved = 1;
+      if (log_data && u.converged && w.f[0] >= kWarmMinX1) {
+        logit = true;
+        rec[0] = w.f[0];
+        rec[1] = w.f[1];
+        rec[2] = w.f[2];
+        rec[3] = w.f[3];
+        rec[4] = warm_target(w, u.s);
+      }
     }
   }
   append_ce(ce_small, j, D.ce_list, &D.ce_count[0], &D.counters[0]);
   append_ce(ce_big, j, D.ce_list_big, &D.ce_count[1], &D.counters[0]);
+  if (log_data) {
+    unsigned mask = __ballot_sync(0xffffffffu, logit);
+    if (mask) {
+      int leader = __ffs(mask) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(log_count, (unsigned long long)__popc(mask));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      unsigned long long slot = base + __popc(mask & ((1u << lane) - 1u));
+      if (logit && slot < (unsigned long long)log_cap)
+        for (int k = 0; k < 5; k++) log_data[5 * slot + k] = rec[k];
+    }
+  }
   int wits = __reduce_add_sync(0xffffffffu, its);
   int wsol = __reduce_add_sync(0xffffffffu, solved);
   int wnc = __reduce_add_sync(0xffffffffu, nonconv);

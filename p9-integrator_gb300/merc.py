@@ -110,6 +110,17 @@ def lib() -> C.CDLL:
     L.merc_launch_count.restype = C.c_int64
     L.merc_step_static.argtypes = [C.c_int, C.POINTER(MercParams), C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+    _f32p = C.POINTER(C.c_float)
+    L.merc_mlp_log.argtypes = [vp, C.c_int64]
+    L.merc_mlp_log_count.argtypes = [vp]
+    L.merc_mlp_log_count.restype = C.c_int64
+    L.merc_mlp_get_log.argtypes = [vp, _f32p, C.c_int64]
+    L.merc_mlp_train.argtypes = [vp, C.c_int32, C.c_int32, C.c_float, C.c_uint64, _f32p]
+    L.merc_mlp_set_weights.argtypes = [vp, _f32p]
+    L.merc_mlp_get_weights.argtypes = [vp, _f32p]
+    L.merc_diag_mlp_grad.argtypes = [C.c_int, C.c_int64, _f32p, _f32p, _f32p, _f32p]
+    L.merc_diag_warm_start.argtypes = [C.c_int, C.c_int64, _f64p, _f64p, C.c_double, _f32p, C.c_double, C.c_int32,
+                                       _f64p, _f64p, _i32p]
     L.merc_diag_math.argtypes = [C.c_int, C.c_int, C.c_int64, _f64p, _f64p, _f64p]
     L.merc_diag_fp64_peak.argtypes = [C.c_int, _f64p]
     L.merc_diag_time_kicks.argtypes = [vp, C.c_int]
@@ -237,6 +248,35 @@ class Integrator:
     def launch_count(self) -> int:
         return int(self.L.merc_launch_count(self.h))
 
+    # ---- learned warm start ----
+    def mlp_log(self, capacity: int):
+        self._check(self.L.merc_mlp_log(self.h, int(capacity)))
+
+    def mlp_log_count(self) -> int:
+        return int(self.L.merc_mlp_log_count(self.h))
+
+    def mlp_get_log(self, max_samples: int | None = None) -> np.ndarray:
+        n = self.mlp_log_count() if max_samples is None else int(max_samples)
+        out = np.zeros(5 * n, np.float32)
+        self._check(self.L.merc_mlp_get_log(self.h, out.ctypes.data_as(C.POINTER(C.c_float)), n))
+        return out.reshape(-1, 5)
+
+    def mlp_train(self, epochs=20, batch=8192, lr=3e-3, seed=1):
+        loss = np.zeros(epochs, np.float32)
+        self._check(self.L.merc_mlp_train(self.h, int(epochs), int(batch), float(lr), int(seed),
+                                          loss.ctypes.data_as(C.POINTER(C.c_float))))
+        return loss
+
+    def mlp_weights(self) -> np.ndarray:
+        w = np.zeros(MLP_BLOB, np.float32)
+        self._check(self.L.merc_mlp_get_weights(self.h, w.ctypes.data_as(C.POINTER(C.c_float))))
+        return w
+
+    def mlp_set_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        assert w.size == MLP_BLOB
+        self._check(self.L.merc_mlp_set_weights(self.h, w.ctypes.data_as(C.POINTER(C.c_float))))
+
     def time_kicks(self, on: bool = True):
         self._check(self.L.merc_diag_time_kicks(self.h, 1 if on else 0))
 
@@ -245,6 +285,42 @@ class Integrator:
         cnt = C.c_int32()
         self._check(self.L.merc_diag_kick_ms(self.h, C.byref(ms), C.byref(cnt)))
         return ms.value, cnt.value
+
+
+MLP_BLOB = 1267
+
+
+def mlp_grad(samples, blob, device: int = 0):
+    """GPU loss and gradient of the warm-start network (diagnostic)."""
+    L = lib()
+    f32 = C.POINTER(C.c_float)
+    s = np.ascontiguousarray(samples, np.float32).reshape(-1)
+    b = np.ascontiguousarray(blob, np.float32)
+    g = np.zeros(MLP_BLOB - 18, np.float32)
+    loss = C.c_float()
+    st = L.merc_diag_mlp_grad(device, s.size // 5, s.ctypes.data_as(f32), b.ctypes.data_as(f32), C.byref(loss),
+                              g.ctypes.data_as(f32))
+    if st:
+        raise MercError(st, "merc_diag_mlp_grad failed")
+    return loss.value, g
+
+
+def warm_start_probe(pos, vel, dt, blob=None, tol=1e-13, max_iter=30, device: int = 0):
+    """GPU warm-start guess, converged s and Newton iterations for drift inputs."""
+    L = lib()
+    pos = _f64(pos)
+    vel = _f64(vel)
+    n = pos.size // 3
+    g = np.zeros(n)
+    s = np.zeros(n)
+    it = np.zeros(n, np.int32)
+    b = np.ascontiguousarray(blob, np.float32) if blob is not None else None
+    st = L.merc_diag_warm_start(device, n, _p(pos, _f64p), _p(vel, _f64p), dt,
+                                b.ctypes.data_as(C.POINTER(C.c_float)) if b is not None else None, tol, max_iter,
+                                _p(g, _f64p), _p(s, _f64p), _p(it, _i32p))
+    if st:
+        raise MercError(st, "merc_diag_warm_start failed")
+    return g, s, it
 
 
 MM_FUNCS = {"sin": 0, "cos": 1, "atan2": 2, "acos": 3, "log": 4, "sinh": 5, "cosh": 6, "cbrt": 7, "exp": 8}

@@ -159,10 +159,14 @@ def test_universal_drift_vs_kepler_equation(oracle):
         dt = period * rng.choice([1e-4, 1e-2, 0.3])
         cases.append((pos, vel, dt))
     for pos, vel, dt in cases:
-        po, vo, its = oracle.universal(pos, vel, dt)
         rp, rv = kepler_reference(pos, vel, dt)
+        # converged to machine precision (tol 1e-16): agrees to ~1e-13
+        po, vo, its = oracle.universal(pos, vel, dt, tol=1e-16)
         assert np.max(np.abs(po - rp)) <= 1e-13 * np.linalg.norm(rp), (dt, its)
         assert np.max(np.abs(vo - rv)) <= 1e-13 * np.linalg.norm(rv)
+        # at the default tolerance (1e-13 on the Newton error estimate of s)
+        po, vo, its = oracle.universal(pos, vel, dt)
+        assert np.max(np.abs(po - rp)) <= 1e-12 * np.linalg.norm(rp), (dt, its)
 
 
 def test_stumpff_closed_forms(oracle):
