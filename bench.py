@@ -195,8 +195,7 @@ def sweep_section(merc, args, local, dist, world, rank):
     by one (one context, load + steps per system, a timed sample of systems).
     Replicas: each rank takes a contiguous share of the systems."""
     full = systems.sweep()
-    share = np.array_split(np.arange(full.n_systems), world)[rank]
-    sysm = full.subset(share)
+    sysm = systems.shard(full, rank, world)
     kw = dict(dt=sysm.dt, hill_factor=sysm.hill_factor, drift=merc.DRIFT_UNIVERSAL)
     g = merc.Integrator(merc.default_params(**kw), device=local)
     g.load_systems(sysm)
@@ -228,6 +227,57 @@ def sweep_section(merc, args, local, dist, world, rank):
             "batched_pairs_per_s": sum_over_ranks(dist, float(pairs)) * steps / (ms / 1e3),
             "one_by_one_body_steps_per_s": one_by_one, "one_by_one_sample_systems": int(sample.n_systems),
             "speedup_vs_one_by_one": batched / one_by_one}
+
+
+def warm_start_section(merc, args, local):
+    """Learned warm start of the universal drift: log ~1e7 (drift input ->
+    converged anomaly) pairs from the embryo disk and the sweep integrated
+    together in one context, train the FP32 MLP on the GPU, then integrate each
+    workload from the same initial state with the plain and the learned guess."""
+    c1, c2 = systems.embryo_disk(), systems.sweep()
+    kw = dict(hill_factor=3.0, drift=merc.DRIFT_UNIVERSAL)
+    g1 = merc.Integrator(merc.default_params(dt=c1.dt, **kw), device=local)
+    g1.load_systems(c1)
+    g1.mlp_log(1_000_000)
+    g1.step(400)
+    log1 = g1.mlp_get_log()
+    g1.close()
+    g = merc.Integrator(merc.default_params(dt=c2.dt, **kw), device=local)
+    g.load_systems(c2)
+    g.mlp_log(12_000_000)
+    g.step(4)
+    g.mlp_append_log(log1)
+    n_log = g.mlp_log_count()
+    t0 = time.perf_counter()
+    loss = g.mlp_train(epochs=12, batch=16384, lr=3e-3, seed=7)
+    train_s = time.perf_counter() - t0
+    w = g.mlp_weights()
+    g.close()
+    out = {"logged_pairs": int(n_log), "train_seconds": train_s, "epochs": 12,
+           "loss_first_last": [float(loss[0]), float(loss[-1])]}
+    steps = max(3, min(args.steps, 20))
+    for name, sysm in (("embryo_disk", c1), ("sweep", c2)):
+        res = {}
+        states = {}
+        for warm in (merc.WARM_PLAIN, merc.WARM_MLP):
+            gi = merc.Integrator(merc.default_params(dt=sysm.dt, hill_factor=3.0, drift=merc.DRIFT_UNIVERSAL,
+                                                     warm_start=warm), device=local)
+            gi.load_systems(sysm)
+            if warm == merc.WARM_MLP:
+                gi.mlp_set_weights(w)
+            gi.step(2)
+            gi.step(steps)
+            st = gi.stats()
+            key = "learned" if warm == merc.WARM_MLP else "plain"
+            res[key] = {"mean_iterations": st.kepler_iterations / max(st.kepler_solves, 1),
+                        "ms_per_step": st.last_step_ms / steps, "nonconverged": int(st.kepler_nonconverged)}
+            states[key] = gi.state().pos
+            gi.close()
+        a, b = states["plain"].reshape(3, -1), states["learned"].reshape(3, -1)
+        res["max_rel_pos_diff"] = float(np.max(np.abs(a - b).max(0) / np.linalg.norm(a, axis=0)))
+        res["iteration_cut"] = res["plain"]["mean_iterations"] / res["learned"]["mean_iterations"]
+        out[name] = res
+    return out
 
 
 def run_ours(args, world, rank, local, dist):
@@ -301,6 +351,7 @@ def run_ours(args, world, rank, local, dist):
         gc.close()
     g.close()
     sweep = None if args.skip_sweep else sweep_section(merc, args, local, dist, world, rank)
+    warm = None if args.skip_warm else warm_start_section(merc, args, local)
 
     if rank != 0:
         return
@@ -326,6 +377,7 @@ def run_ours(args, world, rank, local, dist):
         "kepler_mean_iterations": (st.kepler_iterations / st.kepler_solves) if st.kepler_solves else None,
         "compat_elements_path": compat,
         "sweep": sweep,
+        "learned_warm_start": warm,
     }
     print(json.dumps(line), flush=True)
 
@@ -339,6 +391,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-compat", action="store_true")
     ap.add_argument("--skip-sweep", action="store_true")
+    ap.add_argument("--skip-warm", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

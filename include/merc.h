@@ -164,6 +164,9 @@ int merc_mlp_log(merc_ctx* ctx, int64_t capacity);
 int64_t merc_mlp_log_count(merc_ctx* ctx);
 /* Copy up to max_samples logged samples (5 floats each: x1, x2, x3, x4, target). */
 int merc_mlp_get_log(merc_ctx* ctx, float* out, int64_t max_samples);
+/* Append n host samples (5 floats each) to the drift log, e.g. the log of
+ * another context, to train on several workloads at once. */
+int merc_mlp_append_log(merc_ctx* ctx, const float* samples, int64_t n);
 /* Train the network on the logged samples on the GPU (hand-written forward,
  * backward and Adam kernels, minibatches drawn by a seeded hash), epochs x
  * (samples / batch) steps.  loss_per_epoch (may be NULL): epochs floats. */

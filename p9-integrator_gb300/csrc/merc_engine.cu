@@ -781,6 +781,19 @@ int merc_mlp_get_log(merc_ctx* ctx, float* out, int64_t max_samples) {
   return MERC_OK;
 }
 
+int merc_mlp_append_log(merc_ctx* ctx, const float* samples, int64_t n) {
+  if (!ctx || !samples || n < 0) return MERC_ERR_CONFIG;
+  if (!ctx->d_log) return fail(ctx, MERC_ERR_STATE, "no drift log: call merc_mlp_log first");
+  int64_t have = merc_mlp_log_count(ctx);
+  if (have + n > ctx->log_cap) return fail(ctx, MERC_ERR_CONFIG, "drift log full (%lld + %lld > %lld)",
+                                          (long long)have, (long long)n, (long long)ctx->log_cap);
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpy(ctx->d_log + 5 * (size_t)have, samples, sizeof(float) * 5 * (size_t)n, cudaMemcpyHostToDevice));
+  unsigned long long c = (unsigned long long)(have + n);
+  CK(cudaMemcpy(ctx->d_log_count, &c, sizeof c, cudaMemcpyHostToDevice));
+  return MERC_OK;
+}
+
 int merc_mlp_set_weights(merc_ctx* ctx, const float* w) {
   if (!ctx || !w) return MERC_ERR_CONFIG;
   CK(cudaSetDevice(ctx->device));

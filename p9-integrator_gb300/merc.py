@@ -115,6 +115,7 @@ def lib() -> C.CDLL:
     L.merc_mlp_log_count.argtypes = [vp]
     L.merc_mlp_log_count.restype = C.c_int64
     L.merc_mlp_get_log.argtypes = [vp, _f32p, C.c_int64]
+    L.merc_mlp_append_log.argtypes = [vp, _f32p, C.c_int64]
     L.merc_mlp_train.argtypes = [vp, C.c_int32, C.c_int32, C.c_float, C.c_uint64, _f32p]
     L.merc_mlp_set_weights.argtypes = [vp, _f32p]
     L.merc_mlp_get_weights.argtypes = [vp, _f32p]
@@ -260,6 +261,10 @@ class Integrator:
         out = np.zeros(5 * n, np.float32)
         self._check(self.L.merc_mlp_get_log(self.h, out.ctypes.data_as(C.POINTER(C.c_float)), n))
         return out.reshape(-1, 5)
+
+    def mlp_append_log(self, samples):
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1)
+        self._check(self.L.merc_mlp_append_log(self.h, s.ctypes.data_as(C.POINTER(C.c_float)), s.size // 5))
 
     def mlp_train(self, epochs=20, batch=8192, lr=3e-3, seed=1):
         loss = np.zeros(epochs, np.float32)

@@ -85,6 +85,24 @@ class Systems:
                        None, self.label + "[subset]")
 
 
+def concat(batches) -> "Systems":
+    """Several batches as one (systems in order)."""
+    blocks = []
+    for b in batches:
+        rows = b.element_rows()
+        for s in range(b.n_systems):
+            b0, b1 = int(b.body_offset[s]), int(b.body_offset[s + 1])
+            blocks.append((b.mass[b0:b1], rows[:, b0:b1], int(b.n_massive[s])))
+    first = batches[0]
+    return _pack(blocks, first.dt, first.hill_factor, first.steps, " + ".join(b.label for b in batches))
+
+
+def shard(sysm: "Systems", rank: int, world: int) -> "Systems":
+    """Contiguous share of the systems for one of `world` replicas."""
+    idx = np.array_split(np.arange(sysm.n_systems), world)[rank]
+    return sysm.subset(idx)
+
+
 def _uangle(rng, n):
     return rng.uniform(0.0, TWO_PI, n)
 

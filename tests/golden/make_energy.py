@@ -1,0 +1,48 @@
+"""Generate tests/golden/energy_outer.json: energy of the outer-solar-system
+workload (5 massive bodies + 100 test particles, dt 0.5 yr, changeover 3 Hill
+radii) after 1e4 steps, from the CPU oracle in long double (the energy-error
+reference) and in binary64 with the reference's element drift (the
+reference algorithm).  Run from the repository root:
+    python tests/golden/make_energy.py
+"""
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.join(ROOT, "p9-integrator_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import systems  # noqa: E402
+from oracle import Oracle, build  # noqa: E402
+from oracle import default_params as oparams  # noqa: E402
+
+STEPS = 10000
+
+
+def main():
+    build()
+    O = Oracle()
+    s = systems.outer_solar_system()
+    out = {"workload": s.label, "steps": STEPS, "dt": s.dt, "hill_factor": s.hill_factor}
+    for drift, name in ((0, "elements"), (1, "universal")):
+        p = oparams(dt=s.dt, hill_factor=s.hill_factor, drift=drift)
+        pos, vel, alag = O.load_elements(p, s.body_offset, s.n_massive, s.mass, s.elements)
+        e0 = float(O.energy(s.body_offset, s.n_massive, s.mass, pos, vel)[0])
+        t = time.time()
+        res = {}
+        for prec, tag in ((0, "binary64"), (1, "long_double")):
+            a, b, *_ = O.run(p, s.body_offset, s.n_massive, s.mass, pos, vel, alag, steps=STEPS, precision=prec)
+            e1 = float(O.energy(s.body_offset, s.n_massive, s.mass, a, b)[0])
+            res[tag] = {"energy": e1, "rel_error": abs(e1 - e0) / abs(e0)}
+        out[name] = {"energy0": e0, **res}
+        print(name, res, f"{time.time() - t:.1f}s")
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "energy_outer.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,56 @@
+"""Energy conservation over 1e4 steps of the outer-solar-system workload, against
+the long-double CPU oracle (tests/golden/energy_outer.json, make_energy.py).
+
+The reference algorithm (element drift, binary64) loses 2.3e-6 of the energy in
+1e4 steps, the universal-variable drift 2.4e-8; the GPU universal drift (plain
+and learned warm start) must sit at the long-double value of its own
+algorithm and within 2x of the reference algorithm's error."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import merc
+import systems
+
+pytestmark = pytest.mark.gpu
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "energy_outer.json")))
+
+
+def energy_error(drift, warm=merc.WARM_PLAIN, weights=None, log=0):
+    s = systems.outer_solar_system()
+    g = merc.Integrator(merc.default_params(dt=s.dt, hill_factor=s.hill_factor, drift=drift, warm_start=warm))
+    g.load_systems(s)
+    if weights is not None:
+        g.mlp_set_weights(weights)
+    if log:
+        g.mlp_log(log)
+    e0 = g.energy()[0]
+    g.step(GOLD["steps"])
+    e1 = g.energy()[0]
+    return abs(e1 - e0) / abs(e0), g
+
+
+def test_universal_energy_error_matches_long_double_and_beats_reference():
+    err, g = energy_error(merc.DRIFT_UNIVERSAL, log=2_000_000)
+    w_ld = GOLD["universal"]["long_double"]["rel_error"]
+    ref = GOLD["elements"]["binary64"]["rel_error"]
+    assert abs(err - w_ld) <= 0.01 * w_ld, (err, w_ld)
+    assert err <= 2.0 * ref
+    # learned warm start, trained on this run's own drifts: same energy error
+    loss = g.mlp_train(epochs=20, batch=4096, lr=3e-3, seed=11)
+    w = g.mlp_weights()
+    g.close()
+    err2, g2 = energy_error(merc.DRIFT_UNIVERSAL, merc.WARM_MLP, w)
+    st = g2.stats()
+    g2.close()
+    assert abs(err2 - err) <= 0.01 * err, (err, err2)
+    assert st.kepler_nonconverged == 0
+
+
+def test_element_drift_energy_matches_oracle():
+    err, g = energy_error(merc.DRIFT_ELEMENTS)
+    g.close()
+    ref = GOLD["elements"]["binary64"]["rel_error"]
+    assert abs(err - ref) <= 1e-3 * ref, (err, ref)

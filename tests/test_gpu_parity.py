@@ -105,3 +105,40 @@ def test_universal_parity(oracle, which):
     # the pair sums differ from the oracle's by ulps, which can move a
     # Newton stop by one iteration in rare cases
     assert abs(gs.kepler_iterations - ost[1]) <= max(2, ost[1] // 1000)
+
+
+@pytest.mark.parametrize("drift", [merc.DRIFT_ELEMENTS, merc.DRIFT_UNIVERSAL])
+def test_split_steps_and_resume_are_exact(drift):
+    """Steps in one call or several (graph replays of 8 and of 1 step) give the
+    same bits; so does saving the state and resuming it in a new context."""
+    sysm = systems.embryo_disk(n_embryos=94, seed=12)
+    kw = dict(dt=sysm.dt, hill_factor=3.0, drift=drift)
+    a = merc.Integrator(merc.default_params(**kw))
+    a.load_systems(sysm)
+    a.step(21)
+    sa = a.state()
+    b = merc.Integrator(merc.default_params(**kw))
+    b.load_systems(sysm)
+    b.step(5)
+    b.step(3)
+    saved = b.state()
+    alag = b.a_lag()
+    b.close()
+    c = merc.Integrator(merc.default_params(**kw))
+    c.load_state(sysm.body_offset, sysm.n_massive, sysm.mass, saved.pos, saved.vel, alag)
+    c.step(13)
+    sc = c.state()
+    assert np.array_equal(sa.pos, sc.pos) and np.array_equal(sa.vel, sc.vel)
+    a.close()
+    c.close()
+
+
+def test_errors_are_reported_not_crashed():
+    g = merc.Integrator(merc.default_params())
+    with pytest.raises(merc.MercError) as e:
+        g.step(1)
+    assert e.value.code == merc.MERC_ERR_STATE
+    with pytest.raises(merc.MercError) as e:
+        g.load_elements([0, 3], [5], np.ones(3), np.zeros(18))
+    assert e.value.code == merc.MERC_ERR_CONFIG
+    g.close()
