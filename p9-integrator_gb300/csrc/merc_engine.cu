@@ -28,6 +28,7 @@
 
 #include <algorithm>
 #include <cstdarg>
+#include <array>
 #include <mutex>
 #include <cstdio>
 #include <cstring>
@@ -43,6 +44,7 @@ using namespace merc;
 
 #include "merc_mlp.cuh"
 #include "merc_kernels.cuh"
+#include "merc_sweep.cuh"
 
 // ---------------------------------------------------------------------------
 // context
@@ -83,6 +85,14 @@ struct merc_ctx {
   int64_t steps_done = 0;
   int64_t launches = 0;
   int kernels_per_step = 0;
+  // persistent small-system path: size order, work counter, tuned block size
+  int* d_order = nullptr;
+  int* d_queue = nullptr;
+  int nmax_sys = 0;
+  int sweep_threads = 0;   // 0: not tuned yet
+  int sweep_grid = 0;
+  unsigned long long* d_tune_counters = nullptr;
+  uint32_t* d_tune_flags = nullptr;
   // learned warm start: parameter blob, drift log, training state
   float* d_mlp = nullptr;
   bool mlp_ready = false;
@@ -261,6 +271,20 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
       (st = dalloc(ctx, &D.rc[1], 4 * (size_t)n)) || (st = dalloc(ctx, &D.P, 3 * (size_t)n_systems)) ||
       (st = dalloc(ctx, &D.ce_list, n)) || (st = dalloc(ctx, &D.ce_count, 2)) || (st = dalloc(ctx, &D.counters, 4)))
     return st;
+  {
+    // systems by size, largest first: the persistent kernel's work order
+    std::vector<int> order(n_systems);
+    for (int q = 0; q < n_systems; q++) order[q] = q;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      return (off[a + 1] - off[a]) > (off[b + 1] - off[b]);
+    });
+    ctx->nmax_sys = n_systems ? (int)(off[order[0] + 1] - off[order[0]]) : 0;
+    if ((st = dalloc(ctx, &ctx->d_order, n_systems)) || (st = dalloc(ctx, &ctx->d_queue, 1)) ||
+        (st = dalloc(ctx, &ctx->d_tune_counters, 4)) || (st = dalloc(ctx, &ctx->d_tune_flags, n)))
+      return st;
+    CK(cudaMemcpy(ctx->d_order, order.data(), sizeof(int) * n_systems, cudaMemcpyHostToDevice));
+    ctx->sweep_threads = 0;
+  }
   D.off = ctx->d_off;
   D.nm = ctx->d_nm;
   D.sys = ctx->d_sys;
@@ -366,7 +390,8 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
                                                         p.compat_block, p.hill_factor, ej2, last);
           nk++;
         }
-        k_kick_reduce_sym<<<nb, kThreads, 0, s>>>(D, rc_out, hdt, p.hill_factor, ej2, last);
+        k_kick_reduce_sym<<<(unsigned)((8 * (int64_t)D.n + kThreads - 1) / kThreads), kThreads, 0, s>>>(
+            D, rc_out, hdt, p.hill_factor, ej2, last);
         nk++;
       } else if (ctx->has_big) {
         k_kick_tiled<<<ctx->n_work, kTile, 0, s>>>(D, ctx->d_work, rc_in, rc_out, hdt, p.softening2, p.compat_block,
@@ -417,8 +442,8 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       nk++;
     }
     if (ctx->has_big) {
-      k_encounter_cluster<<<ctx->enc_blocks, kEncThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
-                                                                   p.softening2);
+      k_encounter_cluster<<<ctx->enc_blocks * 2, 32, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
+                                                              p.softening2);
       nk++;
     }
     momentum(D.vo);
@@ -470,6 +495,113 @@ int build_graphs(merc_ctx* ctx) {
   if ((st = capture(ctx, kGraphSteps, ctx->time_kicks, 0, &ctx->graph))) return st;
   if ((st = capture(ctx, 1, ctx->time_kicks, kGraphSteps, &ctx->graph1))) return st;
   ctx->graph_steps = kGraphSteps;
+  return MERC_OK;
+}
+
+// ---- persistent path for batches of small systems ----
+bool use_persistent(const merc_ctx* ctx) {
+  return ctx->p.drift == MERC_DRIFT_UNIVERSAL && !ctx->has_big && ctx->log_cap == 0 && ctx->nmax_sys > 0;
+}
+
+size_t sweep_smem_bytes(const merc_ctx* ctx) {
+  const size_t nmax = (size_t)ctx->nmax_sys;
+  size_t b = 8 * (6 * nmax + kSweepMaxNm + 8 * kSweepMaxNm + 6 * kSweepMaxNm + 4) + 4 * (nmax + (nmax & 1));
+  if (ctx->p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) b += 4 * (size_t)kBlob;
+  return b;
+}
+
+SweepArgs sweep_args(merc_ctx* ctx, int steps, bool trial) {
+  SweepArgs a;
+  a.D = ctx->D;
+  const merc_params& p = ctx->p;
+  if (trial) {  // a timing trial integrates a copy of the state into scratch
+    a.D.x = ctx->D.xo;
+    a.D.v = ctx->D.vo;
+    a.D.flags = ctx->d_tune_flags;
+    a.D.counters = ctx->d_tune_counters;
+  }
+  a.order = ctx->d_order;
+  a.queue = ctx->d_queue;
+  a.nsys = ctx->D.nsys;
+  a.nmax = ctx->nmax_sys;
+  a.steps = steps;
+  a.dt = p.dt;
+  a.soft2 = p.softening2;
+  a.hill = p.hill_factor;
+  a.tol = p.kepler_tol;
+  a.eject_r2 = p.eject_r > 0 ? p.eject_r * p.eject_r : 0.0;
+  a.compat_block = p.compat_block;
+  a.rows = p.bs_rows;
+  a.max_iter = p.kepler_max_iter;
+  a.mlp = (p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) ? ctx->d_mlp : nullptr;
+  a.rc_final = trial ? ctx->D.rc[ctx->rc_cur ^ 1] : ctx->D.rc[ctx->rc_cur];
+  return a;
+}
+
+int launch_sweep(merc_ctx* ctx, int threads, int grid, int steps, bool trial) {
+  const size_t smem = sweep_smem_bytes(ctx);
+  CK(cudaMemsetAsync(ctx->d_queue, 0, sizeof(int), ctx->stream));
+  k_sweep_persistent<<<grid, threads, smem, ctx->stream>>>(sweep_args(ctx, steps, trial));
+  CK(cudaGetLastError());
+  return MERC_OK;
+}
+
+// Tuner of the persistent kernel: the block size (bodies per thread) is
+// chosen by timing a 2-step trial of each candidate on a copy of the state;
+// the choice is cached per (largest system, massive count, systems) bucket.
+std::mutex g_tune_mu;
+std::vector<std::pair<std::array<int, 3>, std::pair<int, int>>> g_tune_cache;
+
+int tune_sweep(merc_ctx* ctx) {
+  const size_t smem = sweep_smem_bytes(ctx);
+  CK(cudaFuncSetAttribute(k_sweep_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int max_nm = 0;
+  for (int v : ctx->h_nm) max_nm = std::max(max_nm, v);
+  int lg = 0;
+  while ((1 << lg) < ctx->nmax_sys) lg++;
+  int sl = 0;
+  while ((1 << sl) < ctx->D.nsys) sl++;
+  std::array<int, 3> key = {lg, max_nm, sl};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (auto& e : g_tune_cache)
+      if (e.first == key) {
+        ctx->sweep_threads = e.second.first;
+        ctx->sweep_grid = e.second.second;
+        return MERC_OK;
+      }
+  }
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  const int cands[3] = {64, 128, 256};
+  float best = 1e30f;
+  int best_t = 128, best_g = sms;
+  for (int t : cands) {
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_persistent, t, smem));
+    if (per_sm < 1) continue;
+    const int grid = std::min(ctx->D.nsys, per_sm * sms);
+    const size_t n3 = 3 * (size_t)ctx->D.n;
+    CK(cudaMemcpyAsync(ctx->D.xo, ctx->D.x, sizeof(double) * n3, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->D.vo, ctx->D.v, sizeof(double) * n3, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_tune_flags, 0, sizeof(uint32_t) * ctx->D.n, ctx->stream));
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    int st = launch_sweep(ctx, t, grid, 2, true);
+    if (st) return st;
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    if (ms < best) {
+      best = ms;
+      best_t = t;
+      best_g = grid;
+    }
+  }
+  ctx->sweep_threads = best_t;
+  ctx->sweep_grid = best_g;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_cache.push_back({key, {best_t, best_g}});
   return MERC_OK;
 }
 
@@ -625,16 +757,33 @@ int merc_step(merc_ctx* ctx, int64_t n_steps) {
   if (n_steps < 0) return fail(ctx, MERC_ERR_CONFIG, "n_steps < 0");
   if (n_steps == 0) return MERC_OK;
   CK(cudaSetDevice(ctx->device));
-  if (!ctx->graph) {
-    int st = build_graphs(ctx);
-    if (st) return st;
+  if (use_persistent(ctx)) {
+    if (!ctx->sweep_threads) {
+      int st = tune_sweep(ctx);
+      if (st) return st;
+    }
+    CK(cudaFuncSetAttribute(k_sweep_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)sweep_smem_bytes(ctx)));
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    const int64_t chunk = 1 << 20;  // steps per launch
+    for (int64_t done = 0; done < n_steps; done += chunk) {
+      int st = launch_sweep(ctx, ctx->sweep_threads, ctx->sweep_grid, (int)std::min(chunk, n_steps - done), false);
+      if (st) return st;
+      ctx->launches++;
+    }
+    ctx->last_graph_steps = 0;
+  } else {
+    if (!ctx->graph) {
+      int st = build_graphs(ctx);
+      if (st) return st;
+    }
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    const int64_t full = n_steps / kGraphSteps, rest = n_steps % kGraphSteps;
+    for (int64_t k = 0; k < full; k++) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+    for (int64_t k = 0; k < rest; k++) CK(cudaGraphLaunch(ctx->graph1, ctx->stream));
+    ctx->last_graph_steps = rest > 0 ? 1 : kGraphSteps;
+    ctx->launches += n_steps * ctx->kernels_per_step;
   }
-  CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  const int64_t full = n_steps / kGraphSteps, rest = n_steps % kGraphSteps;
-  for (int64_t k = 0; k < full; k++) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
-  for (int64_t k = 0; k < rest; k++) CK(cudaGraphLaunch(ctx->graph1, ctx->stream));
-  ctx->last_graph_steps = rest > 0 ? 1 : kGraphSteps;
-  ctx->launches += n_steps * ctx->kernels_per_step;
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   CK(cudaEventSynchronize(ctx->ev1));
   float ms = 0.f;

@@ -519,43 +519,53 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
 }
 
 // Kick of every body of a big system whose sums are in partials: massive
-// bodies add their block partials (symmetric kernel) in block order, test
-// particles their chunk partials in chunk order (when there is more than one
-// chunk; a single chunk was applied by the tiled kernel).
+// bodies add their block partials (symmetric kernel), test particles their
+// chunk partials (when there is more than one chunk; a single chunk was
+// applied by the tiled kernel).  Eight threads per body each add every eighth
+// partial; the eight sums are combined by a fixed butterfly, so the result does
+// not depend on scheduling.
 __global__ void k_kick_reduce_sym(Dev D, double* __restrict__ rc_out, double hdt, double hill, double eject_r2,
                                   int last) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= D.n) return;
-  const int n = D.n, s = D.sys[j];
-  if (!D.big[s]) return;
-  const int b0 = D.off[s], nm = D.nm[s], local = j - b0;
-  d3 acc = {0.0, 0.0, 0.0};
-  if (local < nm) {
-    // four interleaved partial sums (blocks b = 0, 4, 8, ..., 1, 5, ...) added
-    // in a fixed order: independent load/add chains, deterministic result
-    const int NB = (nm + 31) / 32;
-    const double* base = D.part_sym + D.sym_base[s];
-    d3 q[4] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
-#pragma unroll 4
-    for (int b = 0; b < NB; b++) {
-      const double* p = base + (size_t)b * 3 * nm;
-      q[b & 3].x += p[local];
-      q[b & 3].y += p[nm + local];
-      q[b & 3].z += p[2 * nm + local];
-    }
-    acc.x = (q[0].x + q[1].x) + (q[2].x + q[3].x);
-    acc.y = (q[0].y + q[1].y) + (q[2].y + q[3].y);
-    acc.z = (q[0].z + q[1].z) + (q[2].z + q[3].z);
-  } else {
-    const int C = D.nchunk[s];
-    if (C <= 1) return;
-    for (int c = 0; c < C; c++) {
-      const double* p = D.part + (size_t)c * 3 * n;
-      acc.x += p[j];
-      acc.y += p[n + j];
-      acc.z += p[2 * n + j];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = t >> 3, sub = t & 7;
+  const bool valid = j < D.n;
+  const int n = D.n;
+  const int s = valid ? D.sys[j] : 0;
+  bool work = valid && D.big[s];
+  const int b0 = work ? D.off[s] : 0, nm = work ? D.nm[s] : 0, local = j - b0;
+  int count = 0;
+  const double* base = nullptr;
+  size_t stride = 0;
+  int index = 0;
+  if (work) {
+    if (local < nm) {
+      count = (nm + 31) / 32;
+      base = D.part_sym + D.sym_base[s];
+      stride = 3 * (size_t)nm;
+      index = local;
+    } else if (D.nchunk[s] > 1) {
+      count = D.nchunk[s];
+      base = D.part;
+      stride = 3 * (size_t)n;
+      index = j;
+    } else {
+      work = false;
     }
   }
+  const size_t span = stride / 3;
+  d3 acc = {0.0, 0.0, 0.0};
+  for (int b = sub; b < count; b += 8) {
+    const double* p = base + (size_t)b * stride;
+    acc.x += p[index];
+    acc.y += p[span + index];
+    acc.z += p[2 * span + index];
+  }
+  for (int o = 1; o < 8; o <<= 1) {
+    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+  }
+  if (!work || sub != 0) return;
   d3 pos = load3(D.x, n, j), vel = load3(D.v, n, j);
   vel.x = fma(acc.x, hdt, vel.x);
   vel.y = fma(acc.y, hdt, vel.y);
@@ -795,34 +805,25 @@ struct ClusterVelTotal {
   const double* rc;
   int b0, c0, c1, self;
   double soft2;
-  double* red;   // shared, 3 * blockDim.x
   double* slot;  // shared, 2 x 4 doubles (3 used)
   int* parity;   // per-thread evaluation counter
   __device__ __forceinline__ d3 operator()(const d3& pos, const d3& vel, double dt) const {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     d3 acc = {0.0, 0.0, 0.0};
-    for (int i = c0 + (int)threadIdx.x; i < c1; i += blockDim.x)
+    for (int i = c0 + (int)threadIdx.x; i < c1; i += 32)
       pair_fast<true>(pos, self, i, load_src(*D, rc, b0 + i), soft2, acc);
-    const int t = threadIdx.x, B = blockDim.x;
-    __syncthreads();
-    red[t] = acc.x;
-    red[B + t] = acc.y;
-    red[2 * B + t] = acc.z;
-    __syncthreads();
-    for (int w = B / 2; w > 0; w >>= 1) {
-      if (t < w) {
-        red[t] += red[t + w];
-        red[B + t] += red[B + t + w];
-        red[2 * B + t] += red[2 * B + t + w];
-      }
-      __syncthreads();
+    // warp sum in a fixed butterfly order (every lane ends with the total)
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+      acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
     }
     const int buf = *parity & 1;
-    if (t == 0) {
-      slot[4 * buf] = red[0];
-      slot[4 * buf + 1] = red[B];
-      slot[4 * buf + 2] = red[2 * B];
+    if (threadIdx.x == 0) {
+      slot[4 * buf] = acc.x;
+      slot[4 * buf + 1] = acc.y;
+      slot[4 * buf + 2] = acc.z;
     }
     cl.sync();
     acc = {0.0, 0.0, 0.0};
@@ -843,14 +844,15 @@ struct ClusterVelTotal {
 };
 
 // Encounter sub-step of the big systems' encounter bodies: one cluster of
-// kEncCluster blocks per body (grid-stride over the list by cluster).  Every
-// thread of the cluster runs the same Richardson scheme, so the cluster
+// kEncCluster one-warp blocks per body (grid-stride over the list by
+// cluster).  The scalar sub-step arithmetic runs in every warp of the
+// cluster, so one warp per block keeps that redundancy at kEncCluster warps.
+// Every thread of the cluster runs the same Richardson scheme, so the cluster
 // barriers inside the velocity updates are reached uniformly.
-__global__ void __cluster_dims__(kEncCluster, 1, 1) __launch_bounds__(kEncThreads)
+__global__ void __cluster_dims__(kEncCluster, 1, 1) __launch_bounds__(32)
     k_encounter_cluster(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, int rows,
                         double soft2) {
   namespace cg = cooperative_groups;
-  __shared__ double red[3 * kEncThreads];
   __shared__ double slot[8];
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
@@ -861,7 +863,7 @@ __global__ void __cluster_dims__(kEncCluster, 1, 1) __launch_bounds__(kEncThread
     const int j = D.ce_list_big[k];
     const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
     const int c0 = (int)((int64_t)rank * nm / kEncCluster), c1 = (int)((int64_t)(rank + 1) * nm / kEncCluster);
-    ClusterVelTotal vt{&D, rc_in, b0, c0, c1, self_index(j - b0, compat_block), soft2, red, slot, &parity};
+    ClusterVelTotal vt{&D, rc_in, b0, c0, c1, self_index(j - b0, compat_block), soft2, slot, &parity};
     PV c = {load3(D.x, n, j), load3(D.v, n, j)};
     PV bs = richardson(c, vt, dt, rows);
     if (rank == 0 && threadIdx.x == 0) {

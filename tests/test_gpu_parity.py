@@ -107,11 +107,16 @@ def test_universal_parity(oracle, which):
     assert abs(gs.kepler_iterations - ost[1]) <= max(2, ost[1] // 1000)
 
 
-@pytest.mark.parametrize("drift", [merc.DRIFT_ELEMENTS, merc.DRIFT_UNIVERSAL])
-def test_split_steps_and_resume_are_exact(drift):
-    """Steps in one call or several (graph replays of 8 and of 1 step) give the
+@pytest.mark.parametrize("drift,which", [(merc.DRIFT_ELEMENTS, "embryo"), (merc.DRIFT_UNIVERSAL, "embryo"),
+                                         (merc.DRIFT_UNIVERSAL, "sweep")])
+def test_split_steps_and_resume_are_exact(drift, which):
+    """Steps in one call or several (graph replays of 8 and of 1 step, or
+    persistent launches with merged half kicks for small systems) give the
     same bits; so does saving the state and resuming it in a new context."""
-    sysm = systems.embryo_disk(n_embryos=94, seed=12)
+    if which == "embryo":
+        sysm = systems.embryo_disk(n_embryos=94, seed=12)
+    else:
+        sysm = systems.sweep(n_systems=40, nt_lo=20, nt_hi=200, seed=12)
     kw = dict(dt=sysm.dt, hill_factor=3.0, drift=drift)
     a = merc.Integrator(merc.default_params(**kw))
     a.load_systems(sysm)
@@ -142,3 +147,25 @@ def test_errors_are_reported_not_crashed():
         g.load_elements([0, 3], [5], np.ones(3), np.zeros(18))
     assert e.value.code == merc.MERC_ERR_CONFIG
     g.close()
+
+
+def test_persistent_sweep_kernel_equals_per_phase_kernels():
+    """Small systems run in the persistent kernel (work queue, merged half
+    kicks); with the drift log on they run in the per-phase kernels.  Both give
+    the same bits."""
+    sysm = systems.sweep(n_systems=64, nt_lo=16, nt_hi=300, seed=31)
+    kw = dict(dt=sysm.dt, hill_factor=3.0, drift=merc.DRIFT_UNIVERSAL)
+    a = merc.Integrator(merc.default_params(**kw))
+    a.load_systems(sysm)
+    a.step(30)
+    b = merc.Integrator(merc.default_params(**kw))
+    b.load_systems(sysm)
+    b.mlp_log(1 << 16)  # logging routes small systems through the per-phase kernels
+    b.step(30)
+    sa, sb = a.state(), b.state()
+    assert np.array_equal(sa.pos, sb.pos) and np.array_equal(sa.vel, sb.vel)
+    assert np.array_equal(sa.flags, sb.flags)
+    ta, tb = a.stats(), b.stats()
+    assert ta.kepler_iterations == tb.kepler_iterations and ta.ce_body_steps == tb.ce_body_steps
+    a.close()
+    b.close()
