@@ -266,6 +266,7 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
   if ((st = dalloc(ctx, &ctx->d_off, n_systems + 1)) || (st = dalloc(ctx, &ctx->d_nm, n_systems)) ||
       (st = dalloc(ctx, &ctx->d_sys, n)) || (st = dalloc(ctx, &ctx->d_m, n)) || (st = dalloc(ctx, &D.x, 3 * (size_t)n)) ||
       (st = dalloc(ctx, &D.v, 3 * (size_t)n)) || (st = dalloc(ctx, &D.xo, 3 * (size_t)n)) ||
+      (st = dalloc(ctx, &D.xf, 3 * (size_t)n)) ||
       (st = dalloc(ctx, &D.vo, 3 * (size_t)n)) || (st = dalloc(ctx, &D.alag, n)) || (st = dalloc(ctx, &D.flags, n)) ||
       (st = dalloc(ctx, &D.ce, n)) || (st = dalloc(ctx, &D.rc[0], 4 * (size_t)n)) ||
       (st = dalloc(ctx, &D.rc[1], 4 * (size_t)n)) || (st = dalloc(ctx, &D.P, 3 * (size_t)n_systems)) ||
@@ -338,7 +339,8 @@ int dh_convert(merc_ctx* ctx, bool reverse) {
 
 // Enqueue one step on the stream (also used while capturing the graph);
 // returns the number of kernels it launched through *kernels.
-int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int* kernels) {
+int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int* kernels, bool first_in_graph,
+                 bool last_in_graph) {
   Dev& D = ctx->D;
   const merc_params& p = ctx->p;
   cudaStream_t s = ctx->stream;
@@ -373,6 +375,8 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
   } else {
     // the symmetric pair kernels assume a massive body excludes exactly itself
     const bool use_sym = p.compat_block == 0 || p.compat_block >= ctx->max_big_nm;
+    // test particles of big systems: adjacent half kicks merged inside a graph
+    const bool merge_tp = ctx->has_big && use_sym && ctx->n_work_tp > 0 && !ctx->any_multi;
     auto kick = [&](const double* rc_in, double* rc_out, int last, int ev) {
       int st2;
       if ((st2 = kick_ev(ev))) return st2;
@@ -385,14 +389,28 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
         // massive targets: symmetric block pairs; test particles: tiled
         k_sym<true><<<ctx->n_sym, 32, 0, s>>>(D, ctx->d_sym, ctx->n_sym, rc_in, p.softening2);
         nk++;
-        if (ctx->n_work_tp) {
+        // with merging, the first half kick of the test particles was done by
+        // the previous step's merged kernel (except in the first step)
+        const bool tp_here = ctx->n_work_tp && !(merge_tp && ((!last && !first_in_graph) || (last && !last_in_graph)));
+        if (tp_here && !(merge_tp && last)) {
           k_kick_tiled<<<ctx->n_work_tp, kTile, 0, s>>>(D, ctx->d_work_tp, rc_in, rc_out, hdt, p.softening2,
                                                         p.compat_block, p.hill_factor, ej2, last);
           nk++;
         }
         k_kick_reduce_sym<<<(unsigned)((8 * (int64_t)D.n + kThreads - 1) / kThreads), kThreads, 0, s>>>(
-            D, rc_out, hdt, p.hill_factor, ej2, last);
+            D, rc_out, hdt, p.hill_factor, ej2, last, merge_tp ? 1 : 0);
         nk++;
+        if (merge_tp && last) {
+          if (last_in_graph) {
+            k_kick_tiled<<<ctx->n_work_tp, kTile, 0, s>>>(D, ctx->d_work_tp, rc_in, rc_out, hdt, p.softening2,
+                                                          p.compat_block, p.hill_factor, ej2, 1);
+          } else {
+            // rc_out now holds the next step's radii (written by the reduce)
+            k_kick_tiled_merged<<<ctx->n_work_tp, kTile, 0, s>>>(D, ctx->d_work_tp, rc_in, rc_out, hdt,
+                                                                 p.softening2, p.compat_block, ej2);
+          }
+          nk++;
+        }
       } else if (ctx->has_big) {
         k_kick_tiled<<<ctx->n_work, kTile, 0, s>>>(D, ctx->d_work, rc_in, rc_out, hdt, p.softening2, p.compat_block,
                                                    p.hill_factor, ej2, last);
@@ -462,7 +480,7 @@ int capture(merc_ctx* ctx, int steps, bool timed, int first_slot, cudaGraphExec_
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < steps; k++) {
     int nk = 0;
-    int st = enqueue_step(ctx, timed, first_slot + k, &nk);
+    int st = enqueue_step(ctx, timed, first_slot + k, &nk, k == 0, k == steps - 1);
     ctx->kernels_per_step = nk;
     if (st) {
       cudaStreamEndCapture(ctx->stream, &g);
@@ -505,7 +523,8 @@ bool use_persistent(const merc_ctx* ctx) {
 
 size_t sweep_smem_bytes(const merc_ctx* ctx) {
   const size_t nmax = (size_t)ctx->nmax_sys;
-  size_t b = 8 * (6 * nmax + kSweepMaxNm + 8 * kSweepMaxNm + 6 * kSweepMaxNm + 4) + 4 * (nmax + (nmax & 1));
+  size_t b = 8 * (6 * nmax + kSweepMaxNm + 8 * kSweepMaxNm + 6 * kSweepMaxNm + 4) + sizeof(F4) * kSweepMaxNm +
+             4 * kSweepMaxNm + 4 * (nmax + (nmax & 1));
   if (ctx->p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) b += 4 * (size_t)kBlob;
   return b;
 }
@@ -1256,6 +1275,7 @@ extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodi
     *ids = c.take<int>(1);
     *wk = c.take<Work>(big ? (size_t)((n + kTile - 1) / kTile) * C : 1);
     D.sys = c.take<int>(n);
+    D.xf = c.take<float>(3 * (size_t)n);
     D.xo = c.take<double>(3 * (size_t)n);
     D.vo = c.take<double>(3 * (size_t)n);
     D.alag = c.take<double>(n);

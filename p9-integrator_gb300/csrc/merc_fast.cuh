@@ -109,6 +109,27 @@ __device__ __forceinline__ d3 sun_accel(const d3& pos, double soft2) {
   return {-(pos.x / denom), -(pos.y / denom), -(pos.z / denom)};
 }
 
+// FP32 positions of a body for the encounter prefilter: float copies and the
+// largest component magnitude (the scale of their rounding error).
+struct F4 {
+  float x, y, z, sc;
+};
+__device__ __forceinline__ F4 f4_of(float x, float y, float z) {
+  return {x, y, z, fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z)))};
+}
+
+// FP32 prefilter of the encounter test: false only when the pair is certainly
+// farther apart than r_crit.  The float copies are off by at most 2^-24 of each
+// coordinate, the difference and its square add a few 2^-24 relative
+// roundings, so |d| >= |d_f| (1 - 2e-7) - 2.1e-7 (sc_s + sc_t); the limit
+// r_crit (1 + 1e-6) + 1e-6 (sc_s + sc_t) covers that with room.  NaN -> maybe.
+__device__ __forceinline__ bool ce_maybe(const F4& t, const F4& s, float rc) {
+  float dx = s.x - t.x, dy = s.y - t.y, dz = s.z - t.z;
+  float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  float lim = fmaf(rc, 1.000001f, 1e-6f * (s.sc + t.sc));
+  return !(r2 > lim * lim && lim > 0.0f);
+}
+
 // Encounter test of one pair, exact: sqrt(r^2) < r_crit and not self
 // (sim.cuh:602-609); the sqrt is skipped when r^2 is clearly above r_crit^2.
 __device__ __forceinline__ bool pair_ce(const d3& pos, int self, int i, const FastSrc& S) {
@@ -116,6 +137,13 @@ __device__ __forceinline__ bool pair_ce(const d3& pos, int self, int i, const Fa
   double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
   if (hi_word(r2) > S.rc2_hi) return false;
   return (sqrt(r2) < S.rc) && (self != i);
+}
+
+// The same test behind the FP32 prefilter (no FP64 work for far pairs).
+__device__ __forceinline__ bool pair_ce_f(const d3& pos, const F4& tf, int self, int i, const FastSrc& S,
+                                          const F4& sf) {
+  if (!ce_maybe(tf, sf, (float)S.rc)) return false;
+  return pair_ce(pos, self, i, S);
 }
 
 }  // namespace merc

@@ -37,6 +37,7 @@ struct Dev {
   const int* nchunk = nullptr;         // per system: source chunks of the tiled kick
   double* x = nullptr;       // 3 n
   double* v = nullptr;       // 3 n
+  float* xf = nullptr;       // 3 n, FP32 copies of x after each solar jump (encounter prefilter)
   double* xo = nullptr;      // 3 n, drift output
   double* vo = nullptr;      // 3 n
   const double* m = nullptr;
@@ -80,6 +81,10 @@ __device__ __forceinline__ void write_rc(double* rc, int j, const d3& x, const d
   rc[4 * (size_t)j + 1] = 0.1 * r;
   rc[4 * (size_t)j + 2] = 0.9 * r;
   rc[4 * (size_t)j + 3] = (double)rc2_threshold(r);
+}
+
+__device__ __forceinline__ F4 load_f4(const Dev& D, int g) {
+  return f4_of(__ldg(D.xf + g), __ldg(D.xf + D.n + g), __ldg(D.xf + 2 * D.n + g));
 }
 
 __device__ __forceinline__ FastSrc load_src(const Dev& D, const double* __restrict__ rc, int g) {
@@ -224,6 +229,9 @@ __global__ void k_jump(Dev D, const double* __restrict__ xsrc, const double* __r
   x.y = fma(py, hdt, x.y);
   x.z = fma(pz, hdt, x.z);
   store3(D.x, n, j, x);
+  D.xf[j] = (float)x.x;
+  D.xf[n + j] = (float)x.y;
+  D.xf[2 * n + j] = (float)x.z;
   d3 v;
   if (vsrc) {
     v = load3(vsrc, n, j);
@@ -359,6 +367,70 @@ __global__ void __launch_bounds__(kTile) k_kick_tiled(Dev D, const Work* __restr
   }
 }
 
+// Test particles of the big systems (one source chunk): the second half kick
+// of this step (table B) and the first of the next step (table A) in one pass
+// over the sources.  Positions do not move between the two; a pair outside
+// both changeover radii computes its term once and adds it to both
+// accumulators, in source order, so the result equals two separate kicks bit
+// for bit.  Flags are taken after the first of the two kicks.
+__global__ void __launch_bounds__(kTile) k_kick_tiled_merged(Dev D, const Work* __restrict__ work,
+                                                             const double* __restrict__ rcB,
+                                                             const double* __restrict__ rcA, double hdt,
+                                                             double soft2, int compat_block, double eject_r2) {
+  __shared__ FastSrc tile[kSrcTile];
+  __shared__ double tileA[kSrcTile][4];
+  const Work W = work[blockIdx.x];
+  const int n = D.n, s = W.sys, b0 = D.off[s], b1 = D.off[s + 1], nm = D.nm[s];
+  const int j = W.t0 + threadIdx.x;
+  const bool active = j < b1;
+  const int local = j - b0, self = self_index(local, compat_block);
+  d3 pos = active ? load3(D.x, n, j) : d3{0.0, 0.0, 0.0};
+  d3 accB = {0.0, 0.0, 0.0}, accA = {0.0, 0.0, 0.0};
+  for (int c = W.c0; c < W.c1; c += kSrcTile) {
+    const int cnt = min(kSrcTile, W.c1 - c);
+    __syncthreads();
+    stage_sources(D, rcB, b0, c, cnt, tile);
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x)
+      for (int q = 0; q < 4; q++) tileA[k][q] = rcA[4 * (size_t)(b0 + c + k) + q];
+    __syncthreads();
+    if (active) {
+      for (int k = 0; k < cnt; k++) {
+        const FastSrc& SB = tile[k];
+        const int i = c + k;
+        double dx = SB.x - pos.x, dy = SB.y - pos.y, dz = SB.z - pos.z;
+        double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+        if (hi_word(r2) > max(SB.rc2_hi, (int)tileA[k][3]) && i != self && seed_in_range(r2)) {
+          double w = SB.m * inv_softened_r3(r2, r2 + soft2);
+          accB.x = fma(w, dx, accB.x);
+          accB.y = fma(w, dy, accB.y);
+          accB.z = fma(w, dz, accB.z);
+          accA.x = fma(w, dx, accA.x);
+          accA.y = fma(w, dy, accA.y);
+          accA.z = fma(w, dz, accA.z);
+        } else {
+          pair_fast<false>(pos, self, i, SB, soft2, accB);
+          FastSrc SA = SB;
+          SA.rc = tileA[k][0];
+          SA.rc01 = tileA[k][1];
+          SA.rc09 = tileA[k][2];
+          SA.rc2_hi = (int)tileA[k][3];
+          pair_fast<false>(pos, self, i, SA, soft2, accA);
+        }
+      }
+    }
+  }
+  if (!active) return;
+  d3 vel = load3(D.v, n, j);
+  vel.x = fma(accB.x, hdt, vel.x);
+  vel.y = fma(accB.y, hdt, vel.y);
+  vel.z = fma(accB.z, hdt, vel.z);
+  kick_epilogue(D, j, local, nm, pos, vel, nullptr, 0.0, eject_r2, 1);
+  vel.x = fma(accA.x, hdt, vel.x);
+  vel.y = fma(accA.y, hdt, vel.y);
+  vel.z = fma(accA.z, hdt, vel.z);
+  store3(D.v, n, j, vel);
+}
+
 // Sum of the chunk partials in chunk order, then the kick of big-system bodies
 // with more than one chunk.
 __global__ void k_kick_reduce(Dev D, double* __restrict__ rc_out, double hdt, double hill, double eject_r2,
@@ -398,6 +470,8 @@ struct SymTask {
 struct RotSrc {
   double x, y, z, m;
   int thr, idx;
+  F4 f;       // FP32 position copy (encounter prefilter)
+  float rcf;  // r_crit in FP32 (encounter prefilter)
 };
 
 __device__ __forceinline__ void rotate(RotSrc& r, d3& acc, bool& flag) {
@@ -408,6 +482,11 @@ __device__ __forceinline__ void rotate(RotSrc& r, d3& acc, bool& flag) {
   r.m = __shfl_sync(0xffffffffu, r.m, src);
   r.thr = __shfl_sync(0xffffffffu, r.thr, src);
   r.idx = __shfl_sync(0xffffffffu, r.idx, src);
+  r.f.x = __shfl_sync(0xffffffffu, r.f.x, src);
+  r.f.y = __shfl_sync(0xffffffffu, r.f.y, src);
+  r.f.z = __shfl_sync(0xffffffffu, r.f.z, src);
+  r.f.sc = __shfl_sync(0xffffffffu, r.f.sc, src);
+  r.rcf = __shfl_sync(0xffffffffu, r.rcf, src);
   acc.x = __shfl_sync(0xffffffffu, acc.x, src);
   acc.y = __shfl_sync(0xffffffffu, acc.y, src);
   acc.z = __shfl_sync(0xffffffffu, acc.z, src);
@@ -432,6 +511,8 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
   A.m = iv ? D.m[b0 + i] : 0.0;
   A.thr = iv ? (int)rc[4 * (size_t)(b0 + i) + 3] : 0x7fffffff;
   A.idx = i;
+  A.f = (!KICK && iv) ? load_f4(D, b0 + i) : F4{0.f, 0.f, 0.f, 0.f};
+  A.rcf = (!KICK && iv) ? (float)rc[4 * (size_t)(b0 + i)] : 0.f;
   const int j0 = 32 * T.J + lane;
   const bool jv0 = j0 < nm;
   B.x = jv0 ? D.x[b0 + j0] : 0.0;
@@ -440,6 +521,8 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
   B.m = jv0 ? D.m[b0 + j0] : 0.0;
   B.thr = jv0 ? (int)rc[4 * (size_t)(b0 + j0) + 3] : 0x7fffffff;
   B.idx = jv0 ? j0 : -1;
+  B.f = (!KICK && jv0) ? load_f4(D, b0 + j0) : F4{0.f, 0.f, 0.f, 0.f};
+  B.rcf = (!KICK && jv0) ? (float)rc[4 * (size_t)(b0 + j0)] : 0.f;
   d3 accA = {0.0, 0.0, 0.0}, accB = {0.0, 0.0, 0.0};
   bool ceA = false, ceB = false;
   const bool diag = T.I == T.J;
@@ -452,8 +535,20 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
   for (int k = kbeg; k <= kend; k++) {
     const bool act = iv && B.idx >= 0 && !(diag && k == 16 && lane >= 16);
     if (act) {
+      if (!KICK) {
+        // encounter of i with source j uses r_crit(j), of j with i uses r_crit(i);
+        // the FP32 prefilter clears far pairs without FP64 work
+        const bool mA = ce_maybe(A.f, B.f, B.rcf), mB = ce_maybe(B.f, A.f, A.rcf);
+        if (mA || mB) {
+          const double dx = B.x - A.x, dy = B.y - A.y, dz = B.z - A.z;
+          const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+          const int h = __double2hiint(r2);
+          if (mA && h <= B.thr) ceA = ceA || sqrt(r2) < rc[4 * (size_t)(b0 + B.idx)];
+          if (mB && h <= A.thr) ceB = ceB || sqrt(r2) < rc[4 * (size_t)(b0 + A.idx)];
+        }
+      }
       const double dx = B.x - A.x, dy = B.y - A.y, dz = B.z - A.z;
-      const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+      const double r2 = KICK ? fma(dx, dx, fma(dy, dy, dz * dz)) : 0.0;
       const int h = __double2hiint(r2);
       if (KICK) {
         if (h > max(A.thr, B.thr) && seed_in_range(r2)) {
@@ -471,10 +566,6 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
           pair_exact<false>(pa, A.idx, B.idx, load_src(D, rc, b0 + B.idx), soft2, accA);
           pair_exact<false>(pb, B.idx, A.idx, load_src(D, rc, b0 + A.idx), soft2, accB);
         }
-      } else {
-        // encounter of i with source j uses r_crit(j), of j with i uses r_crit(i)
-        if (h <= B.thr) ceA = ceA || sqrt(r2) < rc[4 * (size_t)(b0 + B.idx)];
-        if (h <= A.thr) ceB = ceB || sqrt(r2) < rc[4 * (size_t)(b0 + A.idx)];
       }
     }
     rotate(B, accB, ceB);
@@ -525,7 +616,7 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
 // partial; the eight sums are combined by a fixed butterfly, so the result does
 // not depend on scheduling.
 __global__ void k_kick_reduce_sym(Dev D, double* __restrict__ rc_out, double hdt, double hill, double eject_r2,
-                                  int last) {
+                                  int last, int massive_only) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = t >> 3, sub = t & 7;
   const bool valid = j < D.n;
@@ -543,7 +634,7 @@ __global__ void k_kick_reduce_sym(Dev D, double* __restrict__ rc_out, double hdt
       base = D.part_sym + D.sym_base[s];
       stride = 3 * (size_t)nm;
       index = local;
-    } else if (D.nchunk[s] > 1) {
+    } else if (D.nchunk[s] > 1 && !massive_only) {
       count = D.nchunk[s];
       base = D.part;
       stride = 3 * (size_t)n;
@@ -578,20 +669,23 @@ __global__ void k_kick_reduce_sym(Dev D, double* __restrict__ rc_out, double hdt
 __global__ void __launch_bounds__(kTile) k_ce_tiled(Dev D, const Work* __restrict__ work,
                                                     const double* __restrict__ rc_in, int compat_block) {
   __shared__ FastSrc tile[kSrcTile];
+  __shared__ F4 tilef[kSrcTile];
   const Work W = work[blockIdx.x];
   const int n = D.n, s = W.sys, b0 = D.off[s], b1 = D.off[s + 1];
   const int j = W.t0 + threadIdx.x;
   const bool active = j < b1;
   const int self = self_index(j - b0, compat_block);
   d3 pos = active ? load3(D.x, n, j) : d3{0.0, 0.0, 0.0};
+  F4 pf = active ? load_f4(D, j) : F4{0.f, 0.f, 0.f, 0.f};
   bool ce = false;
   for (int c = W.c0; c < W.c1; c += kSrcTile) {
     const int cnt = min(kSrcTile, W.c1 - c);
     __syncthreads();
     stage_sources(D, rc_in, b0, c, cnt, tile);
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) tilef[k] = load_f4(D, b0 + c + k);
     __syncthreads();
     if (active)
-      for (int k = 0; k < cnt; k++) ce = ce || pair_ce(pos, self, c + k, tile[k]);
+      for (int k = 0; k < cnt; k++) ce = ce || pair_ce_f(pos, pf, self, c + k, tile[k], tilef[k]);
   }
   if (active && ce) D.ce[j] = 1;
 }
@@ -657,8 +751,10 @@ __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, doubl
       ce_big = is_ce;
     } else {
       const int self = self_index(j - b0, compat_block);
+      const F4 pf = load_f4(D, j);
       is_ce = false;
-      for (int i = 0; i < nm; i++) is_ce = is_ce || pair_ce(pos, self, i, load_src(D, rc_in, b0 + i));
+      for (int i = 0; i < nm; i++)
+        is_ce = is_ce || pair_ce_f(pos, pf, self, i, load_src(D, rc_in, b0 + i), load_f4(D, b0 + i));
       D.ce[j] = is_ce;
       ce_small = is_ce;
     }

@@ -87,7 +87,9 @@ __global__ void k_sweep_persistent(SweepArgs A) {
   double* XO = TB + 4 * kSweepMaxNm;         // 3 x 32 drift output of massive bodies
   double* VO = XO + 3 * kSweepMaxNm;         // 3 x 32
   double* P = VO + 3 * kSweepMaxNm;          // 4
-  uint32_t* F = (uint32_t*)(P + 4);          // nmax flags
+  F4* SF = (F4*)(P + 4);                     // 32 FP32 copies of the massive positions + r_crit (prefilter)
+  float* SRC = (float*)(SF + kSweepMaxNm);   // 32 r_crit (FP32)
+  uint32_t* F = (uint32_t*)(SRC + kSweepMaxNm);  // nmax flags
   float* blob = (float*)(F + nmax + (nmax & 1));  // kBlob floats when warm start is on
   __shared__ int sys_slot;
   __shared__ unsigned long long tally[4];    // encounter body-steps, iterations, solves, non-converged
@@ -168,6 +170,8 @@ __global__ void k_sweep_persistent(SweepArgs A) {
       if (tid < nm) {
         d3 x = {X[tid], X[nmax + tid], X[2 * nmax + tid]}, v = {V[tid], V[nmax + tid], V[2 * nmax + tid]};
         rc_entry(TB, tid, x, v, M[tid], A.hill);
+        SF[tid] = f4_of((float)x.x, (float)x.y, (float)x.z);
+        SRC[tid] = (float)TB[4 * tid];
       }
       __syncthreads();
       // encounter test and drift / encounter sub-step (sources frozen: the
@@ -175,8 +179,10 @@ __global__ void k_sweep_persistent(SweepArgs A) {
       for (int j = tid; j < n; j += T) {
         d3 pos = {X[j], X[nmax + j], X[2 * nmax + j]}, vel = {V[j], V[nmax + j], V[2 * nmax + j]};
         const int self = self_index(j, A.compat_block);
+        const F4 pf = f4_of((float)pos.x, (float)pos.y, (float)pos.z);
         bool ce = false;
-        for (int i = 0; i < nm; i++) ce = ce || pair_ce(pos, self, i, smem_src(X, M, TB, nmax, i));
+        for (int i = 0; i < nm; i++)
+          ce = ce || (ce_maybe(pf, SF[i], SRC[i]) && pair_ce(pos, self, i, smem_src(X, M, TB, nmax, i)));
         PV out;
         if (ce) {
           SmemVelTotal vt{X, M, TB, nmax, nm, self, A.soft2};

@@ -17,9 +17,19 @@ pytestmark = pytest.mark.gpu
 
 
 def rel_err(a, b):
+    """Per-body relative difference; bodies that are non-finite in both count
+    as equal (the reference's element conversion yields NaN for a few very
+    eccentric orbits, src/sim.cuh:90-126 with 8 fixed iterations), a body that
+    is non-finite in only one of them counts as a failure."""
     a = a.reshape(3, -1)
     b = b.reshape(3, -1)
-    return np.max(np.abs(a - b), axis=0) / np.maximum(np.linalg.norm(b, axis=0), 1e-300)
+    fa, fb = np.isfinite(a).all(0), np.isfinite(b).all(0)
+    out = np.zeros(a.shape[1])
+    both = fa & fb
+    out[both] = np.max(np.abs(a[:, both] - b[:, both]), axis=0) / np.maximum(np.linalg.norm(b[:, both], axis=0),
+                                                                             1e-300)
+    out[fa != fb] = np.inf
+    return out
 
 
 def run_both(oracle, sysm, steps, **kw):
@@ -169,3 +179,23 @@ def test_persistent_sweep_kernel_equals_per_phase_kernels():
     assert ta.kepler_iterations == tb.kepler_iterations and ta.ce_body_steps == tb.ce_body_steps
     a.close()
     b.close()
+
+
+def test_planetesimal_disk_merged_test_particle_kicks(oracle):
+    """A big system with many test particles (one source chunk): adjacent half
+    kicks of the test particles are merged inside the step graph.  Parity with
+    the oracle at 1e-12, and the result does not depend on how the steps are
+    split into calls."""
+    sysm = systems.planetesimal_disk(seed=41, n_planetesimals=32, n_test=80000)
+    st, gs, alag, (op, ov, oal, of, ost) = run_both(oracle, sysm, 20, drift=merc.DRIFT_UNIVERSAL)
+    assert rel_err(st.pos, op).max() <= 1e-12
+    assert rel_err(st.vel, ov).max() <= 1e-12
+    assert np.array_equal(st.flags, of)
+    g = merc.Integrator(merc.default_params(dt=sysm.dt, hill_factor=sysm.hill_factor, drift=merc.DRIFT_UNIVERSAL))
+    g.load_systems(sysm)
+    g.step(3)
+    g.step(9)
+    g.step(8)
+    s2 = g.state()
+    g.close()
+    assert np.array_equal(s2.pos, st.pos, equal_nan=True) and np.array_equal(s2.vel, st.vel, equal_nan=True)
