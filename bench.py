@@ -8,11 +8,14 @@ universal-variable drift.  Synthetic, seeded initial conditions.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-ours:       K timed steps on the GPU through libmerc.so, one CUDA-graph step per
-            timed iteration with the L2 flushed (512 MB write) in between;
-            `value` is device time (CUDA events), `e2e` is host wall time of the
+ours:       K timed steps on the GPU through libmerc.so.  One bench step is one
+            merc_step call that advances the system by --batch integrator steps
+            (default 8, one replay of the step graph; the reference likewise
+            advances BATCH_SIZE steps per kernel launch), with the L2 flushed
+            (512 MB write) between calls; `value` counts integrator body-steps
+            over device time (CUDA events), `e2e` is host wall time of the
             public C-ABI call sequence set_state (H2D, pinned) -> step -> get_state
-            (D2H) per step.  Also reported: kick-kernel roofline against the
+            (D2H) per bench step.  Also reported: kick-kernel roofline against the
             measured FP64 FMA peak, the CPU oracle on the host cores, and the
             element-drift (reference-compat) path.
 reference:  the CPU restatement of the reference step (oracle/, OpenMP over all
@@ -162,19 +165,21 @@ def run_reference(args, world, rank, dist):
     O = Oracle()
     p = oparams(**kw)
     pos, vel, alag = O.load_elements(p, sysm.body_offset, sysm.n_massive, sysm.mass, sysm.elements)
+    S = args.batch
     pos, vel, alag, fl, _ = O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag,
-                                  steps=args.warmup)
+                                  steps=args.warmup * S)
     t0 = time.perf_counter()
-    O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag, flags=fl, steps=args.steps)
+    O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag, flags=fl, steps=args.steps * S)
     dt = time.perf_counter() - t0
-    value = sysm.n_total * args.steps / dt
+    value = sysm.n_total * S * args.steps / dt
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": sysm.label, "bodies": sysm.n_total, "dt": sysm.dt, "drift": "universal",
-                       "hill_factor": sysm.hill_factor},
+            "config": {"workload": sysm.label, "bodies": sysm.n_total, "n_massive": int(sysm.n_massive[0]),
+                       "dt": sysm.dt, "drift": "universal", "hill_factor": sysm.hill_factor, "batch": S,
+                       "step": f"{S} integrator steps"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.threads(), "kind": "port",
-                             "sample": f"{args.steps} full steps after {args.warmup} warm-up steps"},
+                             "sample": f"{args.steps * S} full integrator steps after {args.warmup * S} warm-up steps"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "CPU restatement of the reference step (the reference ships CUDA only)"}
     print(json.dumps(line), flush=True)
@@ -296,9 +301,10 @@ def run_ours(args, world, rank, local, dist):
     if dist is not None:
         dist.barrier()
     step_ms, kick_ms, kick_n = [], 0.0, 0
+    S = args.batch
     for _ in range(args.steps):
         g.flush_l2(512 << 20)
-        g.step(1)
+        g.step(S)
         step_ms.append(g.stats().last_step_ms)
         km, kc = g.kick_ms()
         kick_ms += km * kc
@@ -308,7 +314,7 @@ def run_ours(args, world, rank, local, dist):
     ck = clocks.stop()
     launches = g.launch_count() - l0
     total_ms = max_over_ranks(dist, float(np.sum(step_ms)))
-    value = sum_over_ranks(dist, float(n * args.steps)) / (total_ms / 1e3)
+    value = sum_over_ranks(dist, float(n * S * args.steps)) / (total_ms / 1e3)
     kick_avg_ms = kick_ms / max(kick_n, 1)
     nm = int(sysm.n_massive[0])
     pairs_per_kick = nm * (nm - 1) + (n - nm) * nm
@@ -330,12 +336,12 @@ def run_ours(args, world, rank, local, dist):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         g.set_state(pos_h, vel_h, alag_h)
-        g.step(1)
+        g.step(S)
         out = g.state()
         pos_h[:] = out.pos
         vel_h[:] = out.vel
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
-    e2e_value = sum_over_ranks(dist, float(n * e2e_steps)) / e2e_s
+    e2e_value = sum_over_ranks(dist, float(n * S * e2e_steps)) / e2e_s
 
     # element-drift (reference-compat, bitwise-checked) path, same workload
     compat = None
@@ -360,9 +366,11 @@ def run_ours(args, world, rank, local, dist):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded embryo disk)",
         "config": {"workload": sysm.label, "bodies": n, "n_massive": nm, "dt": sysm.dt, "drift": "universal",
-                   "hill_factor": sysm.hill_factor, "l2": "flushed (512 MB write) between timed steps",
+                   "hill_factor": sysm.hill_factor, "batch": S,
+                   "step": f"one merc_step call of {S} integrator steps",
+                   "l2": "flushed (512 MB write) between timed steps",
                    "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "fp64", "kernel": "k_kick", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+        "roofline": {"bound": "fp64", "kernel": "k_sym (far-field pair sweep of the kick)", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "measured FP64 FMA loop on this GPU (merc_diag_fp64_peak)",
                      "kick_ms": kick_avg_ms, "kick_launches": kick_n, "pairs_per_launch": pairs_per_kick,
@@ -387,6 +395,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=8, help="integrator steps per bench step (one merc_step call)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-compat", action="store_true")
     ap.add_argument("--skip-sweep", action="store_true")

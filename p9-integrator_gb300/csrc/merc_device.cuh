@@ -34,6 +34,20 @@ __device__ __forceinline__ double rsqrt_ieee(double x) { return 1.0 / sqrt(x); }
 
 // Changeover radius of a source: hill_factor x Hill radius, a from h and e
 // (sim.cuh:133-164).
+// r_crit = a * hc with hc = cbrt(m / 3) * hill_factor (a per-body constant)
+__device__ __forceinline__ double rcrit_hc(const d3& r, const d3& v, double hc) {
+  d3 h = {fma(r.y, v.z, -r.z * v.y), fma(r.z, v.x, -r.x * v.z), fma(r.x, v.y, -r.y * v.x)};
+  double h2 = mag2(h);
+  double rmag = sqrt(mag2(r));
+  double v2 = mag2(v);
+  double rdv = fma(r.x, v.x, fma(r.y, v.y, r.z * v.z));
+  double factor = v2 - 1.0 / rmag;
+  d3 ev = {fma(factor, r.x, -rdv * v.x), fma(factor, r.y, -rdv * v.y), fma(factor, r.z, -rdv * v.z)};
+  double e2 = mag2(ev);
+  double a = h2 / (1.0 - e2);
+  return a * hc;
+}
+
 __device__ __forceinline__ double rcrit(const d3& r, const d3& v, double m, double hill) {
   d3 h = {fma(r.y, v.z, -r.z * v.y), fma(r.z, v.x, -r.x * v.z), fma(r.x, v.y, -r.y * v.x)};
   double h2 = mag2(h);

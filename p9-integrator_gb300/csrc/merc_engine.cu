@@ -81,10 +81,11 @@ struct merc_ctx {
   int enc_blocks = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<cudaEvent_t> kick_ev;  // start/end pairs recorded around kicks inside the graph
+  std::vector<char> kick_ev_used;    // slots recorded by the captured graphs
   bool time_kicks = false;
   int64_t steps_done = 0;
   int64_t launches = 0;
-  int kernels_per_step = 0;
+  int kernels_graph = 0, kernels_graph1 = 0;  // kernels per replay of each graph
   // persistent small-system path: size order, work counter, tuned block size
   int* d_order = nullptr;
   int* d_queue = nullptr;
@@ -238,9 +239,12 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
         w.chunk = c;
         work_tp.push_back(w);
       }
+    // off-diagonal block pairs (full 32x32) first, the half-length diagonal
+    // ones last: blocks start in index order, so the short tasks fill the tail
     const int NB = (nm[s] + 31) / 32;
     for (int I = 0; I < NB; I++)
-      for (int J = I; J < NB; J++) sym.push_back(SymTask{s, I, J});
+      for (int J = I + 1; J < NB; J++) sym.push_back(SymTask{s, I, J});
+    for (int I = 0; I < NB; I++) sym.push_back(SymTask{s, I, I});
     sym_base[s] = sym_total;
     sym_total += (long long)NB * 3 * nm[s];
   }
@@ -254,6 +258,7 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
   Dev& D = ctx->D;
   D.n = n;
   D.nsys = n_systems;
+  const long long sym_set = std::max<long long>(3, sym_total);  // a multiple of 3 (NB * 3 * nm per system)
   int st;
   if ((st = dalloc(ctx, &ctx->d_big, n_systems)) || (st = dalloc(ctx, &ctx->d_nchunk, n_systems)) ||
       (st = dalloc(ctx, &ctx->d_work, std::max(1, ctx->n_work))) ||
@@ -261,15 +266,21 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
       (st = dalloc(ctx, &D.part, ctx->any_multi ? (size_t)max_chunks * 3 * n : 1)) ||
       (st = dalloc(ctx, &D.ce_list_big, n)) || (st = dalloc(ctx, &ctx->d_work_tp, std::max(1, ctx->n_work_tp))) ||
       (st = dalloc(ctx, &ctx->d_sym, std::max(1, ctx->n_sym))) ||
-      (st = dalloc(ctx, &ctx->d_sym_base, n_systems)) || (st = dalloc(ctx, &D.part_sym, std::max<long long>(1, sym_total))))
+      (st = dalloc(ctx, &ctx->d_sym_base, n_systems)) ||
+      (st = dalloc(ctx, &D.part_sym, 2 * (size_t)sym_set)) || (st = dalloc(ctx, &D.near_mask, 2 * (size_t)(sym_set / 3))) ||
+      (st = dalloc(ctx, &D.gate, 1)) || (st = dalloc(ctx, &D.far_recomputes, 1)))
     return st;
+  D.sym_set = sym_set;
+  CK(cudaMemsetAsync(D.gate, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(D.far_recomputes, 0, sizeof(unsigned long long), ctx->stream));
   if ((st = dalloc(ctx, &ctx->d_off, n_systems + 1)) || (st = dalloc(ctx, &ctx->d_nm, n_systems)) ||
-      (st = dalloc(ctx, &ctx->d_sys, n)) || (st = dalloc(ctx, &ctx->d_m, n)) || (st = dalloc(ctx, &D.x, 3 * (size_t)n)) ||
+      (st = dalloc(ctx, &ctx->d_sys, n)) || (st = dalloc(ctx, &ctx->d_m, n)) || (st = dalloc(ctx, &D.hc, n)) ||
+      (st = dalloc(ctx, &D.x, 3 * (size_t)n)) ||
       (st = dalloc(ctx, &D.v, 3 * (size_t)n)) || (st = dalloc(ctx, &D.xo, 3 * (size_t)n)) ||
       (st = dalloc(ctx, &D.xf, 3 * (size_t)n)) ||
       (st = dalloc(ctx, &D.vo, 3 * (size_t)n)) || (st = dalloc(ctx, &D.alag, n)) || (st = dalloc(ctx, &D.flags, n)) ||
-      (st = dalloc(ctx, &D.ce, n)) || (st = dalloc(ctx, &D.rc[0], 4 * (size_t)n)) ||
-      (st = dalloc(ctx, &D.rc[1], 4 * (size_t)n)) || (st = dalloc(ctx, &D.P, 3 * (size_t)n_systems)) ||
+      (st = dalloc(ctx, &D.ce, n)) || (st = dalloc(ctx, &D.rc[0], rc_table_doubles(n))) ||
+      (st = dalloc(ctx, &D.rc[1], rc_table_doubles(n))) || (st = dalloc(ctx, &D.P, 3 * (size_t)n_systems)) ||
       (st = dalloc(ctx, &D.ce_list, n)) || (st = dalloc(ctx, &D.ce_count, 2)) || (st = dalloc(ctx, &D.counters, 4)))
     return st;
   {
@@ -311,8 +322,8 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
   CK(cudaMemsetAsync(D.flags, 0, sizeof(uint32_t) * n, s));
   CK(cudaMemsetAsync(D.ce, 0, n, s));
   CK(cudaMemsetAsync(D.counters, 0, sizeof(unsigned long long) * 4, s));
-  CK(cudaMemsetAsync(D.rc[0], 0, sizeof(double) * 4 * n, s));
-  CK(cudaMemsetAsync(D.rc[1], 0, sizeof(double) * 4 * n, s));
+  CK(cudaMemsetAsync(D.rc[0], 0, sizeof(double) * rc_table_doubles(n), s));
+  CK(cudaMemsetAsync(D.rc[1], 0, sizeof(double) * rc_table_doubles(n), s));
   CK(cudaStreamSynchronize(s));  // the host vectors above are temporaries
   ctx->enc_blocks = dev_sms * 4;
   ctx->steps_done = 0;
@@ -351,8 +362,11 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
   double* rcB = D.rc[ctx->rc_cur ^ 1];
   int nk = 0;
   auto kick_ev = [&](int k) {
-    if (record_kick_events)
-      CK(cudaEventRecordWithFlags(ctx->kick_ev[4 * (size_t)step_in_graph + k], s, cudaEventRecordExternal));
+    if (record_kick_events) {
+      const size_t slot = 4 * (size_t)step_in_graph + k;
+      CK(cudaEventRecordWithFlags(ctx->kick_ev[slot], s, cudaEventRecordExternal));
+      ctx->kick_ev_used[slot] = 1;
+    }
     return MERC_OK;
   };
   int st;
@@ -377,40 +391,66 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     const bool use_sym = p.compat_block == 0 || p.compat_block >= ctx->max_big_nm;
     // test particles of big systems: adjacent half kicks merged inside a graph
     const bool merge_tp = ctx->has_big && use_sym && ctx->n_work_tp > 0 && !ctx->any_multi;
+    const unsigned nred = (unsigned)((8 * (int64_t)D.n + kThreads - 1) / kThreads);
+    auto tp_kick = [&](const double* rc_in, double* rc_out, int last) {
+      k_kick_tiled<<<ctx->n_work_tp, kTile, 0, s>>>(D, ctx->d_work_tp, rc_in, rc_out, hdt, p.softening2,
+                                                    p.compat_block, p.hill_factor, ej2, last);
+      nk++;
+    };
+    auto reduce = [&](const double* rc_in, const int* gate, double* rc_out, int last, int massive_only, int check) {
+      k_kick_reduce_sym<<<nred, kThreads, 0, s>>>(D, rc_in, gate, rc_out, hdt, p.softening2, p.hill_factor, ej2,
+                                                  last, massive_only, check);
+      nk++;
+    };
+    // far-field pass of the massive bodies (timed as the kick kernel)
+    auto far = [&](const double* rc_in, int set, const int* gate, int ev) {
+      int st2;
+      if (ev >= 0 && (st2 = kick_ev(ev))) return st2;
+      k_sym<true><<<ctx->n_sym, 32, 0, s>>>(D, ctx->d_sym, ctx->n_sym, rc_in, p.softening2, set, gate);
+      nk++;
+      return ev >= 0 ? kick_ev(ev + 1) : MERC_OK;
+    };
     auto kick = [&](const double* rc_in, double* rc_out, int last, int ev) {
       int st2;
-      if ((st2 = kick_ev(ev))) return st2;
       if (ctx->has_small) {
+        if (!(ctx->has_big && use_sym) && (st2 = kick_ev(ev))) return st2;
         k_kick_small<<<nb, kThreads, 0, s>>>(D, rc_in, rc_out, hdt, p.softening2, p.compat_block, p.hill_factor,
                                              ej2, last);
         nk++;
+      } else if (!use_sym || !ctx->has_big) {
+        if ((st2 = kick_ev(ev))) return st2;
       }
       if (ctx->has_big && use_sym) {
-        // massive targets: symmetric block pairs; test particles: tiled
-        k_sym<true><<<ctx->n_sym, 32, 0, s>>>(D, ctx->d_sym, ctx->n_sym, rc_in, p.softening2);
-        nk++;
-        // with merging, the first half kick of the test particles was done by
-        // the previous step's merged kernel (except in the first step)
-        const bool tp_here = ctx->n_work_tp && !(merge_tp && ((!last && !first_in_graph) || (last && !last_in_graph)));
-        if (tp_here && !(merge_tp && last)) {
-          k_kick_tiled<<<ctx->n_work_tp, kTile, 0, s>>>(D, ctx->d_work_tp, rc_in, rc_out, hdt, p.softening2,
-                                                        p.compat_block, p.hill_factor, ej2, last);
-          nk++;
-        }
-        k_kick_reduce_sym<<<(unsigned)((8 * (int64_t)D.n + kThreads - 1) / kThreads), kThreads, 0, s>>>(
-            D, rc_out, hdt, p.hill_factor, ej2, last, merge_tp ? 1 : 0);
-        nk++;
-        if (merge_tp && last) {
-          if (last_in_graph) {
-            k_kick_tiled<<<ctx->n_work_tp, kTile, 0, s>>>(D, ctx->d_work_tp, rc_in, rc_out, hdt, p.softening2,
-                                                          p.compat_block, p.hill_factor, ej2, 1);
-          } else {
-            // rc_out now holds the next step's radii (written by the reduce)
+        if (!last) {
+          // inside a graph the first kick of a step was done by the merged
+          // kick that ended the step before
+          if (!first_in_graph) return MERC_OK;
+          if ((st2 = far(rc_in, 0, nullptr, ev))) return st2;
+          if (ctx->n_work_tp) tp_kick(rc_in, nullptr, 0);
+          reduce(rc_in, nullptr, nullptr, 0, 0, 0);
+        } else if (last_in_graph) {
+          if ((st2 = far(rc_in, 0, nullptr, ev))) return st2;
+          if (ctx->n_work_tp) tp_kick(rc_in, rc_out, 1);
+          reduce(rc_in, nullptr, rc_out, 1, 0, 0);
+        } else {
+          // this kick and the next step's first kick (same positions): the
+          // far field is summed once unless a far-field threshold moved
+          // between them (the reduce sets the gate, the second pass runs)
+          if ((st2 = far(rc_in, 0, nullptr, ev))) return st2;
+          if (ctx->n_work_tp && !merge_tp) tp_kick(rc_in, rc_out, 1);
+          reduce(rc_in, nullptr, rc_out, 1, merge_tp ? 1 : 0, 1);
+          if ((st2 = far(rc_out, 1, D.gate, -1))) return st2;
+          if (merge_tp) {
+            // rc_out holds the next step's radii (written by the reduce)
             k_kick_tiled_merged<<<ctx->n_work_tp, kTile, 0, s>>>(D, ctx->d_work_tp, rc_in, rc_out, hdt,
                                                                  p.softening2, p.compat_block, ej2);
+            nk++;
+          } else if (ctx->n_work_tp) {
+            tp_kick(rc_out, nullptr, 0);
           }
-          nk++;
+          reduce(rc_out, D.gate, nullptr, 0, merge_tp ? 1 : 0, 0);
         }
+        return MERC_OK;
       } else if (ctx->has_big) {
         k_kick_tiled<<<ctx->n_work, kTile, 0, s>>>(D, ctx->d_work, rc_in, rc_out, hdt, p.softening2, p.compat_block,
                                                    p.hill_factor, ej2, last);
@@ -428,7 +468,7 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
         nk++;
       }
       if (ctx->has_big) {
-        k_momentum_big<<<ctx->n_big, kThreads, 0, s>>>(D, ctx->d_big_ids, vsrc);
+        k_momentum_big<<<ctx->n_big, kMomThreads, 0, s>>>(D, ctx->d_big_ids, vsrc);
         nk++;
       }
     };
@@ -439,7 +479,7 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     if (ctx->has_big) {
       CK(cudaMemsetAsync(D.ce, 0, D.n, s));
       if (use_sym) {
-        k_sym<false><<<ctx->n_sym, 32, 0, s>>>(D, ctx->d_sym, ctx->n_sym, rcB, p.softening2);
+        k_sym<false><<<ctx->n_sym, 32, 0, s>>>(D, ctx->d_sym, ctx->n_sym, rcB, p.softening2, 0, nullptr);
         nk++;
         if (ctx->n_work_tp) {
           k_ce_tiled<<<ctx->n_work_tp, kTile, 0, s>>>(D, ctx->d_work_tp, rcB, p.compat_block);
@@ -460,8 +500,12 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       nk++;
     }
     if (ctx->has_big) {
-      k_encounter_cluster<<<ctx->enc_blocks * 2, 32, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
-                                                              p.softening2);
+      if (p.bs_rows == 3)
+        k_encounter_rows<<<(ctx->enc_blocks / 2) * kRowCluster, 32, 0, s>>>(D, rcB, p.dt, p.compat_block,
+                                                                           p.softening2);
+      else
+        k_encounter_cluster<<<ctx->enc_blocks * 2, 32, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
+                                                                p.softening2);
       nk++;
     }
     momentum(D.vo);
@@ -475,13 +519,14 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
 }
 
 // Capture `steps` steps; with timing on, kick events use slots first_slot..
-int capture(merc_ctx* ctx, int steps, bool timed, int first_slot, cudaGraphExec_t* out) {
+int capture(merc_ctx* ctx, int steps, bool timed, int first_slot, cudaGraphExec_t* out, int* kernels) {
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  *kernels = 0;
   for (int k = 0; k < steps; k++) {
     int nk = 0;
     int st = enqueue_step(ctx, timed, first_slot + k, &nk, k == 0, k == steps - 1);
-    ctx->kernels_per_step = nk;
+    *kernels += nk;
     if (st) {
       cudaStreamEndCapture(ctx->stream, &g);
       cudaGraphDestroy(g);
@@ -508,10 +553,11 @@ int build_graphs(merc_ctx* ctx) {
       CK(cudaEventCreate(&e));
       ctx->kick_ev.push_back(e);
     }
+    ctx->kick_ev_used.assign(need, 0);
   }
   int st;
-  if ((st = capture(ctx, kGraphSteps, ctx->time_kicks, 0, &ctx->graph))) return st;
-  if ((st = capture(ctx, 1, ctx->time_kicks, kGraphSteps, &ctx->graph1))) return st;
+  if ((st = capture(ctx, kGraphSteps, ctx->time_kicks, 0, &ctx->graph, &ctx->kernels_graph))) return st;
+  if ((st = capture(ctx, 1, ctx->time_kicks, kGraphSteps, &ctx->graph1, &ctx->kernels_graph1))) return st;
   ctx->graph_steps = kGraphSteps;
   return MERC_OK;
 }
@@ -801,7 +847,7 @@ int merc_step(merc_ctx* ctx, int64_t n_steps) {
     for (int64_t k = 0; k < full; k++) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
     for (int64_t k = 0; k < rest; k++) CK(cudaGraphLaunch(ctx->graph1, ctx->stream));
     ctx->last_graph_steps = rest > 0 ? 1 : kGraphSteps;
-    ctx->launches += n_steps * ctx->kernels_per_step;
+    ctx->launches += full * ctx->kernels_graph + rest * ctx->kernels_graph1;
   }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   CK(cudaEventSynchronize(ctx->ev1));
@@ -1279,9 +1325,10 @@ extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodi
     D.xo = c.take<double>(3 * (size_t)n);
     D.vo = c.take<double>(3 * (size_t)n);
     D.alag = c.take<double>(n);
+    D.hc = c.take<double>(n);
     D.ce = c.take<unsigned char>(n);
-    D.rc[0] = c.take<double>(4 * (size_t)n);
-    D.rc[1] = c.take<double>(4 * (size_t)n);
+    D.rc[0] = c.take<double>(rc_table_doubles(n));
+    D.rc[1] = c.take<double>(rc_table_doubles(n));
     D.P = c.take<double>(3);
     D.part = c.take<double>(C > 1 ? (size_t)C * 3 * n : 1);
     D.ce_list = c.take<int>(n);
@@ -1357,7 +1404,7 @@ extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodi
     if (!big)
       k_momentum<<<1, kThreads, 0, s>>>(D, vsrc, 1);
     else
-      k_momentum_big<<<1, kThreads, 0, s>>>(D, d_ids, vsrc);
+      k_momentum_big<<<1, kMomThreads, 0, s>>>(D, d_ids, vsrc);
   };
   for (int64_t k = 0; k < n_steps; k++) {
     kick(rcA, nullptr, 0);
@@ -1451,6 +1498,18 @@ int merc_diag_flush_l2(merc_ctx* ctx, int64_t bytes) {
   return MERC_OK;
 }
 
+int merc_diag_far_recomputes(merc_ctx* ctx, int64_t* count) {
+  if (!ctx || !count) return MERC_ERR_CONFIG;
+  *count = 0;
+  if (!ctx->loaded || !ctx->D.far_recomputes) return MERC_OK;
+  CK(cudaSetDevice(ctx->device));
+  unsigned long long c = 0;
+  CK(cudaMemcpyAsync(&c, ctx->D.far_recomputes, sizeof c, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *count = (int64_t)c;
+  return MERC_OK;
+}
+
 int merc_diag_time_kicks(merc_ctx* ctx, int on) {
   if (!ctx) return MERC_ERR_CONFIG;
   ctx->time_kicks = on != 0;
@@ -1470,13 +1529,14 @@ int merc_diag_kick_ms(merc_ctx* ctx, double* avg_ms, int32_t* n_launches) {
   const int steps = ctx->last_graph_steps == 1 ? 1 : kGraphSteps;
   for (int k = first; k < first + steps; k++) {
     for (int h = 0; h < 2; h++) {
+      if (!ctx->kick_ev_used[4 * k + 2 * h]) continue;  // a kick merged into the one before
       float ms = 0.f;
       CK(cudaEventElapsedTime(&ms, ctx->kick_ev[4 * k + 2 * h], ctx->kick_ev[4 * k + 2 * h + 1]));
       sum += ms;
       cnt++;
     }
   }
-  *avg_ms = sum / cnt;
+  *avg_ms = cnt ? sum / cnt : 0.0;
   if (n_launches) *n_launches = cnt;
   return MERC_OK;
 }

@@ -41,14 +41,21 @@ struct Dev {
   double* xo = nullptr;      // 3 n, drift output
   double* vo = nullptr;      // 3 n
   const double* m = nullptr;
+  double* hc = nullptr;      // n, cbrt(m / 3) * hill_factor (massive bodies; written by k_rc)
   double* alag = nullptr;
   uint32_t* flags = nullptr;
   unsigned char* ce = nullptr;  // encounter flag of the current step
-  double* rc[2] = {nullptr, nullptr};  // 4 per body: rc, 0.1 rc, 0.9 rc, fast threshold (massive bodies)
+  // 4 doubles per body: rc, 0.1 rc, 0.9 rc, fast threshold (massive bodies),
+  // then one int per body: the far-field threshold (rc_far_thr)
+  double* rc[2] = {nullptr, nullptr};
   double* P = nullptr;               // 3 per system
   double* part = nullptr;            // kick partial sums of test-particle targets [chunk][3][n]
-  double* part_sym = nullptr;        // kick partial sums of massive targets, per system [block][3][nm]
-  const long long* sym_base = nullptr;  // per system: offset of its block partials in part_sym (-1: none)
+  double* part_sym = nullptr;        // far-field partial sums of massive targets, 2 sets of per system [block][3][nm]
+  uint32_t* near_mask = nullptr;     // near-pair bits, 2 sets of per system [block][nm] (one bit per source)
+  const long long* sym_base = nullptr;  // per system: offset of its block partials in a set (-1: none)
+  long long sym_set = 0;             // doubles per partial set (the mask set has sym_set / 3 words)
+  int* gate = nullptr;               // set when a merged kick must recompute the far field
+  unsigned long long* far_recomputes = nullptr;  // gated far-field passes that ran
   int* ce_list = nullptr;            // encounter bodies of small systems
   int* ce_list_big = nullptr;        // encounter bodies of big systems
   int* ce_count = nullptr;           // [0] small list, [1] big list
@@ -75,12 +82,36 @@ __device__ __forceinline__ int self_index(int local, int compat_block) {
   return compat_block > 0 ? local % compat_block : local;
 }
 
-__device__ __forceinline__ void write_rc(double* rc, int j, const d3& x, const d3& v, double m, double hill) {
-  double r = rcrit(x, v, m, hill);
+// Doubles of one r_crit table of n bodies (4 doubles and one int per body).
+__host__ __device__ constexpr size_t rc_table_doubles(size_t n) { return 4 * n + (n + 1) / 2; }
+__device__ __forceinline__ int* rc_far_thr(const double* rc, int n) { return (int*)(rc + 4 * (size_t)n); }
+__device__ __forceinline__ const int* rc_far_thr_c(const double* rc, int n) {
+  return (const int*)(rc + 4 * (size_t)n);
+}
+
+// Far-field radius of a source: kFarRadius Hill-scaled heliocentric
+// distances, T = max(R, r_crit) with R = kFarRadius * |x| * cbrt(m/3) * hill.
+// r_crit = a cbrt(m/3) hill, so T = R whenever a <= kFarRadius |x|, which
+// holds for bound orbits with e < 1/3; then T depends on the position alone
+// and the two kicks around a step boundary (same positions, r_crit before
+// and after the first of them) split their pairs identically.  Returned as
+// the high-word threshold of T^2 (a pair is far when hi(r^2) exceeds it);
+// no far pairs for a source without a finite positive r_crit.
+constexpr double kFarRadius = 1.5;
+__device__ __forceinline__ int far_threshold(double rc, const d3& x, double hc) {
+  if (!(rc > 0.0) || !(rc < 1e150)) return 0x7fffffff;
+  const double R = kFarRadius * hc * sqrt(mag2(x));
+  return rc2_threshold(R > rc ? R : rc);
+}
+
+// r_crit table entries of massive body j; hc = cbrt(m_j / 3) * hill_factor
+__device__ __forceinline__ void write_rc(double* rc, int n, int j, const d3& x, const d3& v, double hc) {
+  double r = rcrit_hc(x, v, hc);
   rc[4 * (size_t)j] = r;
   rc[4 * (size_t)j + 1] = 0.1 * r;
   rc[4 * (size_t)j + 2] = 0.9 * r;
   rc[4 * (size_t)j + 3] = (double)rc2_threshold(r);
+  rc_far_thr(rc, n)[j] = far_threshold(r, x, hc);
 }
 
 __device__ __forceinline__ F4 load_f4(const Dev& D, int g) {
@@ -104,7 +135,7 @@ __device__ __forceinline__ FastSrc load_src(const Dev& D, const double* __restri
 __device__ __forceinline__ void kick_epilogue(const Dev& D, int j, int local, int nm, const d3& pos, const d3& vel,
                                               double* rc_out, double hill, double eject_r2, int last) {
   store3(D.v, D.n, j, vel);
-  if (rc_out && local < nm) write_rc(rc_out, j, pos, vel, D.m[j], hill);
+  if (rc_out && local < nm) write_rc(rc_out, D.n, j, pos, vel, D.hc[j]);
   if (last) {
     uint32_t f = D.flags[j] & ~MERC_FLAG_CE_LAST;
     if (D.ce[j]) f |= MERC_FLAG_CE_LAST | MERC_FLAG_CE_EVER;
@@ -177,7 +208,9 @@ __global__ void k_rc(Dev D, double* rc_out, double hill) {
   if (j >= D.n) return;
   const int s = D.sys[j];
   if (j - D.off[s] >= D.nm[s]) return;
-  write_rc(rc_out, j, load3(D.x, D.n, j), load3(D.v, D.n, j), D.m[j], hill);
+  const double hc = mm::cbrt(D.m[j] / 3.0) * hill;
+  D.hc[j] = hc;
+  write_rc(rc_out, D.n, j, load3(D.x, D.n, j), load3(D.v, D.n, j), hc);
 }
 
 // ---------------------------------------------------------------------------
@@ -221,6 +254,7 @@ __global__ void k_momentum(Dev D, const double* __restrict__ vsrc, int skip_big)
 __global__ void k_jump(Dev D, const double* __restrict__ xsrc, const double* __restrict__ vsrc, double* rc_out,
                        double hdt, double hill) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j == 0 && D.gate) *D.gate = 0;  // the last merged kick has read it
   if (j >= D.n) return;
   const int n = D.n, s = D.sys[j];
   const double px = D.P[3 * s], py = D.P[3 * s + 1], pz = D.P[3 * s + 2];
@@ -239,7 +273,7 @@ __global__ void k_jump(Dev D, const double* __restrict__ xsrc, const double* __r
   } else {
     v = load3(D.v, n, j);
   }
-  if (j - D.off[s] < D.nm[s]) write_rc(rc_out, j, x, v, D.m[j], hill);
+  if (j - D.off[s] < D.nm[s]) write_rc(rc_out, n, j, x, v, D.hc[j]);
 }
 
 // warp-aggregated append to an encounter list (ballot + prefix count)
@@ -461,8 +495,15 @@ __global__ void k_kick_reduce(Dev D, double* __restrict__ rc_out, double hdt, do
 // every lane has met every source and the reverse sums are back home.  Both
 // directions of a pair share d, r^2 and u = 1 / ((r^2 + eps^2) r): 22 FP64
 // operations per unordered pair instead of 2 x 18.  The diagonal block runs
-// k = 1..16 (k = 16 on lanes 0..15 only).  Pairs inside either changeover
-// radius, or outside the seed range, take the reference formula per direction.
+// k = 1..16 (k = 16 on lanes 0..15 only).
+//
+// The kick pass sums the far field only: a pair is far when r exceeds both
+// sources' far-field radii (far_threshold; K = 1 in both directions) and the
+// FP32 seed range allows the fast formula.  Every other pair sets one bit per
+// direction in the near-pair masks, and k_kick_reduce_sym adds those pairs
+// with the reference formula.  The far field depends on the positions and the
+// far-field thresholds only, so a kick whose thresholds equal those of the
+// kick before it (the two kicks around a step boundary) reuses its sums.
 struct SymTask {
   int sys, I, J;
 };
@@ -474,7 +515,8 @@ struct RotSrc {
   float rcf;  // r_crit in FP32 (encounter prefilter)
 };
 
-__device__ __forceinline__ void rotate(RotSrc& r, d3& acc, bool& flag) {
+template <bool KICK>
+__device__ __forceinline__ void rotate(RotSrc& r, d3& acc, uint32_t& bits) {
   const int src = (threadIdx.x + 1) & 31;
   r.x = __shfl_sync(0xffffffffu, r.x, src);
   r.y = __shfl_sync(0xffffffffu, r.y, src);
@@ -482,26 +524,35 @@ __device__ __forceinline__ void rotate(RotSrc& r, d3& acc, bool& flag) {
   r.m = __shfl_sync(0xffffffffu, r.m, src);
   r.thr = __shfl_sync(0xffffffffu, r.thr, src);
   r.idx = __shfl_sync(0xffffffffu, r.idx, src);
-  r.f.x = __shfl_sync(0xffffffffu, r.f.x, src);
-  r.f.y = __shfl_sync(0xffffffffu, r.f.y, src);
-  r.f.z = __shfl_sync(0xffffffffu, r.f.z, src);
-  r.f.sc = __shfl_sync(0xffffffffu, r.f.sc, src);
-  r.rcf = __shfl_sync(0xffffffffu, r.rcf, src);
-  acc.x = __shfl_sync(0xffffffffu, acc.x, src);
-  acc.y = __shfl_sync(0xffffffffu, acc.y, src);
-  acc.z = __shfl_sync(0xffffffffu, acc.z, src);
-  flag = __shfl_sync(0xffffffffu, (int)flag, src) != 0;
+  if (!KICK) {
+    r.f.x = __shfl_sync(0xffffffffu, r.f.x, src);
+    r.f.y = __shfl_sync(0xffffffffu, r.f.y, src);
+    r.f.z = __shfl_sync(0xffffffffu, r.f.z, src);
+    r.f.sc = __shfl_sync(0xffffffffu, r.f.sc, src);
+    r.rcf = __shfl_sync(0xffffffffu, r.rcf, src);
+  } else {
+    acc.x = __shfl_sync(0xffffffffu, acc.x, src);
+    acc.y = __shfl_sync(0xffffffffu, acc.y, src);
+    acc.z = __shfl_sync(0xffffffffu, acc.z, src);
+  }
+  bits = __shfl_sync(0xffffffffu, bits, src);
 }
 
-// KICK: accumulate accelerations; !KICK: encounter test flags.
+// KICK: far-field sums and near-pair masks into partial set `set` (thresholds
+// from rc's far-field table); with `gate`, only when *gate is set.
+// !KICK: encounter test flags (rc's fast thresholds).
 template <bool KICK>
 __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ tasks, int ntasks,
-                                             const double* __restrict__ rc, double soft2) {
+                                             const double* __restrict__ rc, double soft2, int set,
+                                             const int* __restrict__ gate) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp >= ntasks) return;  // whole warps leave together
+  if (KICK && gate && *gate == 0) return;
   const int lane = threadIdx.x & 31;
+  if (KICK && gate && warp == 0 && lane == 0) atomicAdd(D.far_recomputes, 1ull);
   const SymTask T = tasks[warp];
   const int s = T.sys, b0 = D.off[s], nm = D.nm[s];
+  const int* far_thr = rc_far_thr_c(rc, D.n);
   const int i = 32 * T.I + lane;
   const bool iv = i < nm;
   RotSrc A, B;
@@ -509,7 +560,7 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
   A.y = iv ? D.x[D.n + b0 + i] : 0.0;
   A.z = iv ? D.x[2 * D.n + b0 + i] : 0.0;
   A.m = iv ? D.m[b0 + i] : 0.0;
-  A.thr = iv ? (int)rc[4 * (size_t)(b0 + i) + 3] : 0x7fffffff;
+  A.thr = iv ? (KICK ? far_thr[b0 + i] : (int)rc[4 * (size_t)(b0 + i) + 3]) : 0x7fffffff;
   A.idx = i;
   A.f = (!KICK && iv) ? load_f4(D, b0 + i) : F4{0.f, 0.f, 0.f, 0.f};
   A.rcf = (!KICK && iv) ? (float)rc[4 * (size_t)(b0 + i)] : 0.f;
@@ -519,17 +570,19 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
   B.y = jv0 ? D.x[D.n + b0 + j0] : 0.0;
   B.z = jv0 ? D.x[2 * D.n + b0 + j0] : 0.0;
   B.m = jv0 ? D.m[b0 + j0] : 0.0;
-  B.thr = jv0 ? (int)rc[4 * (size_t)(b0 + j0) + 3] : 0x7fffffff;
+  B.thr = jv0 ? (KICK ? far_thr[b0 + j0] : (int)rc[4 * (size_t)(b0 + j0) + 3]) : 0x7fffffff;
   B.idx = jv0 ? j0 : -1;
   B.f = (!KICK && jv0) ? load_f4(D, b0 + j0) : F4{0.f, 0.f, 0.f, 0.f};
   B.rcf = (!KICK && jv0) ? (float)rc[4 * (size_t)(b0 + j0)] : 0.f;
   d3 accA = {0.0, 0.0, 0.0}, accB = {0.0, 0.0, 0.0};
-  bool ceA = false, ceB = false;
+  // KICK: near-pair bits (bit q: source 32 J + q for A, 32 I + q for B);
+  // !KICK: encounter flags
+  uint32_t bitsA = 0u, bitsB = 0u;
   const bool diag = T.I == T.J;
   const int kbeg = diag ? 1 : 0, kend = diag ? 16 : 31;
   int rotations = 0;
   if (diag) {
-    rotate(B, accB, ceB);
+    rotate<KICK>(B, accB, bitsB);
     rotations++;
   }
   for (int k = kbeg; k <= kend; k++) {
@@ -543,14 +596,13 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
           const double dx = B.x - A.x, dy = B.y - A.y, dz = B.z - A.z;
           const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
           const int h = __double2hiint(r2);
-          if (mA && h <= B.thr) ceA = ceA || sqrt(r2) < rc[4 * (size_t)(b0 + B.idx)];
-          if (mB && h <= A.thr) ceB = ceB || sqrt(r2) < rc[4 * (size_t)(b0 + A.idx)];
+          if (mA && h <= B.thr && sqrt(r2) < rc[4 * (size_t)(b0 + B.idx)]) bitsA = 1u;
+          if (mB && h <= A.thr && sqrt(r2) < rc[4 * (size_t)(b0 + A.idx)]) bitsB = 1u;
         }
-      }
-      const double dx = B.x - A.x, dy = B.y - A.y, dz = B.z - A.z;
-      const double r2 = KICK ? fma(dx, dx, fma(dy, dy, dz * dz)) : 0.0;
-      const int h = __double2hiint(r2);
-      if (KICK) {
+      } else {
+        const double dx = B.x - A.x, dy = B.y - A.y, dz = B.z - A.z;
+        const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+        const int h = __double2hiint(r2);
         if (h > max(A.thr, B.thr) && seed_in_range(r2)) {
           const double u = inv_softened_r3(r2, r2 + soft2);
           const double wa = B.m * u, wb = A.m * u;
@@ -561,33 +613,35 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
           accB.y = fma(-wb, dy, accB.y);
           accB.z = fma(-wb, dz, accB.z);
         } else {
-          // reference formula in each direction (self = own index here)
-          const d3 pa = {A.x, A.y, A.z}, pb = {B.x, B.y, B.z};
-          pair_exact<false>(pa, A.idx, B.idx, load_src(D, rc, b0 + B.idx), soft2, accA);
-          pair_exact<false>(pb, B.idx, A.idx, load_src(D, rc, b0 + A.idx), soft2, accB);
+          bitsA |= 1u << (B.idx & 31);
+          bitsB |= 1u << lane;
         }
       }
     }
-    rotate(B, accB, ceB);
+    rotate<KICK>(B, accB, bitsB);
     rotations++;
   }
   // bring the reverse accumulators home: lane t takes from lane t + 32 - R
   {
     const int src = (lane + 32 - (rotations & 31)) & 31;
-    accB.x = __shfl_sync(0xffffffffu, accB.x, src);
-    accB.y = __shfl_sync(0xffffffffu, accB.y, src);
-    accB.z = __shfl_sync(0xffffffffu, accB.z, src);
-    ceB = __shfl_sync(0xffffffffu, (int)ceB, src) != 0;
+    if (KICK) {
+      accB.x = __shfl_sync(0xffffffffu, accB.x, src);
+      accB.y = __shfl_sync(0xffffffffu, accB.y, src);
+      accB.z = __shfl_sync(0xffffffffu, accB.z, src);
+    }
+    bitsB = __shfl_sync(0xffffffffu, bitsB, src);
   }
   if (KICK) {
     const size_t stride = 3 * (size_t)nm;
-    double* base = D.part_sym + D.sym_base[s];
+    double* base = D.part_sym + (size_t)set * D.sym_set + D.sym_base[s];
+    uint32_t* mask = D.near_mask + (size_t)set * (D.sym_set / 3) + D.sym_base[s] / 3;
     if (diag) {
       if (iv) {
         double* p = base + (size_t)T.I * stride;
         p[i] = accA.x + accB.x;
         p[nm + i] = accA.y + accB.y;
         p[2 * nm + i] = accA.z + accB.z;
+        mask[(size_t)T.I * nm + i] = bitsA | bitsB;
       }
     } else {
       if (iv) {
@@ -595,28 +649,35 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
         p[i] = accA.x;
         p[nm + i] = accA.y;
         p[2 * nm + i] = accA.z;
+        mask[(size_t)T.J * nm + i] = bitsA;
       }
       if (jv0) {
         double* p = base + (size_t)T.I * stride;  // block J's slot for source block I
         p[j0] = accB.x;
         p[nm + j0] = accB.y;
         p[2 * nm + j0] = accB.z;
+        mask[(size_t)T.I * nm + j0] = bitsB;
       }
     }
   } else {
-    if (iv && ceA) D.ce[b0 + i] = 1;
-    if (jv0 && ceB) D.ce[b0 + j0] = 1;
+    if (iv && bitsA) D.ce[b0 + i] = 1;
+    if (jv0 && bitsB) D.ce[b0 + j0] = 1;
   }
 }
 
 // Kick of every body of a big system whose sums are in partials: massive
-// bodies add their block partials (symmetric kernel), test particles their
-// chunk partials (when there is more than one chunk; a single chunk was
-// applied by the tiled kernel).  Eight threads per body each add every eighth
-// partial; the eight sums are combined by a fixed butterfly, so the result does
-// not depend on scheduling.
-__global__ void k_kick_reduce_sym(Dev D, double* __restrict__ rc_out, double hdt, double hill, double eject_r2,
-                                  int last, int massive_only) {
+// bodies add their far-field block partials (symmetric kernel, set 1 when
+// *gate is set, else set 0) and then their near pairs (reference formula,
+// rc = the kick's r_crit table); test particles add their chunk partials (when
+// there is more than one chunk; a single chunk was applied by the tiled
+// kernel).  Eight threads per body each take every eighth block; their sums
+// are combined by a fixed butterfly, so the result does not depend on
+// scheduling.  check: after writing rc_out, set *D.gate if a massive body's
+// far-field threshold in rc_out differs from the one in rc (the far field of
+// the next kick must then be recomputed).
+__global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const int* __restrict__ gate,
+                                  double* __restrict__ rc_out, double hdt, double soft2, double hill,
+                                  double eject_r2, int last, int massive_only, int check) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = t >> 3, sub = t & 7;
   const bool valid = j < D.n;
@@ -624,17 +685,21 @@ __global__ void k_kick_reduce_sym(Dev D, double* __restrict__ rc_out, double hdt
   const int s = valid ? D.sys[j] : 0;
   bool work = valid && D.big[s];
   const int b0 = work ? D.off[s] : 0, nm = work ? D.nm[s] : 0, local = j - b0;
+  const bool massive = work && local < nm;
   int count = 0;
   const double* base = nullptr;
+  const uint32_t* mask = nullptr;
   size_t stride = 0;
   int index = 0;
-  if (work) {
-    if (local < nm) {
-      count = (nm + 31) / 32;
-      base = D.part_sym + D.sym_base[s];
-      stride = 3 * (size_t)nm;
-      index = local;
-    } else if (D.nchunk[s] > 1 && !massive_only) {
+  if (massive) {
+    const int set = (gate && *gate) ? 1 : 0;
+    count = (nm + 31) / 32;
+    base = D.part_sym + (size_t)set * D.sym_set + D.sym_base[s];
+    mask = D.near_mask + (size_t)set * (D.sym_set / 3) + D.sym_base[s] / 3;
+    stride = 3 * (size_t)nm;
+    index = local;
+  } else if (work) {
+    if (D.nchunk[s] > 1 && !massive_only) {
       count = D.nchunk[s];
       base = D.part;
       stride = 3 * (size_t)n;
@@ -645,23 +710,47 @@ __global__ void k_kick_reduce_sym(Dev D, double* __restrict__ rc_out, double hdt
   }
   const size_t span = stride / 3;
   d3 acc = {0.0, 0.0, 0.0};
+#pragma unroll 4
   for (int b = sub; b < count; b += 8) {
     const double* p = base + (size_t)b * stride;
     acc.x += p[index];
     acc.y += p[span + index];
     acc.z += p[2 * span + index];
   }
+  d3 near = {0.0, 0.0, 0.0};
+  d3 pos = {0.0, 0.0, 0.0};
+  if (work) pos = load3(D.x, n, j);
+  if (massive) {
+    for (int b = sub; b < count; b += 8) {
+      uint32_t w = mask[(size_t)b * nm + local];
+      while (w) {
+        const int q = __ffs(w) - 1;
+        w &= w - 1u;
+        const int src = 32 * b + q;
+        pair_exact<false>(pos, local, src, load_src(D, rc, b0 + src), soft2, near);
+      }
+    }
+  }
   for (int o = 1; o < 8; o <<= 1) {
     acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
     acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
     acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+    near.x += __shfl_xor_sync(0xffffffffu, near.x, o);
+    near.y += __shfl_xor_sync(0xffffffffu, near.y, o);
+    near.z += __shfl_xor_sync(0xffffffffu, near.z, o);
   }
   if (!work || sub != 0) return;
-  d3 pos = load3(D.x, n, j), vel = load3(D.v, n, j);
+  if (massive) {
+    acc.x += near.x;
+    acc.y += near.y;
+    acc.z += near.z;
+  }
+  d3 vel = load3(D.v, n, j);
   vel.x = fma(acc.x, hdt, vel.x);
   vel.y = fma(acc.y, hdt, vel.y);
   vel.z = fma(acc.z, hdt, vel.z);
   kick_epilogue(D, j, local, nm, pos, vel, rc_out, hill, eject_r2, last);
+  if (check && massive && rc_far_thr_c(rc_out, n)[j] != rc_far_thr_c(rc, n)[j]) atomicOr(D.gate, 1);
 }
 
 // Tiled encounter test of the big systems: any source of the chunk within
@@ -692,10 +781,12 @@ __global__ void __launch_bounds__(kTile) k_ce_tiled(Dev D, const Work* __restric
 
 // Momentum of each big system: block per system, strided partial sums and a
 // fixed-order tree (deterministic).
-__global__ void k_momentum_big(Dev D, const int* __restrict__ big_ids, const double* __restrict__ vsrc) {
+constexpr int kMomThreads = 512;
+__global__ void __launch_bounds__(kMomThreads) k_momentum_big(Dev D, const int* __restrict__ big_ids,
+                                                              const double* __restrict__ vsrc) {
   const int s = big_ids[blockIdx.x];
   const int b0 = D.off[s], nm = D.nm[s], n = D.n;
-  __shared__ double red[3][kThreads];
+  __shared__ double red[3][kMomThreads];
   double px = 0.0, py = 0.0, pz = 0.0;
   for (int i = threadIdx.x; i < nm; i += blockDim.x) {
     double mi = D.m[b0 + i];
@@ -889,6 +980,59 @@ __global__ void __launch_bounds__(kEncThreads) k_encounter_big(Dev D, const doub
   }
 }
 
+// Fast term of one source of the encounter sub-step (sim.cuh:357-361 with
+// r > r_crit, i.e. weight 1), computed without branches so that consecutive
+// sources overlap; returns true when the pair needs the reference formula
+// instead (inside r_crit, the body itself, or outside the seed range), in which
+// case nothing was added.
+__device__ __forceinline__ bool bs_fast_term(const Dev& D, const double* __restrict__ rc, int b0, int self, int i,
+                                             const d3& pos, double soft2, d3& acc) {
+  const int g = b0 + i;
+  const double dx = __ldg(D.x + g) - pos.x, dy = __ldg(D.x + D.n + g) - pos.y, dz = __ldg(D.x + 2 * D.n + g) - pos.z;
+  const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+  const bool far = hi_word(r2) > (int)__ldg(rc + 4 * (size_t)g + 3) && i != self && seed_in_range(r2);
+  const double u = inv_softened_r3(r2, r2 + soft2);
+  const double w = far ? __ldg(D.m + g) * u : 0.0;
+  acc.x = fma(w, dx, acc.x);
+  acc.y = fma(w, dy, acc.y);
+  acc.z = fma(w, dz, acc.z);
+  return !far;
+}
+
+// Sum over sources c0..c1 - 1 of the encounter body's pull, by one warp:
+// sources c0 + lane + 32 k, even k into a0, odd k into a1 (two independent
+// FP64 chains in flight), pairs that need the reference formula marked and
+// added to ae after each chunk of 64 k; then a fixed butterfly, so every lane
+// ends with the same total.
+__device__ __forceinline__ d3 warp_source_sum(const Dev& D, const double* __restrict__ rc, int b0, int c0, int c1,
+                                              int self, const d3& pos, double soft2) {
+  const int lane = (int)(threadIdx.x & 31);
+  d3 a0 = {0.0, 0.0, 0.0}, a1 = {0.0, 0.0, 0.0}, ae = {0.0, 0.0, 0.0};
+  for (int base = c0; base < c1; base += 64 * 32) {
+    const int end = min(c1, base + 64 * 32);
+    unsigned long long slow = 0ull;
+    int k = 0, i = base + lane;
+    for (; i + 32 < end; i += 64, k += 2) {
+      if (bs_fast_term(D, rc, b0, self, i, pos, soft2, a0)) slow |= 1ull << k;
+      if (bs_fast_term(D, rc, b0, self, i + 32, pos, soft2, a1)) slow |= 1ull << (k + 1);
+    }
+    if (i < end && bs_fast_term(D, rc, b0, self, i, pos, soft2, a0)) slow |= 1ull << k;
+    while (slow) {
+      const int q = __ffsll((long long)slow) - 1;
+      slow &= slow - 1ull;
+      const int src = base + lane + 32 * q;
+      pair_exact<true>(pos, self, src, load_src(D, rc, b0 + src), soft2, ae);
+    }
+  }
+  d3 acc = {(a0.x + a1.x) + ae.x, (a0.y + a1.y) + ae.y, (a0.z + a1.z) + ae.z};
+  for (int o = 16; o > 0; o >>= 1) {
+    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+  }
+  return acc;
+}
+
 // Velocity update of an encounter sub-step split over the blocks of a
 // thread-block cluster: block `rank` sums its quarter of the sources (fixed
 // tree), publishes the partial in its shared memory, and after one cluster
@@ -906,15 +1050,7 @@ struct ClusterVelTotal {
   __device__ __forceinline__ d3 operator()(const d3& pos, const d3& vel, double dt) const {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
-    d3 acc = {0.0, 0.0, 0.0};
-    for (int i = c0 + (int)threadIdx.x; i < c1; i += 32)
-      pair_fast<true>(pos, self, i, load_src(*D, rc, b0 + i), soft2, acc);
-    // warp sum in a fixed butterfly order (every lane ends with the total)
-    for (int o = 16; o > 0; o >>= 1) {
-      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
-      acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
-    }
+    d3 acc = warp_source_sum(*D, rc, b0, c0, c1, self, pos, soft2);
     const int buf = *parity & 1;
     if (threadIdx.x == 0) {
       slot[4 * buf] = acc.x;
@@ -965,6 +1101,140 @@ __global__ void __cluster_dims__(kEncCluster, 1, 1) __launch_bounds__(32)
     if (rank == 0 && threadIdx.x == 0) {
       store3(D.xo, n, j, bs.pos);
       store3(D.vo, n, j, bs.vel);
+    }
+  }
+  cl.sync();  // no block leaves while another may still read its slots
+}
+
+// Modified-midpoint state of one Richardson row, one evaluation at a time
+// (the arithmetic of mod_midpoint with ClusterVelTotal's velocity update):
+// the next evaluation is at z1; finish_eval applies the velocity update with
+// the summed pull of the sources and advances to the next evaluation point.
+struct MidRow {
+  d3 z0, z1, vel;
+  double h, h2;
+  int N, done;
+  __device__ __forceinline__ void start(const PV& c, double dt, int nsub) {
+    N = nsub;
+    h = dt / (double)N;
+    h2 = 2.0 * h;
+    done = 0;
+    z1 = {fma(c.vel.x, h, c.pos.x), fma(c.vel.y, h, c.pos.y), fma(c.vel.z, h, c.pos.z)};
+    z0 = c.pos;
+    vel = c.vel;
+  }
+  __device__ __forceinline__ void finish_eval(const d3& acc, double soft2) {
+    const d3 sa = sun_accel(z1, soft2);
+    vel = {fma(sa.x, h, fma(acc.x, h, vel.x)), fma(sa.y, h, fma(acc.y, h, vel.y)),
+           fma(sa.z, h, fma(acc.z, h, vel.z))};
+    if (++done < N) {
+      const d3 t = {fma(h2, vel.x, z0.x), fma(h2, vel.y, z0.y), fma(h2, vel.z, z0.z)};
+      z0 = z1;
+      z1 = t;
+    }
+  }
+  __device__ __forceinline__ PV result() const {
+    PV r;
+    r.pos = {0.5 * (z1.x + fma(vel.x, h, z0.x)), 0.5 * (z1.y + fma(vel.y, h, z0.y)),
+             0.5 * (z1.z + fma(vel.z, h, z0.z))};
+    r.vel = vel;
+    return r;
+  }
+};
+
+// Encounter sub-step with three Richardson rows (N = 1, 2, 4) run side by
+// side: a cluster of 7 one-warp blocks per body, ranks 0-3 on row 2, ranks
+// 4-5 on row 1, rank 6 on row 0.  The rows are independent until the final
+// extrapolation, so the critical path is row 2's four evaluations instead of
+// seven in sequence.  Every evaluation is the sum of four quarter sums of the
+// sources (warp_source_sum over quarter q, added in q order), exactly as in
+// k_encounter_cluster; the work is spread over four rounds with one cluster
+// barrier each: in round k row 2's rank r sums quarter r of evaluation k, row
+// 1's ranks sum quarters 2 (k mod 2) + {0, 1} of evaluation k / 2 + 1, and
+// row 0's rank sums quarter k of its single evaluation.  Results are bit for
+// bit those of k_encounter_cluster with rows = 3.
+constexpr int kRowCluster = 7;
+__global__ void __cluster_dims__(kRowCluster, 1, 1) __launch_bounds__(32)
+    k_encounter_rows(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, double soft2) {
+  namespace cg = cooperative_groups;
+  __shared__ double slot[2][4];  // this block's quarter sum, by round parity
+  __shared__ double res[8];      // final position and velocity of row 0 (rank 6) or row 1 (rank 4)
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int row = rank < 4 ? 2 : (rank < 6 ? 1 : 0);
+  const int cid = blockIdx.x / kRowCluster, ncl = gridDim.x / kRowCluster;
+  const int count = D.ce_count[1];
+  int parity = 0;
+  for (int k = cid; k < count; k += ncl) {
+    const int j = D.ce_list_big[k];
+    const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
+    const int self = self_index(j - b0, compat_block);
+    const PV c = {load3(D.x, n, j), load3(D.v, n, j)};
+    MidRow m;
+    m.start(c, dt, 1 << row);
+    d3 q[4];
+    for (int round = 0; round < 4; round++) {
+      const int quarter = row == 2 ? rank : (row == 1 ? 2 * (round & 1) + (rank - 4) : round);
+      const int c0 = (int)((int64_t)quarter * nm / 4), c1 = (int)((int64_t)(quarter + 1) * nm / 4);
+      const d3 S = warp_source_sum(D, rc_in, b0, c0, c1, self, m.z1, soft2);
+      const int buf = parity & 1;
+      if (threadIdx.x == 0) {
+        slot[buf][0] = S.x;
+        slot[buf][1] = S.y;
+        slot[buf][2] = S.z;
+      }
+      cl.sync();
+      parity++;
+      if (row == 2) {
+        d3 acc = {0.0, 0.0, 0.0};
+        for (int r = 0; r < 4; r++) {
+          const double* rs = cl.map_shared_rank(&slot[buf][0], r);
+          acc.x += rs[0];
+          acc.y += rs[1];
+          acc.z += rs[2];
+        }
+        m.finish_eval(acc, soft2);
+      } else {
+        if (row == 1) {
+          const double* ra = cl.map_shared_rank(&slot[buf][0], 4);
+          const double* rb = cl.map_shared_rank(&slot[buf][0], 5);
+          q[2 * (round & 1)] = {ra[0], ra[1], ra[2]};
+          q[2 * (round & 1) + 1] = {rb[0], rb[1], rb[2]};
+        } else {
+          q[round] = S;
+        }
+        if ((row == 1 && (round & 1)) || round == 3) {
+          d3 acc = {0.0, 0.0, 0.0};
+          for (int r = 0; r < 4; r++) {
+            acc.x += q[r].x;
+            acc.y += q[r].y;
+            acc.z += q[r].z;
+          }
+          m.finish_eval(acc, soft2);
+        }
+      }
+    }
+    const PV mine = m.result();
+    if ((rank == 4 || rank == 6) && threadIdx.x == 0) {
+      res[0] = mine.pos.x;
+      res[1] = mine.pos.y;
+      res[2] = mine.pos.z;
+      res[3] = mine.vel.x;
+      res[4] = mine.vel.y;
+      res[5] = mine.vel.z;
+    }
+    cl.sync();
+    if (rank == 0 && threadIdx.x == 0) {
+      const double* r0 = cl.map_shared_rank(res, 6);
+      const double* r1 = cl.map_shared_rank(res, 4);
+      const PV b00 = {{r0[0], r0[1], r0[2]}, {r0[3], r0[4], r0[5]}};
+      const PV b10 = {{r1[0], r1[1], r1[2]}, {r1[3], r1[4], r1[5]}};
+      PV b11, b21, b22;
+      rich_combine(b11, b10, b00, 4.0);
+      rich_combine(b21, mine, b10, 4.0);
+      rich_combine(b22, b21, b11, 16.0);
+      store3(D.xo, n, j, b22.pos);
+      store3(D.vo, n, j, b22.vel);
     }
   }
   cl.sync();  // no block leaves while another may still read its slots

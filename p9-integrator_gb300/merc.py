@@ -126,6 +126,7 @@ def lib() -> C.CDLL:
     L.merc_diag_fp64_peak.argtypes = [C.c_int, _f64p]
     L.merc_diag_time_kicks.argtypes = [vp, C.c_int]
     L.merc_diag_kick_ms.argtypes = [vp, _f64p, _i32p]
+    L.merc_diag_far_recomputes.argtypes = [vp, C.POINTER(C.c_int64)]
     _LIB = L
     return L
 
@@ -290,6 +291,12 @@ class Integrator:
         cnt = C.c_int32()
         self._check(self.L.merc_diag_kick_ms(self.h, C.byref(ms), C.byref(cnt)))
         return ms.value, cnt.value
+
+    def far_recomputes(self) -> int:
+        """Merged kicks whose far field had to be summed a second time."""
+        c = C.c_int64()
+        self._check(self.L.merc_diag_far_recomputes(self.h, C.byref(c)))
+        return c.value
 
 
 MLP_BLOB = 1267

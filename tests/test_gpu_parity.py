@@ -199,3 +199,36 @@ def test_planetesimal_disk_merged_test_particle_kicks(oracle):
     s2 = g.state()
     g.close()
     assert np.array_equal(s2.pos, st.pos, equal_nan=True) and np.array_equal(s2.vel, st.vel, equal_nan=True)
+
+
+def eccentric_embryo_disk(seed=77, n_embryos=126, n_ecc=40):
+    """Embryo disk in which n_ecc embryos move on e = 0.6 orbits: their
+    far-field radius follows r_crit near pericentre, so it moves between the
+    two kicks around a step boundary."""
+    sysm = systems.embryo_disk(seed=seed, n_embryos=n_embryos)
+    el = sysm.elements.reshape(6, -1)
+    el[4, 2:2 + n_ecc] = 0.6
+    return sysm
+
+
+def test_far_field_recompute_with_eccentric_sources(oracle):
+    """Merged kicks reuse the far field of the kick before unless a far-field
+    threshold moved; with e = 0.6 sources the second pass runs.  Parity with
+    the oracle at 1e-12, and the same bits however the steps are split."""
+    sysm = eccentric_embryo_disk()
+    st, gs, alag, (op, ov, oal, of, ost) = run_both(oracle, sysm, 100, drift=merc.DRIFT_UNIVERSAL)
+    assert rel_err(st.pos, op).max() <= 1e-12
+    assert rel_err(st.vel, ov).max() <= 1e-12
+    assert np.array_equal(st.flags, of)
+    kw = dict(dt=sysm.dt, hill_factor=sysm.hill_factor, drift=merc.DRIFT_UNIVERSAL)
+    a = merc.Integrator(merc.default_params(**kw))
+    a.load_systems(sysm)
+    a.step(24)
+    assert a.far_recomputes() > 0
+    b = merc.Integrator(merc.default_params(**kw))
+    b.load_systems(sysm)
+    for k in (1, 2, 5, 16):
+        b.step(k)
+    assert np.array_equal(a.state().pos, b.state().pos) and np.array_equal(a.state().vel, b.state().vel)
+    a.close()
+    b.close()
