@@ -146,7 +146,7 @@ def cpu_baseline(sysm, params_kw, budget_s=12.0):
     t0 = time.perf_counter()
     pos, vel, alag, fl, _ = O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag, steps=1)
     one = time.perf_counter() - t0
-    steps = int(max(1, min(200, budget_s / max(one, 1e-6))))
+    steps = int(max(1, min(5000, budget_s / max(one, 1e-6))))
     t0 = time.perf_counter()
     O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag, flags=fl, steps=steps)
     dt = time.perf_counter() - t0
