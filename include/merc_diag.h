@@ -50,6 +50,12 @@ int merc_diag_kick_ms(merc_ctx* ctx, double* avg_ms, int32_t* n_launches);
  * such passes ran since the load. */
 int merc_diag_far_recomputes(merc_ctx* ctx, int64_t* count);
 
+/* on != 0 (the default): the kernels of the step graphs are launched as
+ * programmatic dependent launches (scheduled while the previous kernel
+ * finishes; each waits for it before touching memory).  Results do not
+ * depend on it.  Takes effect when the step graphs are next captured. */
+int merc_diag_pdl(merc_ctx* ctx, int on);
+
 #ifdef __cplusplus
 }
 #endif

@@ -83,6 +83,7 @@ struct merc_ctx {
   std::vector<cudaEvent_t> kick_ev;  // start/end pairs recorded around kicks inside the graph
   std::vector<char> kick_ev_used;    // slots recorded by the captured graphs
   bool time_kicks = false;
+  bool pdl = true;  // programmatic dependent launches inside the step graphs
   int64_t steps_done = 0;
   int64_t launches = 0;
   int kernels_graph = 0, kernels_graph1 = 0;  // kernels per replay of each graph
@@ -348,6 +349,25 @@ int dh_convert(merc_ctx* ctx, bool reverse) {
   return MERC_OK;
 }
 
+// Launch on the step stream.  With pdl (programmatic dependent launch) the
+// kernel may be scheduled while its predecessor is still running; every kernel
+// of the step waits for its predecessor in griddep_wait() before it touches
+// memory, so only the launch latency overlaps.
+template <typename... P, typename... A>
+cudaError_t step_launch(bool pdl, cudaStream_t s, void (*k)(P...), dim3 grid, dim3 block, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // Enqueue one step on the stream (also used while capturing the graph);
 // returns the number of kernels it launched through *kernels.
 int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int* kernels, bool first_in_graph,
@@ -376,37 +396,45 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     k_kick<<<nb, kThreads, 0, s>>>(D, rcA, nullptr, hdt, p.softening2, p.compat_block, p.hill_factor, ej2, 0);
     if ((st = kick_ev(1))) return st;
     k_momentum<<<sb, kThreads, 0, s>>>(D, D.v, 0);
-    k_jump<<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt, p.hill_factor);
+    k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt);
     CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
     k_drift_elements<<<nb, kThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.kepler_iters);
     k_encounter_elements<<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2);
     k_momentum<<<sb, kThreads, 0, s>>>(D, D.vo, 0);
-    k_jump<<<nb, kThreads, 0, s>>>(D, D.xo, D.vo, rcB, hdt, p.hill_factor);
+    k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.xo, D.vo, rcB, hdt);
     if ((st = kick_ev(2))) return st;
     k_kick<<<nb, kThreads, 0, s>>>(D, rcB, rcA, hdt, p.softening2, p.compat_block, p.hill_factor, ej2, 1);
     if ((st = kick_ev(3))) return st;
     nk = 8;
   } else {
+    // programmatic dependent launches: a kernel may be scheduled while its
+    // predecessor finishes; every kernel here waits for it (griddep_wait)
+    // before touching memory
+    cudaError_t lerr = cudaSuccess;
+    auto launch = [&](auto k, auto grid, auto block, auto... args) {
+      cudaError_t e = step_launch(ctx->pdl, s, k, dim3((unsigned)grid), dim3((unsigned)block), args...);
+      if (e != cudaSuccess && lerr == cudaSuccess) lerr = e;
+    };
     // the symmetric pair kernels assume a massive body excludes exactly itself
     const bool use_sym = p.compat_block == 0 || p.compat_block >= ctx->max_big_nm;
     // test particles of big systems: adjacent half kicks merged inside a graph
     const bool merge_tp = ctx->has_big && use_sym && ctx->n_work_tp > 0 && !ctx->any_multi;
     const unsigned nred = (unsigned)((8 * (int64_t)D.n + kThreads - 1) / kThreads);
     auto tp_kick = [&](const double* rc_in, double* rc_out, int last) {
-      k_kick_tiled<<<ctx->n_work_tp, kTile, 0, s>>>(D, ctx->d_work_tp, rc_in, rc_out, hdt, p.softening2,
-                                                    p.compat_block, p.hill_factor, ej2, last);
+      launch(k_kick_tiled, ctx->n_work_tp, kTile, D, ctx->d_work_tp, rc_in, rc_out, hdt, p.softening2,
+             p.compat_block, p.hill_factor, ej2, last);
       nk++;
     };
     auto reduce = [&](const double* rc_in, const int* gate, double* rc_out, int last, int massive_only, int check) {
-      k_kick_reduce_sym<<<nred, kThreads, 0, s>>>(D, rc_in, gate, rc_out, hdt, p.softening2, p.hill_factor, ej2,
-                                                  last, massive_only, check);
+      launch(k_kick_reduce_sym, nred, kThreads, D, rc_in, gate, rc_out, hdt, p.softening2, p.hill_factor, ej2,
+             last, massive_only, check);
       nk++;
     };
     // far-field pass of the massive bodies (timed as the kick kernel)
     auto far = [&](const double* rc_in, int set, const int* gate, int ev) {
       int st2;
       if (ev >= 0 && (st2 = kick_ev(ev))) return st2;
-      k_sym<true><<<ctx->n_sym, 32, 0, s>>>(D, ctx->d_sym, ctx->n_sym, rc_in, p.softening2, set, gate);
+      launch(k_sym<true>, ctx->n_sym, 32, D, ctx->d_sym, ctx->n_sym, rc_in, p.softening2, set, gate);
       nk++;
       return ev >= 0 ? kick_ev(ev + 1) : MERC_OK;
     };
@@ -414,8 +442,8 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       int st2;
       if (ctx->has_small) {
         if (!(ctx->has_big && use_sym) && (st2 = kick_ev(ev))) return st2;
-        k_kick_small<<<nb, kThreads, 0, s>>>(D, rc_in, rc_out, hdt, p.softening2, p.compat_block, p.hill_factor,
-                                             ej2, last);
+        launch(k_kick_small, nb, kThreads, D, rc_in, rc_out, hdt, p.softening2, p.compat_block, p.hill_factor,
+               ej2, last);
         nk++;
       } else if (!use_sym || !ctx->has_big) {
         if ((st2 = kick_ev(ev))) return st2;
@@ -442,8 +470,8 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
           if ((st2 = far(rc_out, 1, D.gate, -1))) return st2;
           if (merge_tp) {
             // rc_out holds the next step's radii (written by the reduce)
-            k_kick_tiled_merged<<<ctx->n_work_tp, kTile, 0, s>>>(D, ctx->d_work_tp, rc_in, rc_out, hdt,
-                                                                 p.softening2, p.compat_block, ej2);
+            launch(k_kick_tiled_merged, ctx->n_work_tp, kTile, D, ctx->d_work_tp, rc_in, rc_out, hdt,
+                   p.softening2, p.compat_block, ej2);
             nk++;
           } else if (ctx->n_work_tp) {
             tp_kick(rc_out, nullptr, 0);
@@ -452,66 +480,63 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
         }
         return MERC_OK;
       } else if (ctx->has_big) {
-        k_kick_tiled<<<ctx->n_work, kTile, 0, s>>>(D, ctx->d_work, rc_in, rc_out, hdt, p.softening2, p.compat_block,
-                                                   p.hill_factor, ej2, last);
+        launch(k_kick_tiled, ctx->n_work, kTile, D, ctx->d_work, rc_in, rc_out, hdt, p.softening2, p.compat_block,
+               p.hill_factor, ej2, last);
         nk++;
         if (ctx->any_multi) {
-          k_kick_reduce<<<nb, kThreads, 0, s>>>(D, rc_out, hdt, p.hill_factor, ej2, last);
+          launch(k_kick_reduce, nb, kThreads, D, rc_out, hdt, p.hill_factor, ej2, last);
           nk++;
         }
       }
       return kick_ev(ev + 1);
     };
+    // momentum of the small systems (the big systems' is summed inside k_jump)
     auto momentum = [&](const double* vsrc) {
       if (ctx->has_small) {
-        k_momentum<<<sb, kThreads, 0, s>>>(D, vsrc, 1);
-        nk++;
-      }
-      if (ctx->has_big) {
-        k_momentum_big<<<ctx->n_big, kMomThreads, 0, s>>>(D, ctx->d_big_ids, vsrc);
+        launch(k_momentum, sb, kThreads, D, vsrc, 1);
         nk++;
       }
     };
     if ((st = kick(rcA, nullptr, 0, 0))) return st;
     momentum(D.v);
-    k_jump<<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt, p.hill_factor);
+    // also clears the encounter flags and list counts of this step
+    launch(k_jump<true, true>, nb, kThreads, D, D.x, nullptr, rcB, hdt);
     nk++;
     if (ctx->has_big) {
-      CK(cudaMemsetAsync(D.ce, 0, D.n, s));
       if (use_sym) {
-        k_sym<false><<<ctx->n_sym, 32, 0, s>>>(D, ctx->d_sym, ctx->n_sym, rcB, p.softening2, 0, nullptr);
+        launch(k_sym<false>, ctx->n_sym, 32, D, ctx->d_sym, ctx->n_sym, rcB, p.softening2, 0, nullptr);
         nk++;
         if (ctx->n_work_tp) {
-          k_ce_tiled<<<ctx->n_work_tp, kTile, 0, s>>>(D, ctx->d_work_tp, rcB, p.compat_block);
+          launch(k_ce_tiled, ctx->n_work_tp, kTile, D, ctx->d_work_tp, rcB, p.compat_block);
           nk++;
         }
       } else {
-        k_ce_tiled<<<ctx->n_work, kTile, 0, s>>>(D, ctx->d_work, rcB, p.compat_block);
+        launch(k_ce_tiled, ctx->n_work, kTile, D, ctx->d_work, rcB, p.compat_block);
         nk++;
       }
     }
-    CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
     const float* mlp = (p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) ? ctx->d_mlp : nullptr;
-    k_drift_universal<<<nb, kThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.kepler_tol, p.kepler_max_iter, mlp,
-                                              ctx->d_log, ctx->d_log_count, ctx->log_cap);
+    launch(k_drift_universal, nb, kThreads, D, rcB, p.dt, p.compat_block, p.kepler_tol, p.kepler_max_iter, mlp,
+           ctx->d_log, ctx->d_log_count, ctx->log_cap);
     nk++;
     if (ctx->has_small) {
-      k_encounter_small<<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2);
+      launch(k_encounter_small, ctx->enc_blocks, 64, D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2);
       nk++;
     }
     if (ctx->has_big) {
       if (p.bs_rows == 3)
-        k_encounter_rows<<<(ctx->enc_blocks / 2) * kRowCluster, 32, 0, s>>>(D, rcB, p.dt, p.compat_block,
-                                                                           p.softening2);
+        launch(k_encounter_rows, (ctx->enc_blocks / 4) * kRowCluster, 32 * kRowBodies, D, rcB, p.dt,
+               p.compat_block, p.softening2);
       else
-        k_encounter_cluster<<<ctx->enc_blocks * 2, 32, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
-                                                                p.softening2);
+        launch(k_encounter_cluster, ctx->enc_blocks * 2, 32, D, rcB, p.dt, p.compat_block, p.bs_rows,
+               p.softening2);
       nk++;
     }
     momentum(D.vo);
-    k_jump<<<nb, kThreads, 0, s>>>(D, D.xo, D.vo, rcB, hdt, p.hill_factor);
+    launch(k_jump<true, false>, nb, kThreads, D, D.xo, D.vo, rcB, hdt);
     nk++;
     if ((st = kick(rcB, rcA, 1, 2))) return st;
+    if (lerr != cudaSuccess) return fail(ctx, MERC_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(lerr));
   }
   CK(cudaGetLastError());
   if (kernels) *kernels = nk;
@@ -1409,7 +1434,7 @@ extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodi
   for (int64_t k = 0; k < n_steps; k++) {
     kick(rcA, nullptr, 0);
     momentum(D.v);
-    k_jump<<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt, p->hill_factor);
+    k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt);
     if (big) {
       CK(cudaMemsetAsync(D.ce, 0, n, s));
       k_ce_tiled<<<(unsigned)work.size(), kTile, 0, s>>>(D, d_work, rcB, p->compat_block);
@@ -1422,7 +1447,7 @@ extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodi
     else
       k_encounter_big<<<sms * 4, kEncThreads, 0, s>>>(D, rcB, p->dt, p->compat_block, p->bs_rows, p->softening2);
     momentum(D.vo);
-    k_jump<<<nb, kThreads, 0, s>>>(D, D.xo, D.vo, rcB, hdt, p->hill_factor);
+    k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.xo, D.vo, rcB, hdt);
     kick(rcB, rcA, 1);
     CK(cudaGetLastError());
   }
@@ -1507,6 +1532,13 @@ int merc_diag_far_recomputes(merc_ctx* ctx, int64_t* count) {
   CK(cudaMemcpyAsync(&c, ctx->D.far_recomputes, sizeof c, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   *count = (int64_t)c;
+  return MERC_OK;
+}
+
+int merc_diag_pdl(merc_ctx* ctx, int on) {
+  if (!ctx) return MERC_ERR_CONFIG;
+  ctx->pdl = on != 0;
+  drop_graphs(ctx);
   return MERC_OK;
 }
 

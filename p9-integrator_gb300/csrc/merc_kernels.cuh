@@ -23,6 +23,12 @@ constexpr int kSmallNm = 32;     // systems with more sources use the tiled kern
 constexpr int kEncThreads = 128; // threads per block of an encounter body of a big system
 constexpr int kEncCluster = 4;   // blocks (a thread-block cluster) per encounter body of a big system
 
+// Programmatic dependent launch: wait until the preceding kernel of the
+// stream has completed and its writes are visible (a no-op when the kernel
+// was launched without the attribute), then allow the next kernel to be
+// scheduled.  Called first in every kernel of the step graphs.
+__device__ __forceinline__ void griddep_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 struct Work {
   int sys, t0, c0, c1, chunk;
 };
@@ -233,6 +239,7 @@ __global__ void k_kick(Dev D, const double* __restrict__ rc_in, double* __restri
 // sim.cuh:394-399); `vsrc` is the velocity array to sum.  skip_big leaves the
 // big systems to k_momentum_big.
 __global__ void k_momentum(Dev D, const double* __restrict__ vsrc, int skip_big) {
+  griddep_enter();
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.nsys) return;
   if (skip_big && D.big[s]) return;
@@ -251,13 +258,73 @@ __global__ void k_momentum(Dev D, const double* __restrict__ vsrc, int skip_big)
 
 // Solar jump x = xsrc + dt/2 P (sim.cuh:402-404); copies vsrc -> v when the
 // drift wrote to the output buffers; massive bodies write their new r_crit.
-__global__ void k_jump(Dev D, const double* __restrict__ xsrc, const double* __restrict__ vsrc, double* rc_out,
-                       double hdt, double hill) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j == 0 && D.gate) *D.gate = 0;  // the last merged kick has read it
-  if (j >= D.n) return;
-  const int n = D.n, s = D.sys[j];
-  const double px = D.P[3 * s], py = D.P[3 * s + 1], pz = D.P[3 * s + 2];
+// BIG_P: the momentum P = sum m v of every big system is summed here by each
+// block that holds bodies of the system (thread t adds massive bodies t,
+// t + 128, ..., then a fixed tree, so every block gets the same bits); small
+// systems read D.P (k_momentum).  CLEAR: also clears the encounter flags and
+// list counts for the step's encounter test.
+template <bool BIG_P, bool CLEAR>
+__global__ void __launch_bounds__(kThreads) k_jump(Dev D, const double* __restrict__ xsrc,
+                                                  const double* __restrict__ vsrc, double* rc_out, double hdt) {
+  griddep_enter();
+  __shared__ double red[3][kThreads];
+  __shared__ double Pb[kThreads][3];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j == 0) {
+    if (D.gate) *D.gate = 0;  // the last merged kick has read it
+    if (CLEAR) D.ce_count[0] = D.ce_count[1] = 0;
+  }
+  const int n = D.n;
+  const int j0 = blockIdx.x * blockDim.x, j1 = min(n, j0 + (int)blockDim.x);
+  if (j0 >= n) return;  // whole block
+  const int s0 = D.sys[j0];
+  if (BIG_P) {
+    const int s1 = D.sys[j1 - 1];
+    const double* vv = vsrc ? vsrc : D.v;
+    for (int q = s0; q <= s1; q++) {
+      if (!D.big[q]) continue;  // the same for every thread of the block
+      const int b0 = D.off[q], nm = D.nm[q];
+      double px = 0.0, py = 0.0, pz = 0.0;
+#pragma unroll 4
+      for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+        const double mi = D.m[b0 + i];
+        px = fma(mi, vv[b0 + i], px);
+        py = fma(mi, vv[n + b0 + i], py);
+        pz = fma(mi, vv[2 * n + b0 + i], pz);
+      }
+      red[0][threadIdx.x] = px;
+      red[1][threadIdx.x] = py;
+      red[2][threadIdx.x] = pz;
+      __syncthreads();
+      for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+          red[0][threadIdx.x] += red[0][threadIdx.x + w];
+          red[1][threadIdx.x] += red[1][threadIdx.x + w];
+          red[2][threadIdx.x] += red[2][threadIdx.x + w];
+        }
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) {
+        Pb[q - s0][0] = red[0][0];
+        Pb[q - s0][1] = red[1][0];
+        Pb[q - s0][2] = red[2][0];
+      }
+      __syncthreads();
+    }
+  }
+  if (j >= n) return;
+  const int s = D.sys[j];
+  if (CLEAR) D.ce[j] = 0;
+  double px, py, pz;
+  if (BIG_P && D.big[s]) {
+    px = Pb[s - s0][0];
+    py = Pb[s - s0][1];
+    pz = Pb[s - s0][2];
+  } else {
+    px = D.P[3 * s];
+    py = D.P[3 * s + 1];
+    pz = D.P[3 * s + 2];
+  }
   d3 x = load3(xsrc, n, j);
   x.x = fma(px, hdt, x.x);
   x.y = fma(py, hdt, x.y);
@@ -345,6 +412,7 @@ __global__ void k_encounter_elements(Dev D, const double* __restrict__ rc_in, do
 // Half kick of the bodies of small systems.
 __global__ void k_kick_small(Dev D, const double* __restrict__ rc_in, double* __restrict__ rc_out, double hdt,
                              double soft2, int compat_block, double hill, double eject_r2, int last) {
+  griddep_enter();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= D.n) return;
   const int n = D.n, s = D.sys[j];
@@ -372,6 +440,7 @@ __global__ void __launch_bounds__(kTile) k_kick_tiled(Dev D, const Work* __restr
                                                       const double* __restrict__ rc_in, double* __restrict__ rc_out,
                                                       double hdt, double soft2, int compat_block, double hill,
                                                       double eject_r2, int last) {
+  griddep_enter();
   __shared__ FastSrc tile[kSrcTile];
   const Work W = work[blockIdx.x];
   const int n = D.n, s = W.sys, b0 = D.off[s], b1 = D.off[s + 1], nm = D.nm[s];
@@ -411,6 +480,7 @@ __global__ void __launch_bounds__(kTile) k_kick_tiled_merged(Dev D, const Work* 
                                                              const double* __restrict__ rcB,
                                                              const double* __restrict__ rcA, double hdt,
                                                              double soft2, int compat_block, double eject_r2) {
+  griddep_enter();
   __shared__ FastSrc tile[kSrcTile];
   __shared__ double tileA[kSrcTile][4];
   const Work W = work[blockIdx.x];
@@ -469,6 +539,7 @@ __global__ void __launch_bounds__(kTile) k_kick_tiled_merged(Dev D, const Work* 
 // with more than one chunk.
 __global__ void k_kick_reduce(Dev D, double* __restrict__ rc_out, double hdt, double hill, double eject_r2,
                               int last) {
+  griddep_enter();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= D.n) return;
   const int n = D.n, s = D.sys[j], C = D.nchunk[s];
@@ -545,6 +616,7 @@ template <bool KICK>
 __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ tasks, int ntasks,
                                              const double* __restrict__ rc, double soft2, int set,
                                              const int* __restrict__ gate) {
+  griddep_enter();
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp >= ntasks) return;  // whole warps leave together
   if (KICK && gate && *gate == 0) return;
@@ -678,6 +750,7 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
 __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const int* __restrict__ gate,
                                   double* __restrict__ rc_out, double hdt, double soft2, double hill,
                                   double eject_r2, int last, int massive_only, int check) {
+  griddep_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = t >> 3, sub = t & 7;
   const bool valid = j < D.n;
@@ -757,6 +830,7 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
 // r_crit sets ce[j] (the flags were cleared before the launch).
 __global__ void __launch_bounds__(kTile) k_ce_tiled(Dev D, const Work* __restrict__ work,
                                                     const double* __restrict__ rc_in, int compat_block) {
+  griddep_enter();
   __shared__ FastSrc tile[kSrcTile];
   __shared__ F4 tilef[kSrcTile];
   const Work W = work[blockIdx.x];
@@ -823,6 +897,7 @@ constexpr float kWarmMinX1 = 1e-5f;
 __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, double tol,
                                   int max_iter, const float* __restrict__ mlp, float* __restrict__ log_data,
                                   unsigned long long* __restrict__ log_count, long long log_cap) {
+  griddep_enter();
   __shared__ float blob[kBlob];
   if (mlp) {
     for (int k = threadIdx.x; k < kBlob; k += blockDim.x) blob[k] = mlp[k];
@@ -914,6 +989,7 @@ struct FastVelTotal {
 
 __global__ void k_encounter_small(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, int rows,
                                   double soft2) {
+  griddep_enter();
   const int count = D.ce_count[0];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
     const int j = D.ce_list[k];
@@ -1084,6 +1160,7 @@ struct ClusterVelTotal {
 __global__ void __cluster_dims__(kEncCluster, 1, 1) __launch_bounds__(32)
     k_encounter_cluster(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, int rows,
                         double soft2) {
+  griddep_enter();
   namespace cg = cooperative_groups;
   __shared__ double slot[8];
   cg::cluster_group cl = cg::this_cluster();
@@ -1143,30 +1220,39 @@ struct MidRow {
 };
 
 // Encounter sub-step with three Richardson rows (N = 1, 2, 4) run side by
-// side: a cluster of 7 one-warp blocks per body, ranks 0-3 on row 2, ranks
-// 4-5 on row 1, rank 6 on row 0.  The rows are independent until the final
-// extrapolation, so the critical path is row 2's four evaluations instead of
-// seven in sequence.  Every evaluation is the sum of four quarter sums of the
-// sources (warp_source_sum over quarter q, added in q order), exactly as in
-// k_encounter_cluster; the work is spread over four rounds with one cluster
-// barrier each: in round k row 2's rank r sums quarter r of evaluation k, row
-// 1's ranks sum quarters 2 (k mod 2) + {0, 1} of evaluation k / 2 + 1, and
-// row 0's rank sums quarter k of its single evaluation.  Results are bit for
-// bit those of k_encounter_cluster with rows = 3.
+// side: a cluster of 7 blocks serves kRowBodies bodies, warp w of every block
+// working on body w; ranks 0-3 run row 2, ranks 4-5 row 1, rank 6 row 0.  The
+// rows are independent until the final extrapolation, so the critical path is
+// row 2's four evaluations instead of seven in sequence.  Every evaluation is
+// the sum of four quarter sums of the sources (warp_source_sum over quarter q,
+// added in q order), exactly as in k_encounter_cluster; the work is spread
+// over four rounds with one cluster barrier each: in round k row 2's rank r
+// sums quarter r of evaluation k, row 1's ranks sum quarters 2 (k mod 2) +
+// {0, 1} of evaluation k / 2 + 1, and row 0's rank sums quarter k of its
+// single evaluation.  Measured on a 2002-body disk with 150-190 encounter
+// bodies per step: two bodies per cluster (64-thread blocks) beat one, three
+// and four by 8-12%.  Results are bit for bit those of k_encounter_cluster
+// with rows = 3.
 constexpr int kRowCluster = 7;
-__global__ void __cluster_dims__(kRowCluster, 1, 1) __launch_bounds__(32)
+constexpr int kRowBodies = 2;
+__global__ void __cluster_dims__(kRowCluster, 1, 1) __launch_bounds__(32 * kRowBodies)
     k_encounter_rows(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, double soft2) {
+  griddep_enter();
   namespace cg = cooperative_groups;
-  __shared__ double slot[2][4];  // this block's quarter sum, by round parity
-  __shared__ double res[8];      // final position and velocity of row 0 (rank 6) or row 1 (rank 4)
+  __shared__ double slot[2][kRowBodies][4];  // quarter sum of each warp, by round parity
+  __shared__ double res[kRowBodies][8];      // final position and velocity of row 0 (rank 6) or row 1 (rank 4)
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
+  const int w = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
   const int row = rank < 4 ? 2 : (rank < 6 ? 1 : 0);
   const int cid = blockIdx.x / kRowCluster, ncl = gridDim.x / kRowCluster;
   const int count = D.ce_count[1];
   int parity = 0;
-  for (int k = cid; k < count; k += ncl) {
-    const int j = D.ce_list_big[k];
+  // every warp of the cluster runs the same number of iterations and barriers
+  for (int base = cid * kRowBodies; base < count; base += ncl * kRowBodies) {
+    const int k = base + w;
+    const bool active = k < count;
+    const int j = active ? D.ce_list_big[k] : 0;
     const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
     const int self = self_index(j - b0, compat_block);
     const PV c = {load3(D.x, n, j), load3(D.v, n, j)};
@@ -1176,19 +1262,20 @@ __global__ void __cluster_dims__(kRowCluster, 1, 1) __launch_bounds__(32)
     for (int round = 0; round < 4; round++) {
       const int quarter = row == 2 ? rank : (row == 1 ? 2 * (round & 1) + (rank - 4) : round);
       const int c0 = (int)((int64_t)quarter * nm / 4), c1 = (int)((int64_t)(quarter + 1) * nm / 4);
-      const d3 S = warp_source_sum(D, rc_in, b0, c0, c1, self, m.z1, soft2);
+      d3 S = {0.0, 0.0, 0.0};
+      if (active) S = warp_source_sum(D, rc_in, b0, c0, c1, self, m.z1, soft2);
       const int buf = parity & 1;
-      if (threadIdx.x == 0) {
-        slot[buf][0] = S.x;
-        slot[buf][1] = S.y;
-        slot[buf][2] = S.z;
+      if (lane == 0) {
+        slot[buf][w][0] = S.x;
+        slot[buf][w][1] = S.y;
+        slot[buf][w][2] = S.z;
       }
       cl.sync();
       parity++;
       if (row == 2) {
         d3 acc = {0.0, 0.0, 0.0};
         for (int r = 0; r < 4; r++) {
-          const double* rs = cl.map_shared_rank(&slot[buf][0], r);
+          const double* rs = cl.map_shared_rank(&slot[buf][w][0], r);
           acc.x += rs[0];
           acc.y += rs[1];
           acc.z += rs[2];
@@ -1196,8 +1283,8 @@ __global__ void __cluster_dims__(kRowCluster, 1, 1) __launch_bounds__(32)
         m.finish_eval(acc, soft2);
       } else {
         if (row == 1) {
-          const double* ra = cl.map_shared_rank(&slot[buf][0], 4);
-          const double* rb = cl.map_shared_rank(&slot[buf][0], 5);
+          const double* ra = cl.map_shared_rank(&slot[buf][w][0], 4);
+          const double* rb = cl.map_shared_rank(&slot[buf][w][0], 5);
           q[2 * (round & 1)] = {ra[0], ra[1], ra[2]};
           q[2 * (round & 1) + 1] = {rb[0], rb[1], rb[2]};
         } else {
@@ -1215,18 +1302,18 @@ __global__ void __cluster_dims__(kRowCluster, 1, 1) __launch_bounds__(32)
       }
     }
     const PV mine = m.result();
-    if ((rank == 4 || rank == 6) && threadIdx.x == 0) {
-      res[0] = mine.pos.x;
-      res[1] = mine.pos.y;
-      res[2] = mine.pos.z;
-      res[3] = mine.vel.x;
-      res[4] = mine.vel.y;
-      res[5] = mine.vel.z;
+    if ((rank == 4 || rank == 6) && lane == 0) {
+      res[w][0] = mine.pos.x;
+      res[w][1] = mine.pos.y;
+      res[w][2] = mine.pos.z;
+      res[w][3] = mine.vel.x;
+      res[w][4] = mine.vel.y;
+      res[w][5] = mine.vel.z;
     }
     cl.sync();
-    if (rank == 0 && threadIdx.x == 0) {
-      const double* r0 = cl.map_shared_rank(res, 6);
-      const double* r1 = cl.map_shared_rank(res, 4);
+    if (rank == 0 && lane == 0 && active) {
+      const double* r0 = cl.map_shared_rank(&res[w][0], 6);
+      const double* r1 = cl.map_shared_rank(&res[w][0], 4);
       const PV b00 = {{r0[0], r0[1], r0[2]}, {r0[3], r0[4], r0[5]}};
       const PV b10 = {{r1[0], r1[1], r1[2]}, {r1[3], r1[4], r1[5]}};
       PV b11, b21, b22;

@@ -127,6 +127,7 @@ def lib() -> C.CDLL:
     L.merc_diag_time_kicks.argtypes = [vp, C.c_int]
     L.merc_diag_kick_ms.argtypes = [vp, _f64p, _i32p]
     L.merc_diag_far_recomputes.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.merc_diag_pdl.argtypes = [vp, C.c_int]
     _LIB = L
     return L
 
@@ -291,6 +292,10 @@ class Integrator:
         cnt = C.c_int32()
         self._check(self.L.merc_diag_kick_ms(self.h, C.byref(ms), C.byref(cnt)))
         return ms.value, cnt.value
+
+    def programmatic_launches(self, on: bool = True):
+        """Programmatic dependent launches inside the step graphs (default on)."""
+        self._check(self.L.merc_diag_pdl(self.h, 1 if on else 0))
 
     def far_recomputes(self) -> int:
         """Merged kicks whose far field had to be summed a second time."""

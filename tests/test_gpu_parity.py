@@ -232,3 +232,22 @@ def test_far_field_recompute_with_eccentric_sources(oracle):
     assert np.array_equal(a.state().pos, b.state().pos) and np.array_equal(a.state().vel, b.state().vel)
     a.close()
     b.close()
+
+
+def test_programmatic_launches_do_not_change_results():
+    """The step graphs with and without programmatic dependent launches give
+    the same bits (big system with test particles, and a mixed batch)."""
+    for sysm in (systems.planetesimal_disk(seed=43, n_planetesimals=64, n_test=3000), mixed_batch()):
+        kw = dict(dt=sysm.dt, hill_factor=sysm.hill_factor, drift=merc.DRIFT_UNIVERSAL)
+        out = []
+        for on in (True, False):
+            g = merc.Integrator(merc.default_params(**kw))
+            g.load_systems(sysm)
+            g.programmatic_launches(on)
+            g.step(19)
+            st = g.state()
+            out.append((st.pos, st.vel, st.flags))
+            g.close()
+        assert np.array_equal(out[0][0], out[1][0], equal_nan=True)
+        assert np.array_equal(out[0][1], out[1][1], equal_nan=True)
+        assert np.array_equal(out[0][2], out[1][2])
