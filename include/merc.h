@@ -117,6 +117,34 @@ int merc_load_state(merc_ctx* ctx, int32_t n_systems, const int64_t* body_offset
                     const int32_t* n_massive, const double* mass, const double* pos,
                     const double* vel, const double* a_lag);
 
+/* One system of a batch for merc_load_systems: n_bodies bodies, the first
+ * n_massive of them massive, SoA host arrays of this system only
+ * (elements[k * n_bodies + j] as in merc_load_elements, pos/vel[c * n_bodies + j]).
+ * Give elements for every system of the batch, or pos and vel for every one. */
+typedef struct merc_system_desc {
+  int32_t n_bodies;
+  int32_t n_massive;
+  const double* mass;      /* n_bodies */
+  const double* elements;  /* 6 x n_bodies, or NULL */
+  const double* pos;       /* 3 x n_bodies heliocentric (when elements is NULL) */
+  const double* vel;       /* 3 x n_bodies democratic-heliocentric (when elements is NULL) */
+} merc_system_desc;
+
+/* Load a batch of systems given one descriptor each (copied; the host
+ * arrays stay the caller's).  Equivalent to merc_load_elements or
+ * merc_load_state on the concatenated arrays. */
+int merc_load_systems(merc_ctx* ctx, const merc_system_desc* systems, int32_t n_systems);
+
+/* Checkpoint: write the whole state of the context (parameters, layout,
+ * masses, positions, velocities, a_lag, flags, counters, steps done, the
+ * warm-start network if any) to a binary file, and restore it into a context
+ * (any previous load is replaced).  Stepping a restored context gives the
+ * same bits as stepping the saved one.  A damaged or foreign file is
+ * rejected with MERC_ERR_CONFIG (hashed).  The reference writes text
+ * positions and elements only (src/mercurius.cu:201-249). */
+int merc_save_checkpoint(merc_ctx* ctx, const char* path);
+int merc_load_checkpoint(merc_ctx* ctx, const char* path);
+
 /* Overwrite the state of the loaded systems (same layout and sizes as the
  * load) from host buffers; a NULL pointer keeps that part.  Used to stream new
  * initial conditions through a loaded context without reallocation. */
@@ -146,6 +174,11 @@ int merc_get_stats(merc_ctx* ctx, merc_stats* out);
 /* Energy of each system (massive bodies, Sun included, unsoftened), for
  * conservation checks.  energy: n_systems doubles. */
 int merc_energy(merc_ctx* ctx, double* energy);
+
+/* Angular momentum of each system (massive bodies; sum of m x cross v in the
+ * context's heliocentric positions and democratic-heliocentric velocities,
+ * which is the system's total).  L: 3 doubles per system, L[3 s + c]. */
+int merc_angular_momentum(merc_ctx* ctx, double* L);
 
 /* Number of kernel launches issued by this context since creation. */
 int64_t merc_launch_count(const merc_ctx* ctx);

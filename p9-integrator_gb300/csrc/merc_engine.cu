@@ -984,6 +984,23 @@ int merc_energy(merc_ctx* ctx, double* energy) {
   return MERC_OK;
 }
 
+int merc_angular_momentum(merc_ctx* ctx, double* L) {
+  if (!ctx || !L) return MERC_ERR_CONFIG;
+  if (!ctx->loaded) return fail(ctx, MERC_ERR_STATE, "merc_angular_momentum before a load");
+  CK(cudaSetDevice(ctx->device));
+  double* tmp = nullptr;
+  int st;
+  if ((st = dalloc(ctx, &tmp, 3 * (size_t)ctx->D.nsys))) return st;
+  k_angmom<<<ctx->D.nsys, kThreads, 0, ctx->stream>>>(ctx->D, tmp);
+  ctx->launches++;
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(L, tmp, sizeof(double) * 3 * ctx->D.nsys, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(tmp);
+  ctx->allocs.pop_back();
+  return MERC_OK;
+}
+
 int64_t merc_launch_count(const merc_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 // ---- learned warm start ----
@@ -1031,6 +1048,185 @@ int merc_mlp_append_log(merc_ctx* ctx, const float* samples, int64_t n) {
   unsigned long long c = (unsigned long long)(have + n);
   CK(cudaMemcpy(ctx->d_log_count, &c, sizeof c, cudaMemcpyHostToDevice));
   return MERC_OK;
+}
+
+// ---- checkpoint file ----
+// Little-endian binary: "MERCCKP1", uint32 version (1), uint32 sizeof(merc_params),
+// merc_params, int32 n_systems, int64 n_bodies, int64 steps_done,
+// int64 body_offset[n_systems + 1], int32 n_massive[n_systems], double
+// mass[n], pos[3n], vel[3n], a_lag[n], uint32 flags[n], uint64 counters[4],
+// uint32 has_mlp, float mlp[MERC_MLP_BLOB] (when has_mlp), then the FNV-1a
+// 64-bit hash of every byte before it.
+struct CkptWriter {
+  std::FILE* f;
+  uint64_t h = 1469598103934665603ull;
+  bool ok = true;
+  void put(const void* p, size_t n) {
+    const unsigned char* b = (const unsigned char*)p;
+    for (size_t i = 0; i < n; i++) h = (h ^ b[i]) * 1099511628211ull;
+    ok = ok && std::fwrite(p, 1, n, f) == n;
+  }
+};
+
+struct CkptReader {
+  const std::vector<unsigned char>& buf;
+  size_t pos = 0;
+  bool ok = true;
+  void get(void* p, size_t n) {
+    if (pos + n > buf.size()) {
+      ok = false;
+      return;
+    }
+    std::memcpy(p, buf.data() + pos, n);
+    pos += n;
+  }
+};
+
+int merc_save_checkpoint(merc_ctx* ctx, const char* path) {
+  if (!ctx || !path) return MERC_ERR_CONFIG;
+  if (!ctx->loaded) return fail(ctx, MERC_ERR_STATE, "merc_save_checkpoint before a load");
+  CK(cudaSetDevice(ctx->device));
+  const int32_t nsys = ctx->D.nsys;
+  const int64_t n = ctx->D.n;
+  std::vector<int64_t> off(ctx->h_off.begin(), ctx->h_off.end());
+  std::vector<int32_t> nm(ctx->h_nm.begin(), ctx->h_nm.end());
+  std::vector<double> mass(n), pos(3 * n), vel(3 * n), alag(n);
+  std::vector<uint32_t> flags(n);
+  unsigned long long counters[4];
+  CK(cudaMemcpyAsync(mass.data(), ctx->D.m, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(counters, ctx->D.counters, sizeof counters, cudaMemcpyDeviceToHost, ctx->stream));
+  int st;
+  if ((st = merc_get_state(ctx, pos.data(), vel.data(), flags.data())) ||
+      (st = merc_get_a_lag(ctx, alag.data())))
+    return st;
+  std::vector<float> mlp;
+  if (ctx->mlp_ready) {
+    mlp.resize(kBlob);
+    if ((st = merc_mlp_get_weights(ctx, mlp.data()))) return st;
+  }
+  std::FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(ctx, MERC_ERR_CONFIG, "cannot open %s for writing", path);
+  CkptWriter w{f};
+  const uint32_t version = 1, psize = sizeof(merc_params), has_mlp = ctx->mlp_ready ? 1u : 0u;
+  const int64_t steps = ctx->steps_done;
+  w.put("MERCCKP1", 8);
+  w.put(&version, 4);
+  w.put(&psize, 4);
+  w.put(&ctx->p, sizeof(merc_params));
+  w.put(&nsys, 4);
+  w.put(&n, 8);
+  w.put(&steps, 8);
+  w.put(off.data(), 8 * off.size());
+  w.put(nm.data(), 4 * nm.size());
+  w.put(mass.data(), 8 * mass.size());
+  w.put(pos.data(), 8 * pos.size());
+  w.put(vel.data(), 8 * vel.size());
+  w.put(alag.data(), 8 * alag.size());
+  w.put(flags.data(), 4 * flags.size());
+  w.put(counters, sizeof counters);
+  w.put(&has_mlp, 4);
+  if (has_mlp) w.put(mlp.data(), 4 * mlp.size());
+  const uint64_t hash = w.h;
+  w.put(&hash, 8);
+  const bool ok = w.ok && std::fclose(f) == 0;
+  if (!ok) return fail(ctx, MERC_ERR_CONFIG, "writing %s failed", path);
+  return MERC_OK;
+}
+
+int merc_load_checkpoint(merc_ctx* ctx, const char* path) {
+  if (!ctx || !path) return MERC_ERR_CONFIG;
+  std::FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(ctx, MERC_ERR_CONFIG, "cannot open %s", path);
+  std::vector<unsigned char> buf;
+  unsigned char chunk[1 << 16];
+  size_t got;
+  while ((got = std::fread(chunk, 1, sizeof chunk, f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
+  std::fclose(f);
+  if (buf.size() < 8 + 8) return fail(ctx, MERC_ERR_CONFIG, "%s: not a checkpoint", path);
+  uint64_t h = 1469598103934665603ull;
+  for (size_t i = 0; i + 8 < buf.size(); i++) h = (h ^ buf[i]) * 1099511628211ull;
+  uint64_t stored;
+  std::memcpy(&stored, buf.data() + buf.size() - 8, 8);
+  if (std::memcmp(buf.data(), "MERCCKP1", 8) != 0 || stored != h)
+    return fail(ctx, MERC_ERR_CONFIG, "%s: not a checkpoint or damaged (hash mismatch)", path);
+  CkptReader r{buf};
+  char magic[8];
+  uint32_t version = 0, psize = 0, has_mlp = 0;
+  merc_params p;
+  int32_t nsys = 0;
+  int64_t n = 0, steps = 0;
+  r.get(magic, 8);
+  r.get(&version, 4);
+  r.get(&psize, 4);
+  if (version != 1 || psize != sizeof(merc_params))
+    return fail(ctx, MERC_ERR_CONFIG, "%s: checkpoint version %u not supported", path, version);
+  r.get(&p, sizeof p);
+  r.get(&nsys, 4);
+  r.get(&n, 8);
+  r.get(&steps, 8);
+  if (!r.ok || nsys <= 0 || n <= 0 || n > ((int64_t)1 << 31) || (size_t)n > buf.size() / 8)
+    return fail(ctx, MERC_ERR_CONFIG, "%s: bad sizes", path);
+  std::vector<int64_t> off(nsys + 1);
+  std::vector<int32_t> nm(nsys);
+  std::vector<double> mass(n), pos(3 * n), vel(3 * n), alag(n);
+  std::vector<uint32_t> flags(n);
+  unsigned long long counters[4];
+  r.get(off.data(), 8 * off.size());
+  r.get(nm.data(), 4 * nm.size());
+  r.get(mass.data(), 8 * mass.size());
+  r.get(pos.data(), 8 * pos.size());
+  r.get(vel.data(), 8 * vel.size());
+  r.get(alag.data(), 8 * alag.size());
+  r.get(flags.data(), 4 * flags.size());
+  r.get(counters, sizeof counters);
+  r.get(&has_mlp, 4);
+  std::vector<float> mlp;
+  if (has_mlp) {
+    mlp.resize(kBlob);
+    r.get(mlp.data(), 4 * mlp.size());
+  }
+  if (!r.ok || r.pos + 8 != buf.size()) return fail(ctx, MERC_ERR_CONFIG, "%s: truncated", path);
+  int st;
+  if ((st = merc_set_params(ctx, &p)) ||
+      (st = merc_load_state(ctx, nsys, off.data(), nm.data(), mass.data(), pos.data(), vel.data(), alag.data())))
+    return st;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpyAsync(ctx->D.flags, flags.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->D.counters, counters, sizeof counters, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->steps_done = steps;
+  if (has_mlp && (st = merc_mlp_set_weights(ctx, mlp.data()))) return st;
+  return MERC_OK;
+}
+
+int merc_load_systems(merc_ctx* ctx, const merc_system_desc* systems, int32_t n_systems) {
+  if (!ctx) return MERC_ERR_CONFIG;
+  if (!systems || n_systems <= 0) return fail(ctx, MERC_ERR_CONFIG, "no systems");
+  const bool by_elements = systems[0].elements != nullptr;
+  std::vector<int64_t> off(n_systems + 1, 0);
+  std::vector<int32_t> nm(n_systems);
+  for (int s = 0; s < n_systems; s++) {
+    const merc_system_desc& d = systems[s];
+    if (d.n_bodies <= 0 || !d.mass) return fail(ctx, MERC_ERR_CONFIG, "system %d: no bodies or no masses", s);
+    if ((d.elements != nullptr) != by_elements || (!by_elements && (!d.pos || !d.vel)))
+      return fail(ctx, MERC_ERR_CONFIG, "system %d: give elements for every system, or pos and vel for every one", s);
+    off[s + 1] = off[s] + d.n_bodies;
+    nm[s] = d.n_massive;
+  }
+  const int64_t n = off[n_systems];
+  std::vector<double> mass(n), a(by_elements ? 6 * n : 3 * n), b(by_elements ? 0 : 3 * n);
+  for (int s = 0; s < n_systems; s++) {
+    const merc_system_desc& d = systems[s];
+    const int64_t b0 = off[s], ns = d.n_bodies;
+    std::memcpy(mass.data() + b0, d.mass, sizeof(double) * ns);
+    const int rows = by_elements ? 6 : 3;
+    for (int k = 0; k < rows; k++) {
+      std::memcpy(a.data() + k * n + b0, (by_elements ? d.elements : d.pos) + k * ns, sizeof(double) * ns);
+      if (!by_elements) std::memcpy(b.data() + k * n + b0, d.vel + k * ns, sizeof(double) * ns);
+    }
+  }
+  if (by_elements) return merc_load_elements(ctx, n_systems, off.data(), nm.data(), mass.data(), a.data());
+  return merc_load_state(ctx, n_systems, off.data(), nm.data(), mass.data(), a.data(), b.data(), nullptr);
 }
 
 int merc_mlp_set_weights(merc_ctx* ctx, const float* w) {

@@ -1366,6 +1366,36 @@ __global__ void k_energy(Dev D, double* out) {
   }
 }
 
+// Angular momentum of each system's massive bodies, sum of m x cross v over
+// heliocentric positions and democratic-heliocentric (barycentric) velocities,
+// which is the system's total (the Sun's share is in the barycentric momenta):
+// one block per system, strided partial sums and a fixed tree.
+__global__ void k_angmom(Dev D, double* out) {
+  const int s = blockIdx.x;
+  const int b0 = D.off[s], nm = D.nm[s], n = D.n;
+  __shared__ double red[3][kThreads];
+  d3 L = {0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < nm; i += blockDim.x) {
+    const int g = b0 + i;
+    const d3 x = load3(D.x, n, g), v = load3(D.v, n, g);
+    const double mi = D.m[g];
+    L.x = fma(mi, fma(x.y, v.z, -x.z * v.y), L.x);
+    L.y = fma(mi, fma(x.z, v.x, -x.x * v.z), L.y);
+    L.z = fma(mi, fma(x.x, v.y, -x.y * v.x), L.z);
+  }
+  red[0][threadIdx.x] = L.x;
+  red[1][threadIdx.x] = L.y;
+  red[2][threadIdx.x] = L.z;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int c = 0; c < 3; c++) red[c][threadIdx.x] += red[c][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 3; c++) out[3 * s + c] = red[c][0];
+}
+
 __global__ void k_mm_eval(int fn, int n, const double* x, const double* y, double* out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;

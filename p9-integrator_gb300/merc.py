@@ -106,6 +106,10 @@ def lib() -> C.CDLL:
     L.merc_get_elements.argtypes = [vp, _f64p]
     L.merc_get_stats.argtypes = [vp, C.POINTER(MercStats)]
     L.merc_energy.argtypes = [vp, _f64p]
+    L.merc_angular_momentum.argtypes = [vp, _f64p]
+    L.merc_save_checkpoint.argtypes = [vp, C.c_char_p]
+    L.merc_load_checkpoint.argtypes = [vp, C.c_char_p]
+    L.merc_load_systems.argtypes = [vp, C.POINTER(SystemDesc), C.c_int32]
     L.merc_launch_count.argtypes = [vp]
     L.merc_launch_count.restype = C.c_int64
     L.merc_step_static.argtypes = [C.c_int, C.POINTER(MercParams), C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
@@ -130,6 +134,13 @@ def lib() -> C.CDLL:
     L.merc_diag_pdl.argtypes = [vp, C.c_int]
     _LIB = L
     return L
+
+
+class SystemDesc(C.Structure):
+    """Mirror of ``merc_system_desc`` in include/merc.h."""
+
+    _fields_ = [("n_bodies", C.c_int32), ("n_massive", C.c_int32), ("mass", _f64p), ("elements", _f64p),
+                ("pos", _f64p), ("vel", _f64p)]
 
 
 def default_params(**kw) -> MercParams:
@@ -198,6 +209,35 @@ class Integrator:
         """Load a systems.Systems batch from its elements."""
         self.load_elements(sysm.body_offset, sysm.n_massive, sysm.mass, sysm.elements)
 
+    def load_system_list(self, descs):
+        """Load systems given one dict each: n_massive, mass and either
+        elements (6 x n) or pos and vel (3 x n), through merc_load_systems."""
+        keep = []
+        arr = (SystemDesc * len(descs))()
+        for k, d in enumerate(descs):
+            m = _f64(d["mass"])
+            keep.append(m)
+            arr[k].n_bodies = m.size
+            arr[k].n_massive = int(d["n_massive"])
+            arr[k].mass = _p(m, _f64p)
+            for key in ("elements", "pos", "vel"):
+                if d.get(key) is not None:
+                    a = _f64(np.ascontiguousarray(d[key]).reshape(-1))
+                    keep.append(a)
+                    setattr(arr[k], key, _p(a, _f64p))
+        self._check(self.L.merc_load_systems(self.h, arr, len(descs)))
+        self.n = sum(int(np.asarray(d["mass"]).size) for d in descs)
+        self.nsys = len(descs)
+
+    def save_checkpoint(self, path):
+        self._check(self.L.merc_save_checkpoint(self.h, str(path).encode()))
+
+    def load_checkpoint(self, path):
+        """Restore a checkpoint (parameters, layout and state) into this context."""
+        self._check(self.L.merc_load_checkpoint(self.h, str(path).encode()))
+        st = self.stats()
+        self.n, self.nsys = int(st.n_bodies), int(st.n_systems)
+
     def load_state(self, body_offset, n_massive, mass, pos, vel, a_lag=None):
         off = np.ascontiguousarray(body_offset, np.int64)
         nm = np.ascontiguousarray(n_massive, np.int32)
@@ -247,6 +287,12 @@ class Integrator:
         e = np.empty(self.nsys)
         self._check(self.L.merc_energy(self.h, _p(e, _f64p)))
         return e
+
+    def angular_momentum(self) -> np.ndarray:
+        """Total angular momentum of each system: n_systems x 3."""
+        L = np.empty(3 * self.nsys)
+        self._check(self.L.merc_angular_momentum(self.h, _p(L, _f64p)))
+        return L.reshape(self.nsys, 3)
 
     def launch_count(self) -> int:
         return int(self.L.merc_launch_count(self.h))

@@ -6,7 +6,7 @@
 // integrator through the C ABI of libmerc.so.
 //
 //   mint -c <config.json> -t <T> [-i] [-p] [-o <file>] [-d <device>]
-//        [--dump-precise <file>] [--dry-run]
+//        [--dump-precise <file>] [--checkpoint <file>] [--resume <file>] [--dry-run]
 //
 //  -t T      as in the reference: T > batch_size runs T / batch_size batches,
 //            otherwise T batches, each of batch_size steps (src/mercurius.cu:179)
@@ -14,7 +14,12 @@
 //            CHECKPOINT_FREQUENCY = 20 batches with `#`, `$` and "x y z" lines
 //  -i        print the system and per-batch progress
 //  -p        accepted and ignored, as in the reference (src/mercurius.cu:251)
-//  --dump-precise file   also write the positions with 17 significant digits
+//  --dump-precise file   also write the positions with 17 significant digits,
+//            and the elements file with 17 significant digits
+//  --checkpoint file     write a binary checkpoint (merc_save_checkpoint) after
+//            every CHECKPOINT_FREQUENCY-th batch and after the last one
+//  --resume file         start from a checkpoint written by --checkpoint for
+//            the same configuration, continuing with the batch after it
 //  --dry-run parse the configuration, print it, run nothing
 //
 // Optional config keys (reference defaults in brackets): "dt" [0.8219],
@@ -53,7 +58,7 @@ const char* kElementKeys[6] = {"inclination", "longitude_of_ascending_node", "ar
 struct Args {
   bool info = false, positions = false, dry_run = false;
   long long timesteps = 1;
-  std::string config, output, precise;
+  std::string config, output, precise, checkpoint, resume;
   int device = 0;
 };
 
@@ -73,6 +78,8 @@ Args parse_args(int argc, char** argv) {
     else if (s == "-o") a.output = next();
     else if (s == "-d") a.device = std::atoi(next().c_str());
     else if (s == "--dump-precise") a.precise = next();
+    else if (s == "--checkpoint") a.checkpoint = next();
+    else if (s == "--resume") a.resume = next();
     else if (s == "--dry-run") a.dry_run = true;
   }
   if (a.config.empty()) throw std::runtime_error("no config file: use -c <config.json>");
@@ -206,10 +213,21 @@ int main(int argc, char** argv) {
     merc_ctx* ctx = nullptr;
     int st = merc_create(a.device, &c.p, &ctx);
     if (st != MERC_OK) throw std::runtime_error("merc_create failed: status " + std::to_string(st));
-    check(merc_load_elements(ctx, nsys, off.data(), nmv.data(), mass.data(), el.data()), ctx, "load");
+    long long first_batch = 0;
+    if (a.resume.empty()) {
+      check(merc_load_elements(ctx, nsys, off.data(), nmv.data(), mass.data(), el.data()), ctx, "load");
+    } else {
+      check(merc_load_checkpoint(ctx, a.resume.c_str()), ctx, "resume");
+      merc_stats rs;
+      check(merc_get_stats(ctx, &rs), ctx, "stats");
+      if (rs.n_bodies != ntot || rs.n_systems != nsys || rs.steps_done % c.batch_size != 0)
+        throw std::runtime_error("checkpoint " + a.resume + " does not belong to this configuration");
+      first_batch = rs.steps_done / c.batch_size;
+      if (a.info) std::cout << "Resuming after batch " << first_batch << std::endl;
+    }
     std::string outname = a.output.empty() ? "output_" + std::to_string(a.device) : a.output;
     std::vector<double> pos(3 * ntot), elements(6 * ntot);
-    for (long long batch = 0; batch < iters; batch++) {
+    for (long long batch = first_batch; batch < iters; batch++) {
       check(merc_step(ctx, c.batch_size), ctx, "step");
       if (a.info) std::cout << "Batch " << (batch + 1) << " Simulation Complete.\n";
       const bool checkpoint = batch % kCheckpointFrequency == 0;
@@ -252,6 +270,7 @@ int main(int argc, char** argv) {
         }
         // elements file, src/mercurius.cu:210-248
         std::ofstream fe("elements_" + std::to_string(a.device) + ".txt");
+        if (!a.precise.empty()) fe << std::setprecision(17);
         fe << "Timestep: " << batch * c.batch_size << std::endl;
         for (int s = 0; s < nsys; s++) {
           fe << "Experiment: " << s << std::endl;
@@ -267,6 +286,8 @@ int main(int argc, char** argv) {
       // the next batch restarts from the elements, as every kernel launch of
       // the reference does (src/sim.cuh:744-765 then :654-677)
       check(merc_roundtrip(ctx), ctx, "roundtrip");
+      if (!a.checkpoint.empty() && (checkpoint || batch == iters - 1))
+        check(merc_save_checkpoint(ctx, a.checkpoint.c_str()), ctx, "checkpoint");
     }
     merc_destroy(ctx);
     return 0;

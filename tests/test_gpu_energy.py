@@ -54,3 +54,24 @@ def test_element_drift_energy_matches_oracle():
     g.close()
     ref = GOLD["elements"]["binary64"]["rel_error"]
     assert abs(err - ref) <= 1e-3 * ref, (err, ref)
+
+
+def test_angular_momentum_diagnostic():
+    """merc_angular_momentum equals sum m x cross v of the state, and the
+    universal-drift step conserves it (every stage conserves the total angular
+    momentum when no massive pair is inside a changeover radius: the kick's pair
+    forces are central and equal and opposite, the solar jump shifts all
+    positions by the same vector, the drift is a two-body flow)."""
+    s = systems.outer_solar_system()
+    g = merc.Integrator(merc.default_params(dt=s.dt, hill_factor=s.hill_factor, drift=merc.DRIFT_UNIVERSAL))
+    g.load_systems(s)
+    L0 = g.angular_momentum()[0]
+    st = g.state()
+    nm = int(s.n_massive[0])
+    x, v = st.pos.reshape(3, -1)[:, :nm], st.vel.reshape(3, -1)[:, :nm]
+    Lnp = np.sum(s.mass[:nm] * np.cross(x.T, v.T).T, axis=1)
+    assert np.allclose(L0, Lnp, rtol=1e-14, atol=0)
+    g.step(2000)
+    L1 = g.angular_momentum()[0]
+    assert np.linalg.norm(L1 - L0) <= 1e-12 * np.linalg.norm(L0)
+    g.close()
