@@ -233,6 +233,51 @@ def sweep_section(merc, args, local, dist, world, rank):
             "speedup_vs_one_by_one": batched / one_by_one}
 
 
+def p9_section(merc, args, local, dist, world, rank):
+    """The reference's own workload: the Planet Nine configuration (Planet
+    Nine + 4 giants + 10235 TNOs, p9_config.py) as 32 sweep systems in one
+    context (the reference runs 4 per device), dt 0.8219, changeover at 1 Hill
+    radius; universal drift (persistent kernel) and the reference's element
+    drift.  Replicas: each rank takes a share of the systems."""
+    full = systems.p9_sweep()
+    sysm = systems.shard(full, rank, world)
+    out = {"workload": full.label, "systems": int(full.n_systems), "bodies": int(full.n_total)}
+    steps = max(3, min(args.steps, 20))
+    for name, drift in (("universal", merc.DRIFT_UNIVERSAL), ("elements", merc.DRIFT_ELEMENTS)):
+        g = merc.Integrator(merc.default_params(dt=sysm.dt, hill_factor=sysm.hill_factor, drift=drift), device=local)
+        g.load_systems(sysm)
+        g.step(2)
+        g.step(steps)
+        ms = max_over_ranks(dist, g.stats().last_step_ms)
+        g.close()
+        out[name] = {"body_steps_per_s": sum_over_ranks(dist, float(sysm.n_total * steps)) / (ms / 1e3),
+                     "ms_per_step": ms / steps, "steps": steps}
+    return out
+
+
+def planetesimal_section(merc, args, local, dist, world, rank):
+    """Workload 4: Sun + 4 giants + 8192 planetesimals + 131072 test particles,
+    dt 0.25, one 8-step graph (test-particle half kicks merged across step
+    boundaries).  Reports body-steps/s, pair interactions/s and the HBM rate of
+    the test-particle state stream (96 B per body-step: read and write x, v)."""
+    sysm = systems.planetesimal_disk()
+    g = merc.Integrator(merc.default_params(dt=sysm.dt, hill_factor=sysm.hill_factor, drift=merc.DRIFT_UNIVERSAL),
+                        device=local)
+    g.load_systems(sysm)
+    g.step(1)
+    steps = 8
+    g.step(steps)
+    ms = max_over_ranks(dist, g.stats().last_step_ms)
+    g.close()
+    nm = int(sysm.n_massive[0])
+    nt = sysm.n_total - nm
+    t = ms / 1e3
+    return {"workload": sysm.label, "bodies": int(sysm.n_total), "n_massive": nm, "steps": steps,
+            "body_steps_per_s": sum_over_ranks(dist, float(sysm.n_total * steps)) / t, "ms_per_step": ms / steps,
+            "pairs_per_s": sum_over_ranks(dist, float(2 * (nm * (nm - 1) + nt * nm) * steps)) / t,
+            "test_particle_stream_gbs": sum_over_ranks(dist, 96.0 * nt * steps) / t / 1e9}
+
+
 def warm_start_section(merc, args, local):
     """Learned warm start of the universal drift: log ~1e7 (drift input ->
     converged anomaly) pairs from the embryo disk and the sweep integrated
@@ -356,6 +401,8 @@ def run_ours(args, world, rank, local, dist):
         gc.close()
     g.close()
     sweep = None if args.skip_sweep else sweep_section(merc, args, local, dist, world, rank)
+    p9 = None if args.skip_p9 else p9_section(merc, args, local, dist, world, rank)
+    planet = None if args.skip_planetesimal else planetesimal_section(merc, args, local, dist, world, rank)
     warm = None if args.skip_warm else warm_start_section(merc, args, local)
 
     if rank != 0:
@@ -378,12 +425,15 @@ def run_ours(args, world, rank, local, dist):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 7 * 8 * n,
                 "d2h_bytes_per_step": 6 * 8 * n + 4 * n, "steps": e2e_steps},
+        "pairs_per_s": value * 2 * (nm - 1) if n == nm else None,
         "gpu_launches": int(launches),
         "clocks": ck,
         "close_encounter_body_steps": int(st.ce_body_steps),
         "kepler_mean_iterations": (st.kepler_iterations / st.kepler_solves) if st.kepler_solves else None,
         "compat_elements_path": compat,
         "sweep": sweep,
+        "p9_reference_workload": p9,
+        "planetesimal_disk": planet,
         "learned_warm_start": warm,
     }
     print(json.dumps(line), flush=True)
@@ -400,6 +450,8 @@ def main():
     ap.add_argument("--skip-compat", action="store_true")
     ap.add_argument("--skip-sweep", action="store_true")
     ap.add_argument("--skip-warm", action="store_true")
+    ap.add_argument("--skip-p9", action="store_true")
+    ap.add_argument("--skip-planetesimal", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -84,6 +84,7 @@ struct merc_ctx {
   std::vector<char> kick_ev_used;    // slots recorded by the captured graphs
   bool time_kicks = false;
   bool pdl = true;  // programmatic dependent launches inside the step graphs
+  int smem_optin = 0;  // largest dynamic shared memory per block (opt-in)
   int64_t steps_done = 0;
   int64_t launches = 0;
   int kernels_graph = 0, kernels_graph1 = 0;  // kernels per replay of each graph
@@ -588,16 +589,19 @@ int build_graphs(merc_ctx* ctx) {
 }
 
 // ---- persistent path for batches of small systems ----
-bool use_persistent(const merc_ctx* ctx) {
-  return ctx->p.drift == MERC_DRIFT_UNIVERSAL && !ctx->has_big && ctx->log_cap == 0 && ctx->nmax_sys > 0;
-}
-
 size_t sweep_smem_bytes(const merc_ctx* ctx) {
   const size_t nmax = (size_t)ctx->nmax_sys;
   size_t b = 8 * (6 * nmax + kSweepMaxNm + 8 * kSweepMaxNm + 6 * kSweepMaxNm + 4) + sizeof(F4) * kSweepMaxNm +
              4 * kSweepMaxNm + 4 * (nmax + (nmax & 1));
   if (ctx->p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) b += 4 * (size_t)kBlob;
   return b;
+}
+
+// The persistent kernel holds a whole system in shared memory: batches whose
+// largest system does not fit (about 4500 bodies) run the per-phase graphs.
+bool use_persistent(const merc_ctx* ctx) {
+  return ctx->p.drift == MERC_DRIFT_UNIVERSAL && !ctx->has_big && ctx->log_cap == 0 && ctx->nmax_sys > 0 &&
+         sweep_smem_bytes(ctx) <= (size_t)ctx->smem_optin;
 }
 
 SweepArgs sweep_args(merc_ctx* ctx, int steps, bool trial) {
@@ -735,6 +739,7 @@ int merc_create(int device, const merc_params* p, merc_ctx** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   if (e != cudaSuccess) {
     delete ctx;
     return MERC_ERR_CUDA;

@@ -249,3 +249,27 @@ def from_json(path: str) -> dict:
 def count_massive(mass) -> int:
     """Number of bodies heavier than 1e-12 (src/mercurius.cu:4-15)."""
     return int(np.sum(np.asarray(mass) > MASSIVE_THRESHOLD))
+
+
+def p9_sweep(seed: int = 20261209, n_sweeps: int = 32) -> Systems:
+    """The reference's own workload: the Planet Nine configuration of
+    p9_config.py (Planet Nine + 4 giants + 10235 TNOs) as n_sweeps systems,
+    system k taking sweep k's elements for body 0 with mean anomaly 0 and the
+    body's mass unchanged (as mint does, src/mercurius.cu:133-164); the
+    reference's dt 0.8219 yr and changeover at 1 Hill radius."""
+    import p9_config
+
+    doc = p9_config.p9_config(seed, n_sweeps)
+    bodies = doc["bodies"]
+    n = len(bodies)
+    mass = np.array([b["mass"] for b in bodies])
+    base = np.array([[b[k] for b in bodies] for k in ELEMENT_KEYS])
+    nm = int(np.sum(mass > MASSIVE_THRESHOLD))
+    blocks = []
+    for sw in doc["sweeps"]:
+        el = base.copy()
+        el[:, 0] = [sw[k] for k in ELEMENT_KEYS]
+        el[3, 0] = 0.0
+        blocks.append((mass, el, nm))
+    return _pack(blocks, 0.8219, 1.0, 1000, f"p9 sweep: {n_sweeps} systems x {n} bodies ({nm} massive)",
+                 names=None)

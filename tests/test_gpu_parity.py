@@ -251,3 +251,17 @@ def test_programmatic_launches_do_not_change_results():
         assert np.array_equal(out[0][0], out[1][0], equal_nan=True)
         assert np.array_equal(out[0][1], out[1][1], equal_nan=True)
         assert np.array_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.parametrize("steps", [20])
+def test_large_small_system_parity(oracle, steps):
+    """A batch of small systems whose largest system does not fit in one
+    block's shared memory runs the per-phase graphs instead of the persistent
+    kernel; parity with the oracle (one 6000-body system among small ones)."""
+    a = systems.sweep(n_systems=3, nt_lo=20, nt_hi=40, seed=17)
+    b = systems.outer_solar_system(n_test=6000, seed=18)
+    sysm = systems.concat([a, b])
+    st, gs, alag, (op, ov, oal, of, ost) = run_both(oracle, sysm, steps, drift=merc.DRIFT_UNIVERSAL)
+    assert rel_err(st.pos, op).max() <= 1e-12
+    assert rel_err(st.vel, ov).max() <= 1e-12
+    assert np.array_equal(st.flags, of)
