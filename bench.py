@@ -10,8 +10,9 @@ universal-variable drift.  Synthetic, seeded initial conditions.
 
 ours:       K timed steps on the GPU through libmerc.so.  One bench step is one
             merc_step call that advances the system by --batch integrator steps
-            (default 8, one replay of the step graph; the reference likewise
-            advances BATCH_SIZE steps per kernel launch), with the L2 flushed
+            (default 64: eight replays of the 8-step graph, the kicks at the
+            graph boundaries merged; the reference likewise advances
+            BATCH_SIZE steps per kernel launch), with the L2 flushed
             (512 MB write) between calls; `value` counts integrator body-steps
             over device time (CUDA events), `e2e` is host wall time of the
             public C-ABI call sequence set_state (H2D, pinned) -> step -> get_state
@@ -445,7 +446,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--batch", type=int, default=8, help="integrator steps per bench step (one merc_step call)")
+    ap.add_argument("--batch", type=int, default=64, help="integrator steps per bench step (one merc_step call)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-compat", action="store_true")
     ap.add_argument("--skip-sweep", action="store_true")

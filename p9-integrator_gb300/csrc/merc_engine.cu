@@ -72,8 +72,10 @@ struct merc_ctx {
   std::vector<int> h_off, h_nm;
   bool loaded = false;
   int rc_cur = 0;  // buffer holding r_crit for the next first kick
-  cudaGraphExec_t graph = nullptr;  // kGraphSteps steps
-  cudaGraphExec_t graph1 = nullptr;  // one step
+  // step graphs by kind (GraphKind): executable, kernels per replay
+  cudaGraphExec_t graphs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int graph_kernels[5] = {0, 0, 0, 0, 0};
+  unsigned last_kinds = 0;  // bit k: graphs of kind k replayed by the last merc_step
   int graph_steps = 0;
   int last_graph_steps = 0;  // steps of the graph replayed last
   double* flush_buf = nullptr;
@@ -87,7 +89,7 @@ struct merc_ctx {
   int smem_optin = 0;  // largest dynamic shared memory per block (opt-in)
   int64_t steps_done = 0;
   int64_t launches = 0;
-  int kernels_graph = 0, kernels_graph1 = 0;  // kernels per replay of each graph
+
   // persistent small-system path: size order, work counter, tuned block size
   int* d_order = nullptr;
   int* d_queue = nullptr;
@@ -142,10 +144,11 @@ int check_params(merc_ctx* ctx, const merc_params* p) {
 
 void drop_graphs(merc_ctx* ctx) {
   ctx->last_graph_steps = 0;
-  if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
-  if (ctx->graph1) cudaGraphExecDestroy(ctx->graph1);
-  ctx->graph = nullptr;
-  ctx->graph1 = nullptr;
+  ctx->last_kinds = 0;
+  for (auto& g : ctx->graphs) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
   ctx->graph_steps = 0;
 }
 
@@ -545,13 +548,14 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
 }
 
 // Capture `steps` steps; with timing on, kick events use slots first_slot..
-int capture(merc_ctx* ctx, int steps, bool timed, int first_slot, cudaGraphExec_t* out, int* kernels) {
+int capture(merc_ctx* ctx, int steps, bool timed, int first_slot, bool first_alone, bool last_alone,
+            cudaGraphExec_t* out, int* kernels) {
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   *kernels = 0;
   for (int k = 0; k < steps; k++) {
     int nk = 0;
-    int st = enqueue_step(ctx, timed, first_slot + k, &nk, k == 0, k == steps - 1);
+    int st = enqueue_step(ctx, timed, first_slot / 4 + k, &nk, k == 0 && first_alone, k == steps - 1 && last_alone);
     *kernels += nk;
     if (st) {
       cudaStreamEndCapture(ctx->stream, &g);
@@ -568,22 +572,36 @@ int capture(merc_ctx* ctx, int steps, bool timed, int first_slot, cudaGraphExec_
 
 constexpr int kGraphSteps = 8;
 
-// The step graphs: kGraphSteps steps (kick events recorded when timing is on)
-// and a single step.
+// Kinds of step graphs.  Inside a graph the kick that ends a step and the
+// kick that starts the next share their far field (merged); at a graph's ends
+// a kick is either merged with the neighbouring graph's (when merc_step
+// replays another graph right after it) or done alone.  A call of k >= 2
+// full graphs replays HEAD, MID x (k - 2), TAIL; one full graph replays
+// ALONE; the remaining steps replay ONE.  The merged and the separate forms
+// give the same bits.
+enum GraphKind { G_ALONE = 0, G_ONE = 1, G_HEAD = 2, G_MID = 3, G_TAIL = 4 };
+constexpr int kKindSteps[5] = {kGraphSteps, 1, kGraphSteps, kGraphSteps, kGraphSteps};
+constexpr bool kKindFirstAlone[5] = {true, true, true, false, false};  // start kick done in the graph
+constexpr bool kKindLastAlone[5] = {true, true, false, false, true};   // end kick not merged onward
+constexpr int kKindSlot[5] = {0, 4 * kGraphSteps, 4 * (kGraphSteps + 1), 4 * (2 * kGraphSteps + 1),
+                              4 * (3 * kGraphSteps + 1)};
+constexpr int kKickSlots = 4 * (4 * kGraphSteps + 1);
+
 int build_graphs(merc_ctx* ctx) {
   drop_graphs(ctx);
   if (ctx->time_kicks) {
-    size_t need = 4 * (size_t)(kGraphSteps + 1);
-    while (ctx->kick_ev.size() < need) {
+    while (ctx->kick_ev.size() < (size_t)kKickSlots) {
       cudaEvent_t e;
       CK(cudaEventCreate(&e));
       ctx->kick_ev.push_back(e);
     }
-    ctx->kick_ev_used.assign(need, 0);
+    ctx->kick_ev_used.assign(kKickSlots, 0);
   }
-  int st;
-  if ((st = capture(ctx, kGraphSteps, ctx->time_kicks, 0, &ctx->graph, &ctx->kernels_graph))) return st;
-  if ((st = capture(ctx, 1, ctx->time_kicks, kGraphSteps, &ctx->graph1, &ctx->kernels_graph1))) return st;
+  for (int k = 0; k < 5; k++) {
+    int st = capture(ctx, kKindSteps[k], ctx->time_kicks, kKindSlot[k], kKindFirstAlone[k], kKindLastAlone[k],
+                     &ctx->graphs[k], &ctx->graph_kernels[k]);
+    if (st) return st;
+  }
   ctx->graph_steps = kGraphSteps;
   return MERC_OK;
 }
@@ -868,16 +886,29 @@ int merc_step(merc_ctx* ctx, int64_t n_steps) {
     }
     ctx->last_graph_steps = 0;
   } else {
-    if (!ctx->graph) {
+    if (!ctx->graphs[G_ALONE]) {
       int st = build_graphs(ctx);
       if (st) return st;
     }
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     const int64_t full = n_steps / kGraphSteps, rest = n_steps % kGraphSteps;
-    for (int64_t k = 0; k < full; k++) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
-    for (int64_t k = 0; k < rest; k++) CK(cudaGraphLaunch(ctx->graph1, ctx->stream));
+    unsigned kinds = 0;
+    auto replay = [&](int kind, int64_t times) -> int {
+      for (int64_t k = 0; k < times; k++) CK(cudaGraphLaunch(ctx->graphs[kind], ctx->stream));
+      if (times > 0) kinds |= 1u << kind;
+      ctx->launches += times * ctx->graph_kernels[kind];
+      return MERC_OK;
+    };
+    int st = MERC_OK;
+    if (full == 1) {
+      st = replay(G_ALONE, 1);
+    } else if (full >= 2) {
+      if (!(st = replay(G_HEAD, 1)) && !(st = replay(G_MID, full - 2))) st = replay(G_TAIL, 1);
+    }
+    if (!st) st = replay(G_ONE, rest);
+    if (st) return st;
+    ctx->last_kinds = kinds;
     ctx->last_graph_steps = rest > 0 ? 1 : kGraphSteps;
-    ctx->launches += full * ctx->kernels_graph + rest * ctx->kernels_graph1;
   }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   CK(cudaEventSynchronize(ctx->ev1));
@@ -1758,15 +1789,18 @@ int merc_diag_kick_ms(merc_ctx* ctx, double* avg_ms, int32_t* n_launches) {
   CK(cudaStreamSynchronize(ctx->stream));
   double sum = 0.0;
   int cnt = 0;
-  const int first = ctx->last_graph_steps == 1 ? kGraphSteps : 0;
-  const int steps = ctx->last_graph_steps == 1 ? 1 : kGraphSteps;
-  for (int k = first; k < first + steps; k++) {
-    for (int h = 0; h < 2; h++) {
-      if (!ctx->kick_ev_used[4 * k + 2 * h]) continue;  // a kick merged into the one before
-      float ms = 0.f;
-      CK(cudaEventElapsedTime(&ms, ctx->kick_ev[4 * k + 2 * h], ctx->kick_ev[4 * k + 2 * h + 1]));
-      sum += ms;
-      cnt++;
+  // the last replay of every graph kind that the last call used
+  for (int kind = 0; kind < 5; kind++) {
+    if (!(ctx->last_kinds & (1u << kind))) continue;
+    for (int k = 0; k < kKindSteps[kind]; k++) {
+      for (int h = 0; h < 2; h++) {
+        const int slot = kKindSlot[kind] + 4 * k + 2 * h;
+        if (!ctx->kick_ev_used[slot]) continue;  // a kick merged into the one before
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ctx->kick_ev[slot], ctx->kick_ev[slot + 1]));
+        sum += ms;
+        cnt++;
+      }
     }
   }
   *avg_ms = cnt ? sum / cnt : 0.0;
