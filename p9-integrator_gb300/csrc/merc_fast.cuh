@@ -28,6 +28,12 @@ struct FastSrc {
 
 __device__ __forceinline__ int hi_word(double x) { return __double2hiint(x); }
 
+// The fast-path threshold is stored in the fourth double of an r_crit table
+// entry as integer bits, so that reading it back costs no double -> int
+// conversion (which would occupy the FP64 pipe once per pair).
+__device__ __forceinline__ double thr_pack(int t) { return __longlong_as_double((long long)t); }
+__device__ __forceinline__ int thr_unpack(double d) { return (int)__double_as_longlong(d); }
+
 // high-word threshold: r^2 hi word above this means r > r_crit with margin
 __device__ __forceinline__ int rc2_threshold(double rc) {
   if (!(rc > 0.0) || !(rc < 1e150)) return 0x7fffffff;

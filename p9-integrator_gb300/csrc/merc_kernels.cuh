@@ -116,7 +116,7 @@ __device__ __forceinline__ void write_rc(double* rc, int n, int j, const d3& x, 
   rc[4 * (size_t)j] = r;
   rc[4 * (size_t)j + 1] = 0.1 * r;
   rc[4 * (size_t)j + 2] = 0.9 * r;
-  rc[4 * (size_t)j + 3] = (double)rc2_threshold(r);
+  rc[4 * (size_t)j + 3] = thr_pack(rc2_threshold(r));
   rc_far_thr(rc, n)[j] = far_threshold(r, x, hc);
 }
 
@@ -133,7 +133,7 @@ __device__ __forceinline__ FastSrc load_src(const Dev& D, const double* __restri
   S.rc = __ldg(rc + 4 * (size_t)g);
   S.rc01 = __ldg(rc + 4 * (size_t)g + 1);
   S.rc09 = __ldg(rc + 4 * (size_t)g + 2);
-  S.rc2_hi = (int)__ldg(rc + 4 * (size_t)g + 3);
+  S.rc2_hi = thr_unpack(__ldg(rc + 4 * (size_t)g + 3));
   return S;
 }
 
@@ -503,7 +503,7 @@ __global__ void __launch_bounds__(kTile) k_kick_tiled_merged(Dev D, const Work* 
         const int i = c + k;
         double dx = SB.x - pos.x, dy = SB.y - pos.y, dz = SB.z - pos.z;
         double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
-        if (hi_word(r2) > max(SB.rc2_hi, (int)tileA[k][3]) && i != self && seed_in_range(r2)) {
+        if (hi_word(r2) > max(SB.rc2_hi, thr_unpack(tileA[k][3])) && i != self && seed_in_range(r2)) {
           double w = SB.m * inv_softened_r3(r2, r2 + soft2);
           accB.x = fma(w, dx, accB.x);
           accB.y = fma(w, dy, accB.y);
@@ -517,7 +517,7 @@ __global__ void __launch_bounds__(kTile) k_kick_tiled_merged(Dev D, const Work* 
           SA.rc = tileA[k][0];
           SA.rc01 = tileA[k][1];
           SA.rc09 = tileA[k][2];
-          SA.rc2_hi = (int)tileA[k][3];
+          SA.rc2_hi = thr_unpack(tileA[k][3]);
           pair_fast<false>(pos, self, i, SA, soft2, accA);
         }
       }
@@ -632,7 +632,7 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
   A.y = iv ? D.x[D.n + b0 + i] : 0.0;
   A.z = iv ? D.x[2 * D.n + b0 + i] : 0.0;
   A.m = iv ? D.m[b0 + i] : 0.0;
-  A.thr = iv ? (KICK ? far_thr[b0 + i] : (int)rc[4 * (size_t)(b0 + i) + 3]) : 0x7fffffff;
+  A.thr = iv ? (KICK ? far_thr[b0 + i] : thr_unpack(rc[4 * (size_t)(b0 + i) + 3])) : 0x7fffffff;
   A.idx = i;
   A.f = (!KICK && iv) ? load_f4(D, b0 + i) : F4{0.f, 0.f, 0.f, 0.f};
   A.rcf = (!KICK && iv) ? (float)rc[4 * (size_t)(b0 + i)] : 0.f;
@@ -642,7 +642,7 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
   B.y = jv0 ? D.x[D.n + b0 + j0] : 0.0;
   B.z = jv0 ? D.x[2 * D.n + b0 + j0] : 0.0;
   B.m = jv0 ? D.m[b0 + j0] : 0.0;
-  B.thr = jv0 ? (KICK ? far_thr[b0 + j0] : (int)rc[4 * (size_t)(b0 + j0) + 3]) : 0x7fffffff;
+  B.thr = jv0 ? (KICK ? far_thr[b0 + j0] : thr_unpack(rc[4 * (size_t)(b0 + j0) + 3])) : 0x7fffffff;
   B.idx = jv0 ? j0 : -1;
   B.f = (!KICK && jv0) ? load_f4(D, b0 + j0) : F4{0.f, 0.f, 0.f, 0.f};
   B.rcf = (!KICK && jv0) ? (float)rc[4 * (size_t)(b0 + j0)] : 0.f;
@@ -1066,7 +1066,7 @@ __device__ __forceinline__ bool bs_fast_term(const Dev& D, const double* __restr
   const int g = b0 + i;
   const double dx = __ldg(D.x + g) - pos.x, dy = __ldg(D.x + D.n + g) - pos.y, dz = __ldg(D.x + 2 * D.n + g) - pos.z;
   const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
-  const bool far = hi_word(r2) > (int)__ldg(rc + 4 * (size_t)g + 3) && i != self && seed_in_range(r2);
+  const bool far = hi_word(r2) > thr_unpack(__ldg(rc + 4 * (size_t)g + 3)) && i != self && seed_in_range(r2);
   const double u = inv_softened_r3(r2, r2 + soft2);
   const double w = far ? __ldg(D.m + g) * u : 0.0;
   acc.x = fma(w, dx, acc.x);

@@ -44,7 +44,7 @@ __device__ __forceinline__ void rc_entry(double* t, int i, const d3& x, const d3
   t[4 * i] = r;
   t[4 * i + 1] = 0.1 * r;
   t[4 * i + 2] = 0.9 * r;
-  t[4 * i + 3] = (double)rc2_threshold(r);
+  t[4 * i + 3] = thr_pack(rc2_threshold(r));
 }
 
 __device__ __forceinline__ FastSrc smem_src(const double* X, const double* M, const double* T, int nmax, int i) {
@@ -56,7 +56,7 @@ __device__ __forceinline__ FastSrc smem_src(const double* X, const double* M, co
   S.rc = T[4 * i];
   S.rc01 = T[4 * i + 1];
   S.rc09 = T[4 * i + 2];
-  S.rc2_hi = (int)T[4 * i + 3];
+  S.rc2_hi = thr_unpack(T[4 * i + 3]);
   return S;
 }
 
@@ -273,7 +273,7 @@ __global__ void k_sweep_persistent(SweepArgs A) {
           d3 accB = {0.0, 0.0, 0.0}, accA = {0.0, 0.0, 0.0};  // this step's second, next step's first
           for (int i = 0; i < nm; i++) {
             FastSrc SB = smem_src(X, M, TB, nmax, i);
-            const int thrA = (int)TA[4 * i + 3];
+            const int thrA = thr_unpack(TA[4 * i + 3]);
             double dx = SB.x - pos.x, dy = SB.y - pos.y, dz = SB.z - pos.z;
             double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
             if (!last && hi_word(r2) > max(SB.rc2_hi, thrA) && i != self && seed_in_range(r2)) {
