@@ -23,6 +23,10 @@ __device__ __forceinline__ double stable_div(double x, double y) {  // sim.cuh:8
   return (netz * x) / (y + etz);
 }
 __device__ __forceinline__ double stable_sqrt(double x) { return sqrt(x * (double)(x >= 0.0)); }  // :35-40
+
+// 1 / N for N = 2^k (k < 1023), built from the exponent bits: x * inv_pow2(N)
+// equals x / N bit for bit without a division.
+__device__ __forceinline__ double inv_pow2(int N) { return __hiloint2double((1023 - (__ffs(N) - 1)) << 20, 0); }
 __device__ __forceinline__ double stable_log(double x) {                                         // :57-62
   return mm::log(x * (double)(x > 0.0) + (double)(x <= 0.0));
 }
@@ -273,7 +277,7 @@ struct ExactVelTotal {
 
 template <class VT>
 __device__ __forceinline__ PV mod_midpoint(PV c, const VT& vt, double dt, int N) {
-  double h = dt / (double)N;
+  double h = dt * inv_pow2(N);  // = dt / N exactly (N a power of two)
   d3 z1 = c.pos;
   z1.x = fma(c.vel.x, h, z1.x);
   z1.y = fma(c.vel.y, h, z1.y);

@@ -84,6 +84,26 @@ __device__ __forceinline__ void pair_exact(const d3& pos, int self, int i, const
   acc.z = fma(wa, d.z, acc.z);
 }
 
+// The encounter body's own frozen position as a source of its sub-step
+// (sim.cuh:344-374 with notself = 0): K(y < 0) = 0, so the weight is 1 inside
+// r_crit and 0 outside, with no softening: m (x_self - pos) / r^3 for r <=
+// r_crit.  The same decision r <= r_crit as the reference; the fast formula
+// for 1 / r^3 where r_crit is a positive finite number and r^2 is in the seed
+// range, the reference formula otherwise.
+__device__ __forceinline__ void bs_self_term(const d3& pos, int self, const FastSrc& S, double soft2, d3& acc) {
+  const d3 d = {S.x - pos.x, S.y - pos.y, S.z - pos.z};
+  const double r_sq = mag2(d);
+  if (!(S.rc > 0.0) || !(S.rc < 1e150) || !seed_in_range(r_sq)) {
+    pair_exact<true>(pos, self, self, S, soft2, acc);
+    return;
+  }
+  if (!(stable_sqrt(r_sq) <= S.rc)) return;
+  const double wa = S.m * inv_softened_r3(r_sq, r_sq);
+  acc.x = fma(wa, d.x, acc.x);
+  acc.y = fma(wa, d.y, acc.y);
+  acc.z = fma(wa, d.z, acc.z);
+}
+
 // One pair on the fast path when possible.
 template <bool BS>
 __device__ __forceinline__ void pair_fast(const d3& pos, int self, int i, const FastSrc& S, double soft2, d3& acc) {
@@ -94,6 +114,8 @@ __device__ __forceinline__ void pair_fast(const d3& pos, int self, int i, const 
     acc.x = fma(w, dx, acc.x);
     acc.y = fma(w, dy, acc.y);
     acc.z = fma(w, dz, acc.z);
+  } else if (BS && i == self) {
+    bs_self_term(pos, self, S, soft2, acc);
   } else if (BS || i != self || r2 != 0.0) {
     // (in the plain kick a body's own entry, at distance zero, contributes
     // exactly zero: K = 0 and the guarded division returns 0)

@@ -1097,7 +1097,10 @@ __device__ __forceinline__ d3 warp_source_sum(const Dev& D, const double* __rest
       const int q = __ffsll((long long)slow) - 1;
       slow &= slow - 1ull;
       const int src = base + lane + 32 * q;
-      pair_exact<true>(pos, self, src, load_src(D, rc, b0 + src), soft2, ae);
+      if (src == self)
+        bs_self_term(pos, self, load_src(D, rc, b0 + src), soft2, ae);
+      else
+        pair_exact<true>(pos, self, src, load_src(D, rc, b0 + src), soft2, ae);
     }
   }
   d3 acc = {(a0.x + a1.x) + ae.x, (a0.y + a1.y) + ae.y, (a0.z + a1.z) + ae.z};
@@ -1193,7 +1196,7 @@ struct MidRow {
   int N, done;
   __device__ __forceinline__ void start(const PV& c, double dt, int nsub) {
     N = nsub;
-    h = dt / (double)N;
+    h = dt * inv_pow2(N);  // = dt / N exactly
     h2 = 2.0 * h;
     done = 0;
     z1 = {fma(c.vel.x, h, c.pos.x), fma(c.vel.y, h, c.pos.y), fma(c.vel.z, h, c.pos.z)};
