@@ -423,7 +423,7 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     const bool use_sym = p.compat_block == 0 || p.compat_block >= ctx->max_big_nm;
     // test particles of big systems: adjacent half kicks merged inside a graph
     const bool merge_tp = ctx->has_big && use_sym && ctx->n_work_tp > 0 && !ctx->any_multi;
-    const unsigned nred = (unsigned)((8 * (int64_t)D.n + kThreads - 1) / kThreads);
+    const unsigned nred = (unsigned)((kRedThreads * (int64_t)D.n + kThreads - 1) / kThreads);
     auto tp_kick = [&](const double* rc_in, double* rc_out, int last) {
       launch(k_kick_tiled, ctx->n_work_tp, kTile, D, ctx->d_work_tp, rc_in, rc_out, hdt, p.softening2,
              p.compat_block, p.hill_factor, ej2, last);
@@ -504,7 +504,8 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     if ((st = kick(rcA, nullptr, 0, 0))) return st;
     momentum(D.v);
     // also clears the encounter flags and list counts of this step
-    launch(k_jump<true, true>, nb, kThreads, D, D.x, nullptr, rcB, hdt);
+    const unsigned njb = (unsigned)((D.n + kJumpThreads - 1) / kJumpThreads);
+    launch(k_jump<true, true>, njb, kJumpThreads, D, D.x, nullptr, rcB, hdt);
     nk++;
     if (ctx->has_big) {
       if (use_sym) {
@@ -537,7 +538,7 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       nk++;
     }
     momentum(D.vo);
-    launch(k_jump<true, false>, nb, kThreads, D, D.xo, D.vo, rcB, hdt);
+    launch(k_jump<true, false>, njb, kJumpThreads, D, D.xo, D.vo, rcB, hdt);
     nk++;
     if ((st = kick(rcB, rcA, 1, 2))) return st;
     if (lerr != cudaSuccess) return fail(ctx, MERC_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(lerr));

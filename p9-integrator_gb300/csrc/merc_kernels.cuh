@@ -263,12 +263,16 @@ __global__ void k_momentum(Dev D, const double* __restrict__ vsrc, int skip_big)
 // t + 128, ..., then a fixed tree, so every block gets the same bits); small
 // systems read D.P (k_momentum).  CLEAR: also clears the encounter flags and
 // list counts for the step's encounter test.
+#ifndef MERC_JUMP_THREADS
+#define MERC_JUMP_THREADS 128
+#endif
+constexpr int kJumpThreads = MERC_JUMP_THREADS;  // block of the universal-path jumps
 template <bool BIG_P, bool CLEAR>
-__global__ void __launch_bounds__(kThreads) k_jump(Dev D, const double* __restrict__ xsrc,
-                                                  const double* __restrict__ vsrc, double* rc_out, double hdt) {
+__global__ void __launch_bounds__(kJumpThreads) k_jump(Dev D, const double* __restrict__ xsrc,
+                                                      const double* __restrict__ vsrc, double* rc_out, double hdt) {
   griddep_enter();
-  __shared__ double red[3][kThreads];
-  __shared__ double Pb[kThreads][3];
+  __shared__ double wsum[kJumpThreads / 32][3];
+  __shared__ double Pb[kJumpThreads][3];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j == 0) {
     if (D.gate) *D.gate = 0;  // the last merged kick has read it
@@ -279,8 +283,11 @@ __global__ void __launch_bounds__(kThreads) k_jump(Dev D, const double* __restri
   if (j0 >= n) return;  // whole block
   const int s0 = D.sys[j0];
   if (BIG_P) {
+    // thread t adds massive bodies t, t + B, ...; a fixed butterfly per warp;
+    // thread 0 adds the warp sums in warp order
     const int s1 = D.sys[j1 - 1];
     const double* vv = vsrc ? vsrc : D.v;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int q = s0; q <= s1; q++) {
       if (!D.big[q]) continue;  // the same for every thread of the block
       const int b0 = D.off[q], nm = D.nm[q];
@@ -292,22 +299,27 @@ __global__ void __launch_bounds__(kThreads) k_jump(Dev D, const double* __restri
         py = fma(mi, vv[n + b0 + i], py);
         pz = fma(mi, vv[2 * n + b0 + i], pz);
       }
-      red[0][threadIdx.x] = px;
-      red[1][threadIdx.x] = py;
-      red[2][threadIdx.x] = pz;
-      __syncthreads();
-      for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) {
-          red[0][threadIdx.x] += red[0][threadIdx.x + w];
-          red[1][threadIdx.x] += red[1][threadIdx.x + w];
-          red[2][threadIdx.x] += red[2][threadIdx.x + w];
-        }
-        __syncthreads();
+      for (int o = 16; o > 0; o >>= 1) {
+        px += __shfl_xor_sync(0xffffffffu, px, o);
+        py += __shfl_xor_sync(0xffffffffu, py, o);
+        pz += __shfl_xor_sync(0xffffffffu, pz, o);
       }
+      if (lane == 0) {
+        wsum[warp][0] = px;
+        wsum[warp][1] = py;
+        wsum[warp][2] = pz;
+      }
+      __syncthreads();
       if (threadIdx.x == 0) {
-        Pb[q - s0][0] = red[0][0];
-        Pb[q - s0][1] = red[1][0];
-        Pb[q - s0][2] = red[2][0];
+        double sx = 0.0, sy = 0.0, sz = 0.0;
+        for (int w = 0; w < nw; w++) {
+          sx += wsum[w][0];
+          sy += wsum[w][1];
+          sz += wsum[w][2];
+        }
+        Pb[q - s0][0] = sx;
+        Pb[q - s0][1] = sy;
+        Pb[q - s0][2] = sz;
       }
       __syncthreads();
     }
@@ -737,14 +749,19 @@ __global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ t
   }
 }
 
+#ifndef MERC_RED_THREADS
+#define MERC_RED_THREADS 16
+#endif
+constexpr int kRedThreads = MERC_RED_THREADS;  // threads per body of k_kick_reduce_sym (a power of two <= 32)
+
 // Kick of every body of a big system whose sums are in partials: massive
 // bodies add their far-field block partials (symmetric kernel, set 1 when
 // *gate is set, else set 0) and then their near pairs (reference formula,
 // rc = the kick's r_crit table); test particles add their chunk partials (when
 // there is more than one chunk; a single chunk was applied by the tiled
-// kernel).  Eight threads per body each take every eighth block; their sums
-// are combined by a fixed butterfly, so the result does not depend on
-// scheduling.  check: after writing rc_out, set *D.gate if a massive body's
+// kernel).  kRedThreads threads per body each take every kRedThreads-th
+// block; their sums are combined by a fixed butterfly, so the result does not
+// depend on scheduling.  check: after writing rc_out, set *D.gate if a massive body's
 // far-field threshold in rc_out differs from the one in rc (the far field of
 // the next kick must then be recomputed).
 __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const int* __restrict__ gate,
@@ -752,7 +769,7 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
                                   double eject_r2, int last, int massive_only, int check) {
   griddep_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = t >> 3, sub = t & 7;
+  const int j = t / kRedThreads, sub = t % kRedThreads;
   const bool valid = j < D.n;
   const int n = D.n;
   const int s = valid ? D.sys[j] : 0;
@@ -784,7 +801,7 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   const size_t span = stride / 3;
   d3 acc = {0.0, 0.0, 0.0};
 #pragma unroll 4
-  for (int b = sub; b < count; b += 8) {
+  for (int b = sub; b < count; b += kRedThreads) {
     const double* p = base + (size_t)b * stride;
     acc.x += p[index];
     acc.y += p[span + index];
@@ -794,7 +811,7 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   d3 pos = {0.0, 0.0, 0.0};
   if (work) pos = load3(D.x, n, j);
   if (massive) {
-    for (int b = sub; b < count; b += 8) {
+    for (int b = sub; b < count; b += kRedThreads) {
       uint32_t w = mask[(size_t)b * nm + local];
       while (w) {
         const int q = __ffs(w) - 1;
@@ -804,7 +821,7 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
       }
     }
   }
-  for (int o = 1; o < 8; o <<= 1) {
+  for (int o = 1; o < kRedThreads; o <<= 1) {
     acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
     acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
     acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
