@@ -438,7 +438,8 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     auto far = [&](const double* rc_in, int set, const int* gate, int ev) {
       int st2;
       if (ev >= 0 && (st2 = kick_ev(ev))) return st2;
-      launch(k_sym<true>, ctx->n_sym, 32, D, ctx->d_sym, ctx->n_sym, rc_in, p.softening2, set, gate);
+      launch(k_sym<true>, (ctx->n_sym + kSymWarps - 1) / kSymWarps, 32 * kSymWarps, D, ctx->d_sym, ctx->n_sym, rc_in,
+             p.softening2, set, gate);
       nk++;
       return ev >= 0 ? kick_ev(ev + 1) : MERC_OK;
     };
@@ -509,7 +510,8 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     nk++;
     if (ctx->has_big) {
       if (use_sym) {
-        launch(k_sym<false>, ctx->n_sym, 32, D, ctx->d_sym, ctx->n_sym, rcB, p.softening2, 0, nullptr);
+        launch(k_sym<false>, (ctx->n_sym + kSymWarps - 1) / kSymWarps, 32 * kSymWarps, D, ctx->d_sym, ctx->n_sym,
+               rcB, p.softening2, 0, nullptr);
         nk++;
         if (ctx->n_work_tp) {
           launch(k_ce_tiled, ctx->n_work_tp, kTile, D, ctx->d_work_tp, rcB, p.compat_block);
@@ -521,7 +523,7 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       }
     }
     const float* mlp = (p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) ? ctx->d_mlp : nullptr;
-    launch(k_drift_universal, nb, kThreads, D, rcB, p.dt, p.compat_block, p.kepler_tol, p.kepler_max_iter, mlp,
+    launch(k_drift_universal, (unsigned)((D.n + kDriftThreads - 1) / kDriftThreads), kDriftThreads, D, rcB, p.dt, p.compat_block, p.kepler_tol, p.kepler_max_iter, mlp,
            ctx->d_log, ctx->d_log_count, ctx->log_cap);
     nk++;
     if (ctx->has_small) {

@@ -624,8 +624,12 @@ __device__ __forceinline__ void rotate(RotSrc& r, d3& acc, uint32_t& bits) {
 // KICK: far-field sums and near-pair masks into partial set `set` (thresholds
 // from rc's far-field table); with `gate`, only when *gate is set.
 // !KICK: encounter test flags (rc's fast thresholds).
+#ifndef MERC_SYM_WARPS
+#define MERC_SYM_WARPS 1
+#endif
+constexpr int kSymWarps = MERC_SYM_WARPS;  // block-pair tasks (warps) per block of k_sym
 template <bool KICK>
-__global__ void __launch_bounds__(32) k_sym(Dev D, const SymTask* __restrict__ tasks, int ntasks,
+__global__ void __launch_bounds__(32 * kSymWarps) k_sym(Dev D, const SymTask* __restrict__ tasks, int ntasks,
                                              const double* __restrict__ rc, double soft2, int set,
                                              const int* __restrict__ gate) {
   griddep_enter();
@@ -910,6 +914,10 @@ __global__ void __launch_bounds__(kMomThreads) k_momentum_big(Dev D, const int* 
 // != nullptr: every solve with x1 >= kWarmMinX1 appends its features and
 // training target (5 floats) while the log has room.
 constexpr float kWarmMinX1 = 1e-5f;
+#ifndef MERC_DRIFT_THREADS
+#define MERC_DRIFT_THREADS 128
+#endif
+constexpr int kDriftThreads = MERC_DRIFT_THREADS;  // block of the universal drift (a multiple of 32)
 
 __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, double tol,
                                   int max_iter, const float* __restrict__ mlp, float* __restrict__ log_data,

@@ -265,3 +265,40 @@ def test_large_small_system_parity(oracle, steps):
     assert rel_err(st.pos, op).max() <= 1e-12
     assert rel_err(st.vel, ov).max() <= 1e-12
     assert np.array_equal(st.flags, of)
+
+
+@pytest.mark.parametrize("which,eject_r", [("outer", 500.0), ("sweep", 600.0), ("embryo", 1.2)])
+@pytest.mark.parametrize("drift", [merc.DRIFT_UNIVERSAL, merc.DRIFT_ELEMENTS])
+def test_ejection_and_encounter_flags_match_oracle(oracle, which, eject_r, drift):
+    """MERC_FLAG_EJECTED (set when the heliocentric distance is beyond eject_r
+    after a step, and kept), MERC_FLAG_CE_LAST / CE_EVER and MERC_FLAG_NONFINITE
+    equal the oracle's on the per-body, tiled and persistent paths, and some
+    bodies carry each."""
+    if which == "outer":
+        sysm = systems.outer_solar_system(n_test=200, seed=23)
+    elif which == "sweep":
+        sysm = systems.sweep(n_systems=12, nt_lo=20, nt_hi=80, seed=24)
+    else:
+        sysm = systems.embryo_disk(n_embryos=190, seed=25)
+    steps = 40
+    st, gs, alag, (op, ov, oal, of, ost) = run_both(oracle, sysm, steps, drift=drift, eject_r=eject_r)
+    assert np.array_equal(st.flags, of)
+    ej = (st.flags & merc.FLAG_EJECTED) != 0
+    assert 0 < ej.sum() < sysm.n_total
+    r = np.linalg.norm(st.pos.reshape(3, -1), axis=0)
+    assert np.all(ej[r > eject_r])
+    if which == "embryo":
+        assert np.any(st.flags & merc.FLAG_CE_EVER)
+
+
+def test_nonfinite_flag_matches_oracle(oracle):
+    """A test particle given a NaN eccentricity (no finite state) is flagged
+    MERC_FLAG_NONFINITE on both sides, the others are not, and it does not
+    disturb them (it is massless)."""
+    sysm = systems.outer_solar_system(n_test=30, seed=26)
+    el = sysm.elements.reshape(6, -1)
+    el[4, 10] = np.nan
+    st, gs, alag, (op, ov, oal, of, ost) = run_both(oracle, sysm, 10, drift=merc.DRIFT_UNIVERSAL)
+    assert np.array_equal(st.flags, of)
+    nf = (st.flags & merc.FLAG_NONFINITE) != 0
+    assert nf[10] and nf.sum() == 1
