@@ -358,6 +358,39 @@ __device__ __forceinline__ void stumpff(double z, double* c0, double* c1, double
   *c3 = s3;
 }
 
+// 1 / sqrt(x) and 1 / x for positive doubles inside the FP32 normal range
+// (about 1e-37 .. 1e37): an FP32 seed whose double <-> float moves are
+// integer operations on the high word (exponent rebias 1023 - 127 = 896),
+// refined by one Halley step (rsqrt: seed error 2^-22 -> 2^-66) or two Newton
+// steps (rcp: 2^-23 -> 2^-92); the refinement costs 5 and 4 FP64 operations
+// where sqrt and division cost about 10 each.  Within an ulp or two of the
+// correctly rounded value; outside the range, sqrt and division themselves.
+__device__ __forceinline__ bool seed_range_ok(double x) {
+  const int h = __double2hiint(x);
+  return h > 0x38300000 && h < 0x47C00000;
+}
+__device__ __forceinline__ double rsqrt_fast(double x) {
+  if (!seed_range_ok(x)) return 1.0 / sqrt(x);
+  const float xf = __int_as_float((__double2hiint(x) - 0x38000000) << 3);
+  const int yb = __float_as_int(rsqrtf(xf));
+  const double u = __hiloint2double((yb >> 3) + 0x38000000, yb << 29);
+  const double t = x * u;
+  const double e = fma(-t, u, 1.0);
+  const double c = fma(0.375, e, 0.5);
+  const double ue = u * e;
+  return fma(ue, c, u);
+}
+__device__ __forceinline__ double rcp_fast(double x) {
+  if (!seed_range_ok(x)) return 1.0 / x;
+  const float xf = __int_as_float((__double2hiint(x) - 0x38000000) << 3);
+  const int yb = __float_as_int(__frcp_rn(xf));
+  double y = __hiloint2double((yb >> 3) + 0x38000000, yb << 29);
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
+}
+
 struct UD {
   PV out;
   int iters;
@@ -365,14 +398,16 @@ struct UD {
   double s;  // converged universal anomaly
 };
 
-// Universal Kepler drift with mu = 1 from initial guess s0: Newton on
-// r0 s + eta G2 + zeta G3 = dt; after each update the Newton error estimate
-// |f''/(2 f')| ds^2 of the new s is compared with tol |s| (trusted once
-// |ds| <= 1e-3 |s|); f and g at the final s.
+// Universal Kepler drift with mu = 1 from initial guess s0 (s0 <= 0: the
+// plain guess dt / r0): Newton on r0 s + eta G2 + zeta G3 = dt; after each
+// update the Newton error estimate |f''/(2 f')| ds^2 of the new s is compared
+// with tol |s| (trusted once |ds| <= 1e-3 |s|); f and g at the final s.
 __device__ __forceinline__ UD universal_drift(const d3& x0, const d3& v0, double dt, double s0, double tol,
                                               int max_iter) {
-  double r0 = sqrt(mag2(x0));
-  double ir0 = 1.0 / r0;
+  const double rr = mag2(x0);
+  const double ir0 = rsqrt_fast(rr);
+  const double r0 = rr * ir0;
+  if (!(s0 > 0.0)) s0 = dt * ir0;
   double eta = fma(x0.x, v0.x, fma(x0.y, v0.y, x0.z * v0.z));
   double v2 = mag2(v0);
   double alpha = fma(2.0, ir0, -v2);
@@ -388,7 +423,7 @@ __device__ __forceinline__ UD universal_drift(const d3& x0, const d3& v0, double
     double f = fma(r0, s, fma(eta, G2, fma(zeta, G3, -dt)));
     double fp = fma(eta, G1, fma(zeta, G2, r0));
     double fpp = fma(eta, c0, zeta * G1);
-    double ds = -f / fp;
+    double ds = -f * rcp_fast(fp);
     s = s + ds;
     it++;
     double as = fabs(s);
@@ -401,7 +436,7 @@ __device__ __forceinline__ UD universal_drift(const d3& x0, const d3& v0, double
   stumpff(alpha * s2, &c0, &c1, &c2, &c3);
   double G1 = s * c1, G2 = s2 * c2, G3 = s2 * s * c3;
   double r = fma(eta, G1, fma(zeta, G2, r0));
-  double ir = 1.0 / r;
+  double ir = rcp_fast(r);
   double f = fma(-G2, ir0, 1.0);
   double g = dt - G3;
   double fd = -G1 * ir0 * ir;

@@ -951,9 +951,12 @@ __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, doubl
     }
     if (!is_ce) {
       d3 vel = load3(D.v, n, j);
-      WarmIn w = warm_features(pos, vel, dt);
-      double s0 = w.s0;
-      if (mlp && w.f[0] >= kWarmMinX1) s0 = warm_guess(blob, w);
+      WarmIn w;
+      double s0 = 0.0;  // plain guess
+      if (mlp || log_data) {
+        w = warm_features(pos, vel, dt);
+        if (mlp && w.f[0] >= kWarmMinX1) s0 = warm_guess(blob, w);
+      }
       UD u = universal_drift(pos, vel, dt, s0, tol, max_iter);
       store3(D.xo, n, j, u.out.pos);
       store3(D.vo, n, j, u.out.vel);

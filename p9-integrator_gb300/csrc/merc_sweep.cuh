@@ -189,9 +189,11 @@ __global__ void k_sweep_persistent(SweepArgs A) {
           out = richardson(PV{pos, vel}, vt, A.dt, A.rows);
           my_ce++;
         } else {
-          WarmIn w = warm_features(pos, vel, A.dt);
-          double s0 = w.s0;
-          if (A.mlp && w.f[0] >= kWarmMinX1) s0 = warm_guess(blob, w);
+          double s0 = 0.0;  // plain guess
+          if (A.mlp) {
+            const WarmIn w = warm_features(pos, vel, A.dt);
+            if (w.f[0] >= kWarmMinX1) s0 = warm_guess(blob, w);
+          }
           UD u = universal_drift(pos, vel, A.dt, s0, A.tol, A.max_iter);
           out = u.out;
           my_it += u.iters;
