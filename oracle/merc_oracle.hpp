@@ -335,7 +335,8 @@ PV<R> richardson(const PV<R>& c, int self, const Src<R>* src, int nm, R dt, int 
 
 // ---- universal-variable drift (new formulation; no reference counterpart) ----
 // Stumpff functions c0..c3 of z by quartering z until |z| <= 0.1, a 7-term
-// Taylor series (Horner) for c2 and c3, then the doubling identities
+// Taylor series (Horner) for c2 and c3 (3 terms in binary64 when |z| < 5e-5,
+// where the z^3 terms are below 1e-17 relative), then the doubling identities
 //   c0(4z) = 2 c0^2 - 1, c1(4z) = c0 c1, c2(4z) = c1^2 / 2, c3(4z) = (c2 + c0 c3) / 4
 // (Stumpff; Danby, Fundamentals of Celestial Mechanics, 2nd ed., sec. 6.9).
 // Shared bit for bit with the CUDA kernel: only +, *, fma and one division.
@@ -350,8 +351,15 @@ template <class R> inline void stumpff(R z, R* c0, R* c1, R* c2, R* c3) {
     z = z * R(0.25);
     k++;
   }
-  R s3 = std::fma(z, std::fma(z, std::fma(z, std::fma(z, std::fma(z, std::fma(z, a6, a5), a4), a3), a2), a1), a0);
-  R s2 = std::fma(z, std::fma(z, std::fma(z, std::fma(z, std::fma(z, std::fma(z, b6, b5), b4), b3), b2), b1), b0);
+  R s3, s2;
+  if (sizeof(R) == sizeof(double) && std::fabs(z) < R(5e-5)) {
+    // binary64: the z^3 terms are below 1e-17 relative here
+    s3 = std::fma(z, std::fma(z, a2, a1), a0);
+    s2 = std::fma(z, std::fma(z, b2, b1), b0);
+  } else {
+    s3 = std::fma(z, std::fma(z, std::fma(z, std::fma(z, std::fma(z, std::fma(z, a6, a5), a4), a3), a2), a1), a0);
+    s2 = std::fma(z, std::fma(z, std::fma(z, std::fma(z, std::fma(z, std::fma(z, b6, b5), b4), b3), b2), b1), b0);
+  }
   R s1 = std::fma(-z, s3, R(1));
   R s0 = std::fma(-z, s2, R(1));
   for (; k > 0; k--) {

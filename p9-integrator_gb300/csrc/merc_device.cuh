@@ -327,19 +327,27 @@ __device__ __forceinline__ PV richardson(const PV& c, const VT& vt, double dt, i
 }
 
 // ---- universal-variable drift (new formulation, no reference counterpart) ----
-// Stumpff functions by quartering and doubling, Horner-form Taylor series.
+// Stumpff functions by quartering and doubling, Horner-form Taylor series
+// (three terms when |z| < 5e-5, seven otherwise).
 __device__ __forceinline__ void stumpff(double z, double* c0, double* c1, double* c2, double* c3) {
   int k = 0;
   while (fabs(z) > 0.1 && k < 60) {
     z = z * 0.25;
     k++;
   }
-  double s3 = fma(z, fma(z, fma(z, fma(z, fma(z, fma(z, 1.0 / 1307674368000.0, -1.0 / 6227020800.0),
-                                                  1.0 / 39916800.0), -1.0 / 362880.0), 1.0 / 5040.0),
-                         -1.0 / 120.0), 1.0 / 6.0);
-  double s2 = fma(z, fma(z, fma(z, fma(z, fma(z, fma(z, 1.0 / 87178291200.0, -1.0 / 479001600.0),
-                                                  1.0 / 3628800.0), -1.0 / 40320.0), 1.0 / 720.0),
-                         -1.0 / 24.0), 0.5);
+  double s3, s2;
+  if (fabs(z) < 5e-5) {
+    // the z^3 terms are below 1e-17 relative here
+    s3 = fma(z, fma(z, 1.0 / 5040.0, -1.0 / 120.0), 1.0 / 6.0);
+    s2 = fma(z, fma(z, 1.0 / 720.0, -1.0 / 24.0), 0.5);
+  } else {
+    s3 = fma(z, fma(z, fma(z, fma(z, fma(z, fma(z, 1.0 / 1307674368000.0, -1.0 / 6227020800.0),
+                                           1.0 / 39916800.0), -1.0 / 362880.0), 1.0 / 5040.0),
+                    -1.0 / 120.0), 1.0 / 6.0);
+    s2 = fma(z, fma(z, fma(z, fma(z, fma(z, fma(z, 1.0 / 87178291200.0, -1.0 / 479001600.0),
+                                           1.0 / 3628800.0), -1.0 / 40320.0), 1.0 / 720.0),
+                    -1.0 / 24.0), 0.5);
+  }
   double s1 = fma(-z, s3, 1.0);
   double s0 = fma(-z, s2, 1.0);
   for (; k > 0; k--) {

@@ -207,3 +207,22 @@ def test_product_math_policy_close_to_host_libm(oracle):
     b = oracle.run(p, s.body_offset, s.n_massive, s.mass, pos, vel, alag, steps=100, precision=2)[0]
     rel = np.abs(a - b).reshape(3, -1).max(0) / np.linalg.norm(b.reshape(3, -1), axis=0)
     assert rel.max() < 1e-13
+
+
+def test_stumpff_short_series_for_small_arguments(oracle):
+    """Below |z| = 5e-5 the binary64 Stumpff functions use three Taylor terms;
+    against the series summed in extended precision they stay within 2 ulp."""
+    z = np.concatenate([np.linspace(-5e-5, 5e-5, 201), [4.99e-5, -4.99e-5, 1e-9, -3e-7]])
+    c = oracle.stumpff(z)
+    zl = z.astype(np.longdouble)
+    c2 = np.zeros_like(zl)
+    c3 = np.zeros_like(zl)
+    f2, f3 = np.longdouble(2), np.longdouble(6)
+    term2, term3 = 1 / f2, 1 / f3
+    for k in range(8):
+        c2 += term2
+        c3 += term3
+        term2 = -term2 * zl / ((2 * k + 3) * (2 * k + 4))
+        term3 = -term3 * zl / ((2 * k + 4) * (2 * k + 5))
+    assert np.all(np.abs(c[2] - c2.astype(np.float64)) <= 2 * np.spacing(0.5))
+    assert np.all(np.abs(c[3] - c3.astype(np.float64)) <= 2 * np.spacing(1.0 / 6.0))
