@@ -283,7 +283,10 @@ def warm_start_section(merc, args, local):
     """Learned warm start of the universal drift: log ~1e7 (drift input ->
     converged anomaly) pairs from the embryo disk and the sweep integrated
     together in one context, train the FP32 MLP on the GPU, then integrate each
-    workload from the same initial state with the plain and the learned guess."""
+    workload from the same initial state with the plain guess dt/r0, the
+    learned guess and the third-order series guess (the default).  Reported
+    per guess: Newton iterations per solve, and the iterations the warps
+    executed per solve (a warp runs as many iterations as its slowest lane)."""
     c1, c2 = systems.embryo_disk(), systems.sweep()
     kw = dict(hill_factor=3.0, drift=merc.DRIFT_UNIVERSAL)
     g1 = merc.Integrator(merc.default_params(dt=c1.dt, **kw), device=local)
@@ -306,10 +309,11 @@ def warm_start_section(merc, args, local):
     out = {"logged_pairs": int(n_log), "train_seconds": train_s, "epochs": 12,
            "loss_first_last": [float(loss[0]), float(loss[-1])]}
     steps = max(3, min(args.steps, 20))
+    guesses = (("plain", merc.WARM_PLAIN), ("learned", merc.WARM_MLP), ("series", merc.WARM_SERIES))
     for name, sysm in (("embryo_disk", c1), ("sweep", c2)):
         res = {}
         states = {}
-        for warm in (merc.WARM_PLAIN, merc.WARM_MLP):
+        for key, warm in guesses:
             gi = merc.Integrator(merc.default_params(dt=sysm.dt, hill_factor=3.0, drift=merc.DRIFT_UNIVERSAL,
                                                      warm_start=warm), device=local)
             gi.load_systems(sysm)
@@ -318,14 +322,18 @@ def warm_start_section(merc, args, local):
             gi.step(2)
             gi.step(steps)
             st = gi.stats()
-            key = "learned" if warm == merc.WARM_MLP else "plain"
-            res[key] = {"mean_iterations": st.kepler_iterations / max(st.kepler_solves, 1),
+            solves = max(st.kepler_solves, 1)
+            res[key] = {"mean_iterations": st.kepler_iterations / solves,
+                        "simt_iterations": st.kepler_simt_iterations / solves,
                         "ms_per_step": st.last_step_ms / steps, "nonconverged": int(st.kepler_nonconverged)}
             states[key] = gi.state().pos
             gi.close()
-        a, b = states["plain"].reshape(3, -1), states["learned"].reshape(3, -1)
-        res["max_rel_pos_diff"] = float(np.max(np.abs(a - b).max(0) / np.linalg.norm(a, axis=0)))
+        a = states["plain"].reshape(3, -1)
+        for key in ("learned", "series"):
+            b = states[key].reshape(3, -1)
+            res[key]["max_rel_pos_diff_vs_plain"] = float(np.max(np.abs(a - b).max(0) / np.linalg.norm(a, axis=0)))
         res["iteration_cut"] = res["plain"]["mean_iterations"] / res["learned"]["mean_iterations"]
+        res["simt_iteration_cut"] = res["plain"]["simt_iterations"] / res["learned"]["simt_iterations"]
         out[name] = res
     return out
 

@@ -49,8 +49,9 @@ extern "C" {
 #define MERC_DRIFT_UNIVERSAL 1 /* universal-variable (Stumpff) f and g solve */
 
 /* warm start of the universal-variable solve */
-#define MERC_WARM_PLAIN 0 /* s0 = dt / r0 */
-#define MERC_WARM_MLP 1   /* FP32 MLP guess, then the same FP64 Newton */
+#define MERC_WARM_PLAIN 0  /* s0 = dt / r0 */
+#define MERC_WARM_MLP 1    /* FP32 MLP guess, then the same FP64 Newton */
+#define MERC_WARM_SERIES 2 /* the Kepler equation inverted to third order in dt (default) */
 
 /* per-body flags (uint32) */
 #define MERC_FLAG_CE_LAST 1u   /* close encounter detected in the most recent step */
@@ -65,7 +66,7 @@ typedef struct merc_params {
   double dt;            /* step, yr                          (ref 0.8219) */
   double softening2;    /* epsilon^2 of the pair/Sun forces  (ref 1e-8, constants.cuh:8) */
   double hill_factor;   /* r_crit = hill_factor * Hill radius of the source (ref 1) */
-  double kepler_tol;    /* universal solve: stop when |ds| <= tol*|s| (ref CUTOFF 1e-13) */
+  double kepler_tol;    /* universal solve: stop when the Newton error estimate of s is <= tol*|s| (ref CUTOFF 1e-13) */
   double eject_r;       /* flag bodies beyond this distance; 0 = off */
   int32_t kepler_iters; /* Danby iterations, element drift (ref 8, constants.cuh:4) */
   int32_t bs_rows;      /* Richardson rows of the encounter sub-stepper (ref 3, constants.cuh:10), 1..4 */
@@ -86,6 +87,8 @@ typedef struct merc_stats {
   int64_t n_bodies;          /* total bodies loaded (all systems) */
   int64_t n_systems;
   double last_step_ms;       /* device time of the last merc_step call */
+  int64_t kepler_simt_iterations; /* universal drift: iterations executed, per solve the most that any
+                                     solve of its warp took (the SIMT cost of the Newton loop) */
 } merc_stats;
 
 typedef struct merc_ctx merc_ctx;

@@ -160,7 +160,7 @@ template <class R, class M> static void step_system(Sys<R>& S, const Params& P, 
       if (is_ce) {
         out = richardson<R, M>(cur, self, src.data(), nm, dt, P.bs_rows, soft2);
       } else {
-        R s0 = plain_guess(cur.pos, dt);
+        R s0 = P.warm_start == 2 ? series_guess(cur.pos, cur.vel, dt) : plain_guess(cur.pos, dt);
         UDrift<R> u = universal_drift(cur.pos, cur.vel, dt, s0, R(P.kepler_tol), P.kepler_max_iter);
         out = u.out;
         its[j] = u.iters;

@@ -430,4 +430,22 @@ UDrift<R> universal_drift(const V3<R>& x0, const V3<R>& v0, R dt, R s0, R tol, i
 // Plain initial guess of the universal solve: s0 = dt / r0.
 template <class R> inline R plain_guess(const V3<R>& x0, R dt) { return dt / std::sqrt(mag2(x0)); }
 
+// Series guess: the universal Kepler equation t = r0 s + eta s^2/2 + zeta s^3/6
+// + O(s^4) inverted to third order in t,
+//   s = s0 (1 - (eta / (2 r0)) s0 + ((3 eta^2 - r0 zeta) / (6 r0^2)) s0^2),  s0 = t / r0,
+// (the second-order part is the usual small-dt guess of Wisdom-Holman codes);
+// kept only when it lies within a factor 2 of s0.
+template <class R> inline R series_guess(const V3<R>& x0, const V3<R>& v0, R dt) {
+  R r0 = std::sqrt(mag2(x0));
+  R ir0 = R(1) / r0;
+  R eta = std::fma(x0.x, v0.x, std::fma(x0.y, v0.y, x0.z * v0.z));
+  R v2 = mag2(v0);
+  R zeta = std::fma(-std::fma(R(2), ir0, -v2), r0, R(1));
+  R s0 = dt * ir0;
+  R a1 = R(0.5) * eta * ir0;
+  R a2 = std::fma(R(3) * eta, eta, -r0 * zeta) * (ir0 * ir0) * (R(1) / R(6));
+  R g = s0 * std::fma(s0, std::fma(s0, a2, -a1), R(1));
+  return (g > R(0.5) * s0 && g < R(2) * s0) ? g : s0;
+}
+
 }  // namespace oracle

@@ -43,7 +43,7 @@ class MercParams(C.Structure):
 
 def default_params(**kw) -> MercParams:
     p = MercParams(dt=0.8219, softening2=1e-8, hill_factor=1.0, kepler_tol=1e-13, eject_r=0.0,
-                   kepler_iters=8, bs_rows=3, compat_block=0, drift=0, kepler_max_iter=30, warm_start=0)
+                   kepler_iters=8, bs_rows=3, compat_block=0, drift=0, kepler_max_iter=30, warm_start=2)
     for k, v in kw.items():
         setattr(p, k, v)
     return p

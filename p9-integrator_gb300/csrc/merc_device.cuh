@@ -406,20 +406,48 @@ struct UD {
   double s;  // converged universal anomaly
 };
 
-// Universal Kepler drift with mu = 1 from initial guess s0 (s0 <= 0: the
-// plain guess dt / r0): Newton on r0 s + eta G2 + zeta G3 = dt; after each
-// update the Newton error estimate |f''/(2 f')| ds^2 of the new s is compared
-// with tol |s| (trusted once |ds| <= 1e-3 |s|); f and g at the final s.
+// |x| as an FP32 number, from the high word by integer operations (the top 20
+// bits of the mantissa): 0 below the FP32 normal range, 3e38 above it.
+__device__ __forceinline__ float abs_f32_trunc(double x) {
+  const int h = __double2hiint(x) & 0x7fffffff;
+  if (h < 0x38100000) return 0.0f;
+  if (h > 0x47E00000) return 3e38f;
+  return __int_as_float((h - 0x38000000) << 3);
+}
+
+// Initial guesses of the universal anomaly (the s0 argument of universal_drift)
+constexpr double kGuessPlain = 0.0;    // s0 = dt / r0
+constexpr double kGuessSeries = -1.0;  // third-order series in dt (below)
+
+// Universal Kepler drift with mu = 1 from initial guess s0 (kGuessPlain: dt /
+// r0; kGuessSeries: the universal Kepler equation t = r0 s + eta s^2/2 + zeta
+// s^3/6 + O(s^4) inverted to third order, s = s0 (1 - (eta / 2 r0) s0 + ((3
+// eta^2 - r0 zeta) / 6 r0^2) s0^2) with s0 = dt / r0, kept when within a factor
+// 2 of s0): Newton on r0 s + eta G2 + zeta G3 = dt; after each update the
+// Newton error estimate |f''/(2 f')| ds^2 of the new s is compared with tol |s|
+// (trusted once |ds| <= 1e-3 |s|), in FP32 on truncated copies (the decision
+// needs no more than a factor of 2); f and g at the final s.
 __device__ __forceinline__ UD universal_drift(const d3& x0, const d3& v0, double dt, double s0, double tol,
                                               int max_iter) {
   const double rr = mag2(x0);
   const double ir0 = rsqrt_fast(rr);
   const double r0 = rr * ir0;
-  if (!(s0 > 0.0)) s0 = dt * ir0;
   double eta = fma(x0.x, v0.x, fma(x0.y, v0.y, x0.z * v0.z));
   double v2 = mag2(v0);
   double alpha = fma(2.0, ir0, -v2);
   double zeta = fma(-alpha, r0, 1.0);
+  if (!(s0 > 0.0)) {
+    const double p0 = dt * ir0;
+    double g = p0;
+    if (s0 == kGuessSeries) {
+      const double a1 = 0.5 * eta * ir0;
+      const double a2 = fma(3.0 * eta, eta, -r0 * zeta) * (ir0 * ir0) * (1.0 / 6.0);
+      const double q = p0 * fma(p0, fma(p0, a2, -a1), 1.0);
+      if (q > 0.5 * p0 && q < 2.0 * p0) g = q;
+    }
+    s0 = g;
+  }
+  const float tol2f = abs_f32_trunc(2.0 * tol);
   double s = s0;
   int it = 0;
   bool conv = false;
@@ -434,8 +462,8 @@ __device__ __forceinline__ UD universal_drift(const d3& x0, const d3& v0, double
     double ds = -f * rcp_fast(fp);
     s = s + ds;
     it++;
-    double as = fabs(s);
-    if (fabs(ds) <= 1e-3 * as && fabs(fpp * ds * ds) <= 2.0 * tol * as * fabs(fp)) {
+    const float dsf = abs_f32_trunc(ds), sf = abs_f32_trunc(s);
+    if (dsf <= 1e-3f * sf && abs_f32_trunc(fpp) * dsf * dsf <= tol2f * sf * abs_f32_trunc(fp)) {
       conv = true;
       break;
     }

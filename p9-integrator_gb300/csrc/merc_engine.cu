@@ -87,6 +87,7 @@ struct merc_ctx {
   bool time_kicks = false;
   bool pdl = true;  // programmatic dependent launches inside the step graphs
   int smem_optin = 0;  // largest dynamic shared memory per block (opt-in)
+  int sms = 0;         // multiprocessors of the device
   int64_t steps_done = 0;
   int64_t launches = 0;
 
@@ -137,7 +138,7 @@ int check_params(merc_ctx* ctx, const merc_params* p) {
   if (p->softening2 > 1.0) return fail(ctx, MERC_ERR_CONFIG, "softening2 > 1 AU^2 is not supported");
   if (p->kepler_max_iter < 1 || p->kepler_max_iter > 1000)
     return fail(ctx, MERC_ERR_CONFIG, "kepler_max_iter out of 1..1000");
-  if (p->warm_start != MERC_WARM_PLAIN && p->warm_start != MERC_WARM_MLP)
+  if (p->warm_start != MERC_WARM_PLAIN && p->warm_start != MERC_WARM_MLP && p->warm_start != MERC_WARM_SERIES)
     return fail(ctx, MERC_ERR_CONFIG, "unknown warm_start %d", p->warm_start);
   return MERC_OK;
 }
@@ -286,7 +287,7 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
       (st = dalloc(ctx, &D.vo, 3 * (size_t)n)) || (st = dalloc(ctx, &D.alag, n)) || (st = dalloc(ctx, &D.flags, n)) ||
       (st = dalloc(ctx, &D.ce, n)) || (st = dalloc(ctx, &D.rc[0], rc_table_doubles(n))) ||
       (st = dalloc(ctx, &D.rc[1], rc_table_doubles(n))) || (st = dalloc(ctx, &D.P, 3 * (size_t)n_systems)) ||
-      (st = dalloc(ctx, &D.ce_list, n)) || (st = dalloc(ctx, &D.ce_count, 2)) || (st = dalloc(ctx, &D.counters, 4)))
+      (st = dalloc(ctx, &D.ce_list, n)) || (st = dalloc(ctx, &D.ce_count, 2)) || (st = dalloc(ctx, &D.counters, kNumCounters)))
     return st;
   {
     // systems by size, largest first: the persistent kernel's work order
@@ -297,7 +298,7 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
     });
     ctx->nmax_sys = n_systems ? (int)(off[order[0] + 1] - off[order[0]]) : 0;
     if ((st = dalloc(ctx, &ctx->d_order, n_systems)) || (st = dalloc(ctx, &ctx->d_queue, 1)) ||
-        (st = dalloc(ctx, &ctx->d_tune_counters, 4)) || (st = dalloc(ctx, &ctx->d_tune_flags, n)))
+        (st = dalloc(ctx, &ctx->d_tune_counters, kNumCounters)) || (st = dalloc(ctx, &ctx->d_tune_flags, n)))
       return st;
     CK(cudaMemcpy(ctx->d_order, order.data(), sizeof(int) * n_systems, cudaMemcpyHostToDevice));
     ctx->sweep_threads = 0;
@@ -326,7 +327,7 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
   CK(cudaMemcpyAsync(ctx->d_sym_base, sym_base.data(), sizeof(long long) * n_systems, cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(D.flags, 0, sizeof(uint32_t) * n, s));
   CK(cudaMemsetAsync(D.ce, 0, n, s));
-  CK(cudaMemsetAsync(D.counters, 0, sizeof(unsigned long long) * 4, s));
+  CK(cudaMemsetAsync(D.counters, 0, sizeof(unsigned long long) * kNumCounters, s));
   CK(cudaMemsetAsync(D.rc[0], 0, sizeof(double) * rc_table_doubles(n), s));
   CK(cudaMemsetAsync(D.rc[1], 0, sizeof(double) * rc_table_doubles(n), s));
   CK(cudaStreamSynchronize(s));  // the host vectors above are temporaries
@@ -352,6 +353,10 @@ int dh_convert(merc_ctx* ctx, bool reverse) {
   CK(cudaGetLastError());
   return MERC_OK;
 }
+
+// initial guess of the universal drift for the parameters (the network's
+// fallback outside its box is the plain guess)
+double guess_of(const merc_params& p) { return p.warm_start == MERC_WARM_SERIES ? kGuessSeries : kGuessPlain; }
 
 // Launch on the step stream.  With pdl (programmatic dependent launch) the
 // kernel may be scheduled while its predecessor is still running; every kernel
@@ -523,8 +528,9 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       }
     }
     const float* mlp = (p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) ? ctx->d_mlp : nullptr;
-    launch(k_drift_universal, (unsigned)((D.n + kDriftThreads - 1) / kDriftThreads), kDriftThreads, D, rcB, p.dt, p.compat_block, p.kepler_tol, p.kepler_max_iter, mlp,
-           ctx->d_log, ctx->d_log_count, ctx->log_cap);
+    launch(k_drift_universal, (unsigned)((D.n + kDriftThreads - 1) / kDriftThreads), kDriftThreads, D, rcB, p.dt,
+           p.compat_block, p.kepler_tol, p.kepler_max_iter, guess_of(p), mlp, ctx->d_log, ctx->d_log_count,
+           ctx->log_cap);
     nk++;
     if (ctx->has_small) {
       launch(k_encounter_small, ctx->enc_blocks, 64, D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2);
@@ -610,19 +616,28 @@ int build_graphs(merc_ctx* ctx) {
 }
 
 // ---- persistent path for batches of small systems ----
+constexpr int kSweepChunk = 16;  // steps of massive-body history per chunk
+
+int sweep_nh(const merc_ctx* ctx) {
+  int nh = 1;
+  for (int v : ctx->h_nm) nh = std::max(nh, v);
+  return nh;
+}
+
 size_t sweep_smem_bytes(const merc_ctx* ctx) {
-  const size_t nmax = (size_t)ctx->nmax_sys;
-  size_t b = 8 * (6 * nmax + kSweepMaxNm + 8 * kSweepMaxNm + 6 * kSweepMaxNm + 4) + sizeof(F4) * kSweepMaxNm +
-             4 * kSweepMaxNm + 4 * (nmax + (nmax & 1));
+  size_t b = 8 * hist_step_doubles(sweep_nh(ctx)) * kSweepChunk;
   if (ctx->p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) b += 4 * (size_t)kBlob;
   return b;
 }
 
-// The persistent kernel holds a whole system in shared memory: batches whose
-// largest system does not fit (about 4500 bodies) run the per-phase graphs.
+// The persistent kernel keeps only the massive bodies and their history in
+// shared memory, so any batch of small systems fits.
+// A block integrates one system at a time, so the persistent kernel needs
+// more systems than SMs; a few large systems (the reference's Planet Nine
+// sweep: 4 to 32 systems of 10240 bodies) run faster in the per-phase graphs.
 bool use_persistent(const merc_ctx* ctx) {
   return ctx->p.drift == MERC_DRIFT_UNIVERSAL && !ctx->has_big && ctx->log_cap == 0 && ctx->nmax_sys > 0 &&
-         sweep_smem_bytes(ctx) <= (size_t)ctx->smem_optin;
+         ctx->D.nsys >= ctx->sms && sweep_smem_bytes(ctx) <= (size_t)ctx->smem_optin;
 }
 
 SweepArgs sweep_args(merc_ctx* ctx, int steps, bool trial) {
@@ -639,6 +654,8 @@ SweepArgs sweep_args(merc_ctx* ctx, int steps, bool trial) {
   a.queue = ctx->d_queue;
   a.nsys = ctx->D.nsys;
   a.nmax = ctx->nmax_sys;
+  a.nh = sweep_nh(ctx);
+  a.chunk = kSweepChunk;
   a.steps = steps;
   a.dt = p.dt;
   a.soft2 = p.softening2;
@@ -649,6 +666,7 @@ SweepArgs sweep_args(merc_ctx* ctx, int steps, bool trial) {
   a.rows = p.bs_rows;
   a.max_iter = p.kepler_max_iter;
   a.mlp = (p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) ? ctx->d_mlp : nullptr;
+  a.guess = guess_of(p);
   a.rc_final = trial ? ctx->D.rc[ctx->rc_cur ^ 1] : ctx->D.rc[ctx->rc_cur];
   return a;
 }
@@ -738,7 +756,7 @@ void merc_default_params(merc_params* p) {
   p->compat_block = 0;
   p->drift = MERC_DRIFT_ELEMENTS;
   p->kepler_max_iter = 30;
-  p->warm_start = MERC_WARM_PLAIN;
+  p->warm_start = MERC_WARM_SERIES;
 }
 
 int merc_create(int device, const merc_params* p, merc_ctx** out) {
@@ -761,6 +779,7 @@ int merc_create(int device, const merc_params* p, merc_ctx** out) {
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) {
     delete ctx;
     return MERC_ERR_CUDA;
@@ -995,13 +1014,14 @@ int merc_get_stats(merc_ctx* ctx, merc_stats* out) {
   out->last_step_ms = ctx->last_ms;
   if (ctx->loaded) {
     CK(cudaSetDevice(ctx->device));
-    unsigned long long c[4];
+    unsigned long long c[kNumCounters];
     CK(cudaMemcpyAsync(c, ctx->D.counters, sizeof c, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     out->ce_body_steps = (int64_t)c[0];
     out->kepler_iterations = (int64_t)c[1];
     out->kepler_solves = (int64_t)c[2];
     out->kepler_nonconverged = (int64_t)c[3];
+    out->kepler_simt_iterations = (int64_t)c[4];
   }
   return MERC_OK;
 }
@@ -1090,10 +1110,10 @@ int merc_mlp_append_log(merc_ctx* ctx, const float* samples, int64_t n) {
 }
 
 // ---- checkpoint file ----
-// Little-endian binary: "MERCCKP1", uint32 version (1), uint32 sizeof(merc_params),
+// Little-endian binary: "MERCCKP1", uint32 version (2), uint32 sizeof(merc_params),
 // merc_params, int32 n_systems, int64 n_bodies, int64 steps_done,
 // int64 body_offset[n_systems + 1], int32 n_massive[n_systems], double
-// mass[n], pos[3n], vel[3n], a_lag[n], uint32 flags[n], uint64 counters[4],
+// mass[n], pos[3n], vel[3n], a_lag[n], uint32 flags[n], uint64 counters[5],
 // uint32 has_mlp, float mlp[MERC_MLP_BLOB] (when has_mlp), then the FNV-1a
 // 64-bit hash of every byte before it.
 struct CkptWriter {
@@ -1131,7 +1151,7 @@ int merc_save_checkpoint(merc_ctx* ctx, const char* path) {
   std::vector<int32_t> nm(ctx->h_nm.begin(), ctx->h_nm.end());
   std::vector<double> mass(n), pos(3 * n), vel(3 * n), alag(n);
   std::vector<uint32_t> flags(n);
-  unsigned long long counters[4];
+  unsigned long long counters[kNumCounters];
   CK(cudaMemcpyAsync(mass.data(), ctx->D.m, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(counters, ctx->D.counters, sizeof counters, cudaMemcpyDeviceToHost, ctx->stream));
   int st;
@@ -1146,7 +1166,7 @@ int merc_save_checkpoint(merc_ctx* ctx, const char* path) {
   std::FILE* f = std::fopen(path, "wb");
   if (!f) return fail(ctx, MERC_ERR_CONFIG, "cannot open %s for writing", path);
   CkptWriter w{f};
-  const uint32_t version = 1, psize = sizeof(merc_params), has_mlp = ctx->mlp_ready ? 1u : 0u;
+  const uint32_t version = 2, psize = sizeof(merc_params), has_mlp = ctx->mlp_ready ? 1u : 0u;
   const int64_t steps = ctx->steps_done;
   w.put("MERCCKP1", 8);
   w.put(&version, 4);
@@ -1197,7 +1217,7 @@ int merc_load_checkpoint(merc_ctx* ctx, const char* path) {
   r.get(magic, 8);
   r.get(&version, 4);
   r.get(&psize, 4);
-  if (version != 1 || psize != sizeof(merc_params))
+  if (version != 2 || psize != sizeof(merc_params))
     return fail(ctx, MERC_ERR_CONFIG, "%s: checkpoint version %u not supported", path, version);
   r.get(&p, sizeof p);
   r.get(&nsys, 4);
@@ -1209,7 +1229,7 @@ int merc_load_checkpoint(merc_ctx* ctx, const char* path) {
   std::vector<int32_t> nm(nsys);
   std::vector<double> mass(n), pos(3 * n), vel(3 * n), alag(n);
   std::vector<uint32_t> flags(n);
-  unsigned long long counters[4];
+  unsigned long long counters[kNumCounters];
   r.get(off.data(), 8 * off.size());
   r.get(nm.data(), 4 * nm.size());
   r.get(mass.data(), 8 * mass.size());
@@ -1594,7 +1614,7 @@ extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodi
     D.ce_list = c.take<int>(n);
     D.ce_list_big = c.take<int>(n);
     D.ce_count = c.take<int>(2);
-    D.counters = c.take<unsigned long long>(4);
+    D.counters = c.take<unsigned long long>(kNumCounters);
     *fl = c.take<uint32_t>(n);
   };
   {
@@ -1642,7 +1662,7 @@ extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodi
   if (big) CK(cudaMemcpyAsync(d_work, work.data(), sizeof(Work) * work.size(), cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync((void*)D.sys, 0, sizeof(int) * n, s));
   CK(cudaMemsetAsync(D.ce, 0, n, s));
-  CK(cudaMemsetAsync(D.counters, 0, 4 * sizeof(unsigned long long), s));
+  CK(cudaMemsetAsync(D.counters, 0, kNumCounters * sizeof(unsigned long long), s));
   if (!flags) CK(cudaMemsetAsync(d_flags_scratch, 0, sizeof(uint32_t) * n, s));
   // the kernel sequence of the universal path, on the caller's stream
   const double hdt = 0.5 * p->dt;
@@ -1676,7 +1696,7 @@ extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodi
     }
     CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
     k_drift_universal<<<nb, kThreads, 0, s>>>(D, rcB, p->dt, p->compat_block, p->kepler_tol, p->kepler_max_iter,
-                                              nullptr, nullptr, nullptr, 0);
+                                              guess_of(*p), nullptr, nullptr, nullptr, 0);
     if (!big)
       k_encounter_small<<<sms * 4, 64, 0, s>>>(D, rcB, p->dt, p->compat_block, p->bs_rows, p->softening2);
     else

@@ -17,6 +17,7 @@
 namespace {
 
 constexpr int kThreads = 128;
+constexpr int kNumCounters = 5;  // entries of Dev::counters
 constexpr int kTile = 128;       // targets per work item (one per thread)
 constexpr int kSrcTile = 256;    // sources staged in shared memory per pass
 constexpr int kSmallNm = 32;     // systems with more sources use the tiled kernels
@@ -65,7 +66,8 @@ struct Dev {
   int* ce_list = nullptr;            // encounter bodies of small systems
   int* ce_list_big = nullptr;        // encounter bodies of big systems
   int* ce_count = nullptr;           // [0] small list, [1] big list
-  unsigned long long* counters = nullptr;  // CE body-steps, Kepler iterations, solves, non-converged
+  unsigned long long* counters = nullptr;  // kNumCounters: CE body-steps, Kepler iterations, solves,
+                                           // non-converged, iterations executed per warp (SIMT)
 };
 
 __device__ __forceinline__ SrcView src_view(const Dev& D, const double* rc, int b0) {
@@ -910,7 +912,8 @@ __global__ void __launch_bounds__(kMomThreads) k_momentum_big(Dev D, const int* 
 
 // Encounter test (small systems inline, big systems from ce[]) and universal
 // drift of every body not in encounter; encounter bodies go to the lists.
-// mlp != nullptr: learned warm start of the solve (merc_mlp.cuh).  log_data
+// guess: kGuessPlain or kGuessSeries (universal_drift); mlp != nullptr:
+// learned warm start of the solve (merc_mlp.cuh).  log_data
 // != nullptr: every solve with x1 >= kWarmMinX1 appends its features and
 // training target (5 floats) while the log has room.
 constexpr float kWarmMinX1 = 1e-5f;
@@ -920,8 +923,9 @@ constexpr float kWarmMinX1 = 1e-5f;
 constexpr int kDriftThreads = MERC_DRIFT_THREADS;  // block of the universal drift (a multiple of 32)
 
 __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, double tol,
-                                  int max_iter, const float* __restrict__ mlp, float* __restrict__ log_data,
-                                  unsigned long long* __restrict__ log_count, long long log_cap) {
+                                  int max_iter, double guess, const float* __restrict__ mlp,
+                                  float* __restrict__ log_data, unsigned long long* __restrict__ log_count,
+                                  long long log_cap) {
   griddep_enter();
   __shared__ float blob[kBlob];
   if (mlp) {
@@ -952,7 +956,7 @@ __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, doubl
     if (!is_ce) {
       d3 vel = load3(D.v, n, j);
       WarmIn w;
-      double s0 = 0.0;  // plain guess
+      double s0 = guess;  // kGuessPlain or kGuessSeries unless the network guesses
       if (mlp || log_data) {
         w = warm_features(pos, vel, dt);
         if (mlp && w.f[0] >= kWarmMinX1) s0 = warm_guess(blob, w);
@@ -990,10 +994,13 @@ __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, doubl
   int wits = __reduce_add_sync(0xffffffffu, its);
   int wsol = __reduce_add_sync(0xffffffffu, solved);
   int wnc = __reduce_add_sync(0xffffffffu, nonconv);
+  // iterations the warp executed: the most any of its solves took, for every solving lane
+  int wmax = __reduce_max_sync(0xffffffffu, solved ? its : 0);
   if (lane == 0 && wsol) {
     atomicAdd(&D.counters[1], (unsigned long long)wits);
     atomicAdd(&D.counters[2], (unsigned long long)wsol);
     if (wnc) atomicAdd(&D.counters[3], (unsigned long long)wnc);
+    atomicAdd(&D.counters[4], (unsigned long long)wmax * (unsigned long long)wsol);
   }
 }
 

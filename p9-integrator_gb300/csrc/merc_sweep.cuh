@@ -3,11 +3,19 @@
 // One launch integrates every system of the batch for all the steps of a
 // merc_step call.  Persistent blocks take systems from a device work queue
 // (an atomic counter over the systems sorted by size, largest first, so the
-// last systems handed out are the shortest).  A block keeps its system's
-// whole state in shared memory for all the steps:
-//   X[3][nmax], V[3][nmax]          every body (test particles in place)
-//   massive-body tables (<= 32):    masses, r_crit tables A and B, drift output
-// and runs the Mercurius step with block barriers between the phases.
+// last systems handed out are the shortest).
+//
+// Test particles are massless: nothing in the step depends on them except
+// their own state.  So for a chunk of steps the block's first warp integrates
+// the massive bodies (<= 32, one lane each, state in shared memory) and
+// records what the test particles need from every step (the history: the two
+// momenta of the solar jumps, the massive positions and r_crit tables after
+// each jump, the table of the next step's first kick); then every thread
+// integrates test particles through the whole chunk, each in registers, with
+// no barrier between the phases of a step.  The state of the test particles
+// stays in global memory between chunks.  Per body the operations are those
+// of the per-phase kernels, in the same order, so the results are the same
+// bit for bit.
 //
 // Adjacent half kicks are merged: the second half kick of step k and the first
 // of step k+1 see the same positions, and differ only through the changeover
@@ -17,8 +25,8 @@
 // either radius get each kick's own weight.  Both accumulators are summed in
 // source order exactly as two separate kicks would be, so the result does not
 // depend on how the steps are split into calls (and equals the per-phase
-// kernels bit for bit).  The massive bodies (<= 32 of them) take the two
-// kicks separately, the first of step k+1 after the radii are recomputed.
+// kernels bit for bit).  The massive bodies take the two kicks separately, the
+// first of step k+1 after the radii are recomputed.
 #pragma once
 
 namespace {
@@ -29,9 +37,12 @@ struct SweepArgs {
   Dev D;
   const int* order;  // systems, largest first
   int* queue;        // work counter (zeroed before the launch)
-  int nsys, nmax;    // systems, largest system size (shared-memory capacity)
+  int nsys, nmax;    // systems, largest system size
+  int nh;            // largest massive count of the batch (history stride)
+  int chunk;         // steps per history chunk
   int steps;
   double dt, soft2, hill, tol, eject_r2;
+  double guess;      // kGuessPlain or kGuessSeries
   int compat_block, rows, max_iter;
   const float* mlp;  // warm-start blob or nullptr
   double* rc_final;  // r_crit table for the next call (massive bodies), like D.rc
@@ -39,8 +50,8 @@ struct SweepArgs {
 
 // r_crit table entry of a massive body in shared memory: rc, 0.1 rc, 0.9 rc,
 // threshold (as in write_rc)
-__device__ __forceinline__ void rc_entry(double* t, int i, const d3& x, const d3& v, double m, double hill) {
-  double r = rcrit(x, v, m, hill);
+__device__ __forceinline__ void rc_entry(double* t, int i, const d3& x, const d3& v, double hc) {
+  double r = rcrit_hc(x, v, hc);
   t[4 * i] = r;
   t[4 * i + 1] = 0.1 * r;
   t[4 * i + 2] = 0.9 * r;
@@ -58,6 +69,34 @@ __device__ __forceinline__ FastSrc smem_src(const double* X, const double* M, co
   S.rc09 = T[4 * i + 2];
   S.rc2_hi = thr_unpack(T[4 * i + 3]);
   return S;
+}
+
+// History of one step of the massive bodies (stride nh): momenta of the two
+// jumps; positions, r_crit table and FP32 prefilter copies after the first
+// jump (encounter test and frozen sources of the sub-step); positions and
+// r_crit table after the second jump (second half kick) and the table of the
+// next step's first half kick.
+struct Hist {
+  double *P1, *P2, *X1, *T1, *X2, *T2, *TN;
+  F4* F1;
+  float* R1;
+};
+__host__ __device__ constexpr size_t hist_step_doubles(int nh) {
+  return 6 + 18 * (size_t)nh + 2 * (size_t)nh + ((size_t)nh + 1) / 2;
+}
+__device__ __forceinline__ Hist hist_at(double* base, int nh, int k) {
+  double* p = base + hist_step_doubles(nh) * k;
+  Hist h;
+  h.P1 = p;
+  h.P2 = p + 3;
+  h.X1 = p + 6;
+  h.T1 = h.X1 + 3 * nh;
+  h.X2 = h.T1 + 4 * nh;
+  h.T2 = h.X2 + 3 * nh;
+  h.TN = h.T2 + 4 * nh;
+  h.F1 = (F4*)(h.TN + 4 * nh);
+  h.R1 = (float*)(h.F1 + nh);
+  return h;
 }
 
 struct SmemVelTotal {  // encounter sub-step velocity update, sources in shared memory
@@ -78,208 +117,223 @@ struct SmemVelTotal {  // encounter sub-step velocity update, sources in shared 
 
 __global__ void k_sweep_persistent(SweepArgs A) {
   extern __shared__ double sm[];
-  const int nmax = A.nmax;
-  double* X = sm;                            // 3 nmax
-  double* V = X + 3 * (size_t)nmax;          // 3 nmax
-  double* M = V + 3 * (size_t)nmax;          // 32
-  double* TA = M + kSweepMaxNm;              // 4 x 32
-  double* TB = TA + 4 * kSweepMaxNm;         // 4 x 32
-  double* XO = TB + 4 * kSweepMaxNm;         // 3 x 32 drift output of massive bodies
-  double* VO = XO + 3 * kSweepMaxNm;         // 3 x 32
-  double* P = VO + 3 * kSweepMaxNm;          // 4
-  F4* SF = (F4*)(P + 4);                     // 32 FP32 copies of the massive positions + r_crit (prefilter)
-  float* SRC = (float*)(SF + kSweepMaxNm);   // 32 r_crit (FP32)
-  uint32_t* F = (uint32_t*)(SRC + kSweepMaxNm);  // nmax flags
-  float* blob = (float*)(F + nmax + (nmax & 1));  // kBlob floats when warm start is on
+  const int nh = A.nh, C = A.chunk;
+  double* hist = sm;                                           // C steps of history
+  float* blob = (float*)(sm + hist_step_doubles(nh) * C);      // kBlob floats when warm start is on
+  __shared__ double M[kSweepMaxNm], HC[kSweepMaxNm];           // masses, cbrt(m / 3) * hill
+  __shared__ double XM[3 * kSweepMaxNm], VM[3 * kSweepMaxNm];  // massive state
+  __shared__ double X0[3 * kSweepMaxNm], T0[4 * kSweepMaxNm];  // positions and table of the call's first kick
   __shared__ int sys_slot;
-  __shared__ unsigned long long tally[4];    // encounter body-steps, iterations, solves, non-converged
+  __shared__ unsigned long long tally[kNumCounters];  // as Dev::counters
 
   const Dev& D = A.D;
-  const int T = blockDim.x, tid = threadIdx.x;
+  const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const double hdt = 0.5 * A.dt;
   if (A.mlp) {
     for (int k = tid; k < kBlob; k += T) blob[k] = A.mlp[k];
   }
+  unsigned long long my_ce = 0, my_it = 0, my_sol = 0, my_nc = 0, my_simt = 0;
+  // Kepler drift or encounter sub-step of one body whose sources are (Xs, Ts)
+  auto drift = [&](d3& pos, d3& vel, int self, const Hist& h, int nm, bool& ce) {
+    const F4 pf = f4_of((float)pos.x, (float)pos.y, (float)pos.z);
+    ce = false;
+    for (int i = 0; i < nm; i++)
+      ce = ce || (ce_maybe(pf, h.F1[i], h.R1[i]) && pair_ce(pos, self, i, smem_src(h.X1, M, h.T1, nh, i)));
+    PV out;
+    if (ce) {
+      SmemVelTotal vt{h.X1, M, h.T1, nh, nm, self, A.soft2};
+      out = richardson(PV{pos, vel}, vt, A.dt, A.rows);
+      my_ce++;
+    } else {
+      double s0 = A.guess;  // kGuessPlain or kGuessSeries unless the network guesses
+      if (A.mlp) {
+        const WarmIn w = warm_features(pos, vel, A.dt);
+        if (w.f[0] >= kWarmMinX1) s0 = warm_guess(blob, w);
+      }
+      UD u = universal_drift(pos, vel, A.dt, s0, A.tol, A.max_iter);
+      out = u.out;
+      my_it += u.iters;
+      my_sol++;
+      my_nc += !u.converged;
+      {  // iterations the warp executed: the most among the lanes solving here
+        const unsigned act = __activemask();
+        my_simt += (unsigned long long)__reduce_max_sync(act, u.iters);
+      }
+    }
+    pos = out.pos;
+    vel = out.vel;
+  };
+  auto kick_sum = [&](const d3& pos, int self, const double* Xs, const double* Ts, int nm) {
+    d3 acc = {0.0, 0.0, 0.0};
+    for (int i = 0; i < nm; i++) pair_fast<false>(pos, self, i, smem_src(Xs, M, Ts, nh, i), A.soft2, acc);
+    return acc;
+  };
+  auto step_flags = [&](uint32_t f, const d3& pos, const d3& vel) {
+    if (A.eject_r2 > 0.0 && mag2(pos) > A.eject_r2) f |= MERC_FLAG_EJECTED;
+    bool fin = mm::isfinite_(pos.x) && mm::isfinite_(pos.y) && mm::isfinite_(pos.z) && mm::isfinite_(vel.x) &&
+               mm::isfinite_(vel.y) && mm::isfinite_(vel.z);
+    if (!fin) f |= MERC_FLAG_NONFINITE;
+    return f;
+  };
+
   for (;;) {
     if (tid == 0) sys_slot = atomicAdd(A.queue, 1);
-    if (tid < 4) tally[tid] = 0ull;
+    if (tid < kNumCounters) tally[tid] = 0ull;
     __syncthreads();
     const int slot = sys_slot;
     if (slot >= A.nsys) break;
     const int s = A.order[slot];
     const int b0 = D.off[s], n = D.off[s + 1] - b0, nm = D.nm[s];
-    // load the system
-    for (int j = tid; j < n; j += T) {
-      X[j] = D.x[b0 + j];
-      X[nmax + j] = D.x[D.n + b0 + j];
-      X[2 * nmax + j] = D.x[2 * D.n + b0 + j];
-      V[j] = D.v[b0 + j];
-      V[nmax + j] = D.v[D.n + b0 + j];
-      V[2 * nmax + j] = D.v[2 * D.n + b0 + j];
-      F[j] = D.flags[b0 + j];
-    }
-    if (tid < nm) M[tid] = D.m[b0 + tid];
-    __syncthreads();
-    if (tid < nm) {
-      d3 x = {X[tid], X[nmax + tid], X[2 * nmax + tid]}, v = {V[tid], V[nmax + tid], V[2 * nmax + tid]};
-      rc_entry(TA, tid, x, v, M[tid], A.hill);
-    }
-    __syncthreads();
-    unsigned long long my_ce = 0, my_it = 0, my_sol = 0, my_nc = 0;
-    // sum_i m_i v_i in source order (as k_momentum), one thread
-    auto momentum = [&](const double* VV) {
-      if (tid == 0) {
-        double px = 0.0, py = 0.0, pz = 0.0;
-        for (int i = 0; i < nm; i++) {
-          px = fma(M[i], VV[i], px);
-          py = fma(M[i], VV[nmax + i], py);
-          pz = fma(M[i], VV[2 * nmax + i], pz);
-        }
-        P[0] = px;
-        P[1] = py;
-        P[2] = pz;
+    // massive bodies: lane i of warp 0 owns body i
+    uint32_t fm = 0;
+    if (warp == 0 && lane < nm) {
+      const int g = b0 + lane;
+      M[lane] = D.m[g];
+      HC[lane] = mm::cbrt(M[lane] / 3.0) * A.hill;
+      for (int c = 0; c < 3; c++) {
+        XM[c * kSweepMaxNm + lane] = D.x[c * D.n + g];
+        VM[c * kSweepMaxNm + lane] = D.v[c * D.n + g];
       }
-    };
-    // one half kick of body j with table TT (plain kick: self at distance 0 adds nothing)
-    auto kick_one = [&](int j, const double* TT) {
-      d3 pos = {X[j], X[nmax + j], X[2 * nmax + j]};
-      const int self = self_index(j, A.compat_block);
-      d3 acc = {0.0, 0.0, 0.0};
-      for (int i = 0; i < nm; i++) pair_fast<false>(pos, self, i, smem_src(X, M, TT, nmax, i), A.soft2, acc);
-      return acc;
-    };
-    // first half kick of the call
-    for (int j = tid; j < n; j += T) {
-      d3 a = kick_one(j, TA);
-      V[j] = fma(a.x, hdt, V[j]);
-      V[nmax + j] = fma(a.y, hdt, V[nmax + j]);
-      V[2 * nmax + j] = fma(a.z, hdt, V[2 * nmax + j]);
+      fm = D.flags[g];
     }
-    __syncthreads();
-    for (int step = 0; step < A.steps; step++) {
-      const bool last = step == A.steps - 1;
-      // solar jump, then the radii of the drift
-      momentum(V);
-      __syncthreads();
-      for (int j = tid; j < n; j += T) {
-        X[j] = fma(P[0], hdt, X[j]);
-        X[nmax + j] = fma(P[1], hdt, X[nmax + j]);
-        X[2 * nmax + j] = fma(P[2], hdt, X[2 * nmax + j]);
-      }
-      __syncthreads();
-      if (tid < nm) {
-        d3 x = {X[tid], X[nmax + tid], X[2 * nmax + tid]}, v = {V[tid], V[nmax + tid], V[2 * nmax + tid]};
-        rc_entry(TB, tid, x, v, M[tid], A.hill);
-        SF[tid] = f4_of((float)x.x, (float)x.y, (float)x.z);
-        SRC[tid] = (float)TB[4 * tid];
-      }
-      __syncthreads();
-      // encounter test and drift / encounter sub-step (sources frozen: the
-      // massive bodies write to XO/VO until every body has finished)
-      for (int j = tid; j < n; j += T) {
-        d3 pos = {X[j], X[nmax + j], X[2 * nmax + j]}, vel = {V[j], V[nmax + j], V[2 * nmax + j]};
-        const int self = self_index(j, A.compat_block);
-        const F4 pf = f4_of((float)pos.x, (float)pos.y, (float)pos.z);
-        bool ce = false;
-        for (int i = 0; i < nm; i++)
-          ce = ce || (ce_maybe(pf, SF[i], SRC[i]) && pair_ce(pos, self, i, smem_src(X, M, TB, nmax, i)));
-        PV out;
-        if (ce) {
-          SmemVelTotal vt{X, M, TB, nmax, nm, self, A.soft2};
-          out = richardson(PV{pos, vel}, vt, A.dt, A.rows);
-          my_ce++;
-        } else {
-          double s0 = 0.0;  // plain guess
-          if (A.mlp) {
-            const WarmIn w = warm_features(pos, vel, A.dt);
-            if (w.f[0] >= kWarmMinX1) s0 = warm_guess(blob, w);
+    __syncwarp();
+    for (int c0 = 0; c0 < A.steps; c0 += C) {
+      const int cn = min(C, A.steps - c0);
+      // ---- the massive bodies through the chunk, recording the history ----
+      if (warp == 0) {
+        const bool act = lane < nm;
+        const int self = self_index(lane, A.compat_block);
+        auto xm = [&]() { return d3{XM[lane], XM[kSweepMaxNm + lane], XM[2 * kSweepMaxNm + lane]}; };
+        auto vm = [&]() { return d3{VM[lane], VM[kSweepMaxNm + lane], VM[2 * kSweepMaxNm + lane]}; };
+        auto set_x = [&](const d3& x) {
+          XM[lane] = x.x;
+          XM[kSweepMaxNm + lane] = x.y;
+          XM[2 * kSweepMaxNm + lane] = x.z;
+        };
+        auto set_v = [&](const d3& v) {
+          VM[lane] = v.x;
+          VM[kSweepMaxNm + lane] = v.y;
+          VM[2 * kSweepMaxNm + lane] = v.z;
+        };
+        // sum_i m_i v_i in source order (as k_momentum), one lane
+        auto momentum = [&](double* P) {
+          if (lane == 0) {
+            double px = 0.0, py = 0.0, pz = 0.0;
+            for (int i = 0; i < nm; i++) {
+              px = fma(M[i], VM[i], px);
+              py = fma(M[i], VM[kSweepMaxNm + i], py);
+              pz = fma(M[i], VM[2 * kSweepMaxNm + i], pz);
+            }
+            P[0] = px;
+            P[1] = py;
+            P[2] = pz;
           }
-          UD u = universal_drift(pos, vel, A.dt, s0, A.tol, A.max_iter);
-          out = u.out;
-          my_it += u.iters;
-          my_sol++;
-          my_nc += !u.converged;
-        }
-        uint32_t f = F[j] & ~MERC_FLAG_CE_LAST;
-        if (ce) f |= MERC_FLAG_CE_LAST | MERC_FLAG_CE_EVER;
-        F[j] = f;
-        if (j < nm) {
-          XO[j] = out.pos.x;
-          XO[kSweepMaxNm + j] = out.pos.y;
-          XO[2 * kSweepMaxNm + j] = out.pos.z;
-          VO[j] = out.vel.x;
-          VO[kSweepMaxNm + j] = out.vel.y;
-          VO[2 * kSweepMaxNm + j] = out.vel.z;
-        } else {
-          X[j] = out.pos.x;
-          X[nmax + j] = out.pos.y;
-          X[2 * nmax + j] = out.pos.z;
-          V[j] = out.vel.x;
-          V[nmax + j] = out.vel.y;
-          V[2 * nmax + j] = out.vel.z;
-        }
-      }
-      __syncthreads();
-      if (tid < nm) {
-        X[tid] = XO[tid];
-        X[nmax + tid] = XO[kSweepMaxNm + tid];
-        X[2 * nmax + tid] = XO[2 * kSweepMaxNm + tid];
-        V[tid] = VO[tid];
-        V[nmax + tid] = VO[kSweepMaxNm + tid];
-        V[2 * nmax + tid] = VO[2 * kSweepMaxNm + tid];
-      }
-      __syncthreads();
-      // second solar jump, radii of the second half kick
-      momentum(V);
-      __syncthreads();
-      for (int j = tid; j < n; j += T) {
-        X[j] = fma(P[0], hdt, X[j]);
-        X[nmax + j] = fma(P[1], hdt, X[nmax + j]);
-        X[2 * nmax + j] = fma(P[2], hdt, X[2 * nmax + j]);
-      }
-      __syncthreads();
-      if (tid < nm) {
-        d3 x = {X[tid], X[nmax + tid], X[2 * nmax + tid]}, v = {V[tid], V[nmax + tid], V[2 * nmax + tid]};
-        rc_entry(TB, tid, x, v, M[tid], A.hill);
-      }
-      __syncthreads();
-      // second half kick of the massive bodies, then the radii of the next
-      // step's first half kick from the kicked velocities
-      if (tid < nm) {
-        d3 a = kick_one(tid, TB);
-        V[tid] = fma(a.x, hdt, V[tid]);
-        V[nmax + tid] = fma(a.y, hdt, V[nmax + tid]);
-        V[2 * nmax + tid] = fma(a.z, hdt, V[2 * nmax + tid]);
-      }
-      __syncthreads();
-      if (tid < nm) {
-        d3 x = {X[tid], X[nmax + tid], X[2 * nmax + tid]}, v = {V[tid], V[nmax + tid], V[2 * nmax + tid]};
-        rc_entry(TA, tid, x, v, M[tid], A.hill);
-      }
-      __syncthreads();
-      // test particles: the second half kick of this step and (unless this is
-      // the last step of the call) the first of the next, in one pass;
-      // massive bodies: the first half kick of the next step
-      for (int j = tid; j < n; j += T) {
-        const int self = self_index(j, A.compat_block);
-        d3 pos = {X[j], X[nmax + j], X[2 * nmax + j]};
-        d3 vel = {V[j], V[nmax + j], V[2 * nmax + j]};
-        if (j < nm) {
-          if (!last) {
-            d3 a = kick_one(j, TA);
-            vel.x = fma(a.x, hdt, vel.x);
-            vel.y = fma(a.y, hdt, vel.y);
-            vel.z = fma(a.z, hdt, vel.z);
+          __syncwarp();
+        };
+        auto jump = [&](const double* P) {
+          if (act) {
+            d3 x = xm();
+            x.x = fma(P[0], hdt, x.x);
+            x.y = fma(P[1], hdt, x.y);
+            x.z = fma(P[2], hdt, x.z);
+            set_x(x);
           }
-        } else {
-          d3 accB = {0.0, 0.0, 0.0}, accA = {0.0, 0.0, 0.0};  // this step's second, next step's first
+          __syncwarp();
+        };
+        // positions and table of a kick (stride nh copies of XM)
+        auto record = [&](double* Xs, double* Ts) {
+          if (act) {
+            const d3 x = xm();
+            Xs[lane] = x.x;
+            Xs[nh + lane] = x.y;
+            Xs[2 * nh + lane] = x.z;
+            rc_entry(Ts, lane, x, vm(), HC[lane]);
+          }
+          __syncwarp();
+        };
+        auto kick = [&](const double* Xs, const double* Ts) {
+          if (act) {
+            const d3 x = xm();
+            const d3 a = kick_sum(x, self, Xs, Ts, nm);
+            d3 v = vm();
+            v.x = fma(a.x, hdt, v.x);
+            v.y = fma(a.y, hdt, v.y);
+            v.z = fma(a.z, hdt, v.z);
+            set_v(v);
+          }
+          __syncwarp();
+        };
+        if (c0 == 0) {  // the call's first half kick
+          record(X0, T0);
+          kick(X0, T0);
+        }
+        for (int k = 0; k < cn; k++) {
+          const bool last = c0 + k == A.steps - 1;
+          Hist h = hist_at(hist, nh, k);
+          momentum(h.P1);
+          jump(h.P1);
+          record(h.X1, h.T1);
+          if (act) {
+            h.F1[lane] = f4_of((float)h.X1[lane], (float)h.X1[nh + lane], (float)h.X1[2 * nh + lane]);
+            h.R1[lane] = (float)h.T1[4 * lane];
+          }
+          __syncwarp();
+          if (act) {
+            d3 pos = xm(), vel = vm();
+            bool ce;
+            drift(pos, vel, self, h, nm, ce);
+            fm &= ~MERC_FLAG_CE_LAST;
+            if (ce) fm |= MERC_FLAG_CE_LAST | MERC_FLAG_CE_EVER;
+            set_x(pos);
+            set_v(vel);
+          }
+          __syncwarp();
+          momentum(h.P2);
+          jump(h.P2);
+          record(h.X2, h.T2);
+          kick(h.X2, h.T2);
+          if (act) rc_entry(h.TN, lane, xm(), vm(), HC[lane]);
+          __syncwarp();
+          if (!last) kick(h.X2, h.TN);
+          if (act) fm = step_flags(fm, xm(), vm());
+        }
+      }
+      __syncthreads();  // the history of the chunk is complete
+      // ---- test particles through the chunk, each in registers ----
+      for (int j = nm + tid; j < n; j += T) {
+        const int g = b0 + j, self = self_index(j, A.compat_block);
+        d3 pos = {D.x[g], D.x[D.n + g], D.x[2 * D.n + g]};
+        d3 vel = {D.v[g], D.v[D.n + g], D.v[2 * D.n + g]};
+        uint32_t f = D.flags[g];
+        if (c0 == 0) {  // the call's first half kick
+          const d3 a = kick_sum(pos, self, X0, T0, nm);
+          vel.x = fma(a.x, hdt, vel.x);
+          vel.y = fma(a.y, hdt, vel.y);
+          vel.z = fma(a.z, hdt, vel.z);
+        }
+        for (int k = 0; k < cn; k++) {
+          const bool last = c0 + k == A.steps - 1;
+          const Hist h = hist_at(hist, nh, k);
+          pos.x = fma(h.P1[0], hdt, pos.x);
+          pos.y = fma(h.P1[1], hdt, pos.y);
+          pos.z = fma(h.P1[2], hdt, pos.z);
+          bool ce;
+          drift(pos, vel, self, h, nm, ce);
+          f &= ~MERC_FLAG_CE_LAST;
+          if (ce) f |= MERC_FLAG_CE_LAST | MERC_FLAG_CE_EVER;
+          pos.x = fma(h.P2[0], hdt, pos.x);
+          pos.y = fma(h.P2[1], hdt, pos.y);
+          pos.z = fma(h.P2[2], hdt, pos.z);
+          // the second half kick of this step and (unless this is the last
+          // step of the call) the first of the next, in one pass
+          d3 accB = {0.0, 0.0, 0.0}, accA = {0.0, 0.0, 0.0};
           for (int i = 0; i < nm; i++) {
-            FastSrc SB = smem_src(X, M, TB, nmax, i);
-            const int thrA = thr_unpack(TA[4 * i + 3]);
-            double dx = SB.x - pos.x, dy = SB.y - pos.y, dz = SB.z - pos.z;
-            double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+            const FastSrc SB = smem_src(h.X2, M, h.T2, nh, i);
+            const int thrA = thr_unpack(h.TN[4 * i + 3]);
+            const double dx = SB.x - pos.x, dy = SB.y - pos.y, dz = SB.z - pos.z;
+            const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
             if (!last && hi_word(r2) > max(SB.rc2_hi, thrA) && i != self && seed_in_range(r2)) {
-              double w = SB.m * inv_softened_r3(r2, r2 + A.soft2);
+              const double w = SB.m * inv_softened_r3(r2, r2 + A.soft2);
               accB.x = fma(w, dx, accB.x);
               accB.y = fma(w, dy, accB.y);
               accB.z = fma(w, dz, accB.z);
@@ -288,7 +342,7 @@ __global__ void k_sweep_persistent(SweepArgs A) {
               accA.z = fma(w, dz, accA.z);
             } else {
               pair_fast<false>(pos, self, i, SB, A.soft2, accB);
-              if (!last) pair_fast<false>(pos, self, i, smem_src(X, M, TA, nmax, i), A.soft2, accA);
+              if (!last) pair_fast<false>(pos, self, i, smem_src(h.X2, M, h.TN, nh, i), A.soft2, accA);
             }
           }
           vel.x = fma(accB.x, hdt, vel.x);
@@ -299,41 +353,41 @@ __global__ void k_sweep_persistent(SweepArgs A) {
             vel.y = fma(accA.y, hdt, vel.y);
             vel.z = fma(accA.z, hdt, vel.z);
           }
+          f = step_flags(f, pos, vel);
         }
-        // flags of the step (positions are the step's final ones)
-        uint32_t f = F[j];
-        if (A.eject_r2 > 0.0 && mag2(pos) > A.eject_r2) f |= MERC_FLAG_EJECTED;
-        // the state checked is the one after the second half kick
-        bool fin = mm::isfinite_(pos.x) && mm::isfinite_(pos.y) && mm::isfinite_(pos.z) && mm::isfinite_(vel.x) &&
-                   mm::isfinite_(vel.y) && mm::isfinite_(vel.z);
-        if (!fin) f |= MERC_FLAG_NONFINITE;
-        F[j] = f;
-        V[j] = vel.x;
-        V[nmax + j] = vel.y;
-        V[2 * nmax + j] = vel.z;
+        D.x[g] = pos.x;
+        D.x[D.n + g] = pos.y;
+        D.x[2 * D.n + g] = pos.z;
+        D.v[g] = vel.x;
+        D.v[D.n + g] = vel.y;
+        D.v[2 * D.n + g] = vel.z;
+        D.flags[g] = f;
+        if (c0 + cn == A.steps) D.ce[g] = (f & MERC_FLAG_CE_LAST) ? 1 : 0;
       }
-      __syncthreads();
+      __syncthreads();  // before the next chunk overwrites the history
     }
-    // write the system back, and the radii the next call's first kick uses
-    for (int j = tid; j < n; j += T) {
-      D.x[b0 + j] = X[j];
-      D.x[D.n + b0 + j] = X[nmax + j];
-      D.x[2 * D.n + b0 + j] = X[2 * nmax + j];
-      D.v[b0 + j] = V[j];
-      D.v[D.n + b0 + j] = V[nmax + j];
-      D.v[2 * D.n + b0 + j] = V[2 * nmax + j];
-      D.flags[b0 + j] = F[j];
-      D.ce[b0 + j] = (F[j] & MERC_FLAG_CE_LAST) ? 1 : 0;
-    }
-    if (tid < nm) {
-      for (int k = 0; k < 4; k++) A.rc_final[4 * (size_t)(b0 + tid) + k] = TA[4 * tid + k];
+    // write the massive bodies back, and the radii the next call's first kick uses
+    if (warp == 0 && lane < nm) {
+      const int g = b0 + lane;
+      for (int c = 0; c < 3; c++) {
+        D.x[c * D.n + g] = XM[c * kSweepMaxNm + lane];
+        D.v[c * D.n + g] = VM[c * kSweepMaxNm + lane];
+      }
+      D.flags[g] = fm;
+      D.ce[g] = (fm & MERC_FLAG_CE_LAST) ? 1 : 0;
+      if (A.steps > 0) {
+        const Hist h = hist_at(hist, nh, (A.steps - 1) % C);
+        for (int k = 0; k < 4; k++) A.rc_final[4 * (size_t)g + k] = h.TN[4 * lane + k];
+      }
     }
     atomicAdd(&tally[0], my_ce);
     atomicAdd(&tally[1], my_it);
     atomicAdd(&tally[2], my_sol);
     atomicAdd(&tally[3], my_nc);
+    atomicAdd(&tally[4], my_simt);
+    my_ce = my_it = my_sol = my_nc = my_simt = 0;
     __syncthreads();
-    if (tid < 4 && tally[tid]) atomicAdd(&D.counters[tid], tally[tid]);
+    if (tid < kNumCounters && tally[tid]) atomicAdd(&D.counters[tid], tally[tid]);
     __syncthreads();
   }
 }

@@ -27,6 +27,7 @@ DRIFT_ELEMENTS = 0
 DRIFT_UNIVERSAL = 1
 WARM_PLAIN = 0
 WARM_MLP = 1
+WARM_SERIES = 2
 
 FLAG_CE_LAST = 1
 FLAG_CE_EVER = 2
@@ -67,6 +68,7 @@ class MercStats(C.Structure):
         ("n_bodies", C.c_int64),
         ("n_systems", C.c_int64),
         ("last_step_ms", C.c_double),
+        ("kepler_simt_iterations", C.c_int64),
     ]
 
 

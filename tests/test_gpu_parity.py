@@ -102,8 +102,8 @@ def test_universal_parity(oracle, which):
         sysm = systems.outer_solar_system()
     elif which == "embryo":
         sysm = systems.embryo_disk(n_embryos=254)
-    elif which == "sweep":
-        sysm = systems.sweep(n_systems=24, nt_lo=16, nt_hi=96)
+    elif which == "sweep":  # more systems than SMs: the persistent kernel
+        sysm = systems.sweep(n_systems=300, nt_lo=4, nt_hi=24)
     else:
         sysm = mixed_batch()
     st, gs, alag, (op, ov, oal, of, ost) = run_both(oracle, sysm, 100, drift=merc.DRIFT_UNIVERSAL)
@@ -125,8 +125,8 @@ def test_split_steps_and_resume_are_exact(drift, which):
     same bits; so does saving the state and resuming it in a new context."""
     if which == "embryo":
         sysm = systems.embryo_disk(n_embryos=94, seed=12)
-    else:
-        sysm = systems.sweep(n_systems=40, nt_lo=20, nt_hi=200, seed=12)
+    else:  # more systems than SMs: the persistent kernel
+        sysm = systems.sweep(n_systems=320, nt_lo=8, nt_hi=60, seed=12)
     kw = dict(dt=sysm.dt, hill_factor=3.0, drift=drift)
     a = merc.Integrator(merc.default_params(**kw))
     a.load_systems(sysm)
@@ -163,7 +163,7 @@ def test_persistent_sweep_kernel_equals_per_phase_kernels():
     """Small systems run in the persistent kernel (work queue, merged half
     kicks); with the drift log on they run in the per-phase kernels.  Both give
     the same bits."""
-    sysm = systems.sweep(n_systems=64, nt_lo=16, nt_hi=300, seed=31)
+    sysm = systems.sweep(n_systems=320, nt_lo=8, nt_hi=120, seed=31)  # more systems than SMs
     kw = dict(dt=sysm.dt, hill_factor=3.0, drift=merc.DRIFT_UNIVERSAL)
     a = merc.Integrator(merc.default_params(**kw))
     a.load_systems(sysm)
