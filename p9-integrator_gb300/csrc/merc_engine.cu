@@ -1479,7 +1479,7 @@ __global__ void k_mlp_probe(int n, const double* pos, const double* vel, double 
   WarmIn w = warm_features(x, v, dt);
   double s0 = (blob && w.f[0] >= kWarmMinX1) ? warm_guess(blob, w) : w.s0;
   guess[j] = s0;
-  UD u = universal_drift(x, v, dt, s0, tol, max_iter);
+  UD u = universal_drift(FU{1.0, -0.0}, x, v, dt, s0, tol, max_iter);
   solved[j] = u.s;
   iters[j] = u.iters;
 }

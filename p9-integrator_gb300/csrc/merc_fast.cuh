@@ -44,17 +44,17 @@ __device__ __forceinline__ int rc2_threshold(double rc) {
 // when (r2 + eps2)^2 r2 is a normal FP32 number (checked by the caller).  The
 // double <-> float moves of the seed are done on the integer pipes from the
 // high word (exponent rebias by 1023 - 127 = 896), so the FP64 pipe only sees
-// the 8 arithmetic operations.
-__device__ __forceinline__ double inv_softened_r3(double r2, double s) {
-  double q = s * s;
-  q = q * r2;
+// the 8 arithmetic operations (products as FMAs on the unit constants U).
+__device__ __forceinline__ double inv_softened_r3(const FU& U, double r2, double s) {
+  double q = fmul(U, s, s);
+  q = fmul(U, q, r2);
   float qf = __int_as_float((__double2hiint(q) - 0x38000000) << 3);
   int yb = __float_as_int(rsqrtf(qf));
   double u = __hiloint2double((yb >> 3) + 0x38000000, yb << 29);
-  double t = q * u;
+  double t = fmul(U, q, u);
   double e = fma(-t, u, 1.0);
   double c = fma(0.375, e, 0.5);
-  double ue = u * e;
+  double ue = fmul(U, u, e);
   return fma(ue, c, u);
 }
 
@@ -90,7 +90,8 @@ __device__ __forceinline__ void pair_exact(const d3& pos, int self, int i, const
 // r_crit.  The same decision r <= r_crit as the reference; the fast formula
 // for 1 / r^3 where r_crit is a positive finite number and r^2 is in the seed
 // range, the reference formula otherwise.
-__device__ __forceinline__ void bs_self_term(const d3& pos, int self, const FastSrc& S, double soft2, d3& acc) {
+__device__ __forceinline__ void bs_self_term(const FU& U, const d3& pos, int self, const FastSrc& S, double soft2,
+                                             d3& acc) {
   const d3 d = {S.x - pos.x, S.y - pos.y, S.z - pos.z};
   const double r_sq = mag2(d);
   if (!(S.rc > 0.0) || !(S.rc < 1e150) || !seed_in_range(r_sq)) {
@@ -98,7 +99,7 @@ __device__ __forceinline__ void bs_self_term(const d3& pos, int self, const Fast
     return;
   }
   if (!(stable_sqrt(r_sq) <= S.rc)) return;
-  const double wa = S.m * inv_softened_r3(r_sq, r_sq);
+  const double wa = fmul(U, S.m, inv_softened_r3(U, r_sq, r_sq));
   acc.x = fma(wa, d.x, acc.x);
   acc.y = fma(wa, d.y, acc.y);
   acc.z = fma(wa, d.z, acc.z);
@@ -106,16 +107,17 @@ __device__ __forceinline__ void bs_self_term(const d3& pos, int self, const Fast
 
 // One pair on the fast path when possible.
 template <bool BS>
-__device__ __forceinline__ void pair_fast(const d3& pos, int self, int i, const FastSrc& S, double soft2, d3& acc) {
-  double dx = S.x - pos.x, dy = S.y - pos.y, dz = S.z - pos.z;
-  double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+__device__ __forceinline__ void pair_fast(const FU& U, const d3& pos, int self, int i, const FastSrc& S, double soft2,
+                                          d3& acc) {
+  double dx = fsub(U, S.x, pos.x), dy = fsub(U, S.y, pos.y), dz = fsub(U, S.z, pos.z);
+  double r2 = fma(dx, dx, fma(dy, dy, fmul(U, dz, dz)));
   if (hi_word(r2) > S.rc2_hi && i != self && seed_in_range(r2)) {
-    double w = S.m * inv_softened_r3(r2, r2 + soft2);
+    double w = fmul(U, S.m, inv_softened_r3(U, r2, fadd(U, r2, soft2)));
     acc.x = fma(w, dx, acc.x);
     acc.y = fma(w, dy, acc.y);
     acc.z = fma(w, dz, acc.z);
   } else if (BS && i == self) {
-    bs_self_term(pos, self, S, soft2, acc);
+    bs_self_term(U, pos, self, S, soft2, acc);
   } else if (BS || i != self || r2 != 0.0) {
     // (in the plain kick a body's own entry, at distance zero, contributes
     // exactly zero: K = 0 and the guarded division returns 0)
@@ -125,12 +127,12 @@ __device__ __forceinline__ void pair_fast(const d3& pos, int self, int i, const 
 
 // Sun pull of the encounter sub-stepper: -pos / ((r^2 + eps^2) r)
 // (sim.cuh:431-441), fast where the seed range allows.
-__device__ __forceinline__ d3 sun_accel(const d3& pos, double soft2) {
-  double r2 = mag2(pos);
-  double s = r2 + soft2;
+__device__ __forceinline__ d3 sun_accel(const FU& U, const d3& pos, double soft2) {
+  double r2 = fma(pos.x, pos.x, fma(pos.y, pos.y, fmul(U, pos.z, pos.z)));
+  double s = fadd(U, r2, soft2);
   if (seed_in_range(r2)) {
-    double u = inv_softened_r3(r2, s);
-    return {-pos.x * u, -pos.y * u, -pos.z * u};
+    double u = inv_softened_r3(U, r2, s);
+    return {fmul(U, -pos.x, u), fmul(U, -pos.y, u), fmul(U, -pos.z, u)};
   }
   double r = stable_sqrt(r2);
   double denom = s * r;

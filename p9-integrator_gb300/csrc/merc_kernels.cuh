@@ -35,6 +35,7 @@ struct Work {
 };
 
 struct Dev {
+  FU u = {1.0, -0.0};  // run-time unit constants (fadd / fmul)
   int n = 0;     // bodies, all systems
   int nsys = 0;  // systems
   const int* off = nullptr;
@@ -434,7 +435,7 @@ __global__ void k_kick_small(Dev D, const double* __restrict__ rc_in, double* __
   const int b0 = D.off[s], nm = D.nm[s], local = j - b0, self = self_index(local, compat_block);
   d3 pos = load3(D.x, n, j);
   d3 acc = {0.0, 0.0, 0.0};
-  for (int i = 0; i < nm; i++) pair_fast<false>(pos, self, i, load_src(D, rc_in, b0 + i), soft2, acc);
+  for (int i = 0; i < nm; i++) pair_fast<false>(D.u, pos, self, i, load_src(D, rc_in, b0 + i), soft2, acc);
   d3 vel = load3(D.v, n, j);
   vel.x = fma(acc.x, hdt, vel.x);
   vel.y = fma(acc.y, hdt, vel.y);
@@ -469,7 +470,7 @@ __global__ void __launch_bounds__(kTile) k_kick_tiled(Dev D, const Work* __restr
     stage_sources(D, rc_in, b0, c, cnt, tile);
     __syncthreads();
     if (active)
-      for (int k = 0; k < cnt; k++) pair_fast<false>(pos, self, c + k, tile[k], soft2, acc);
+      for (int k = 0; k < cnt; k++) pair_fast<false>(D.u, pos, self, c + k, tile[k], soft2, acc);
   }
   if (!active) return;
   if (D.nchunk[s] == 1) {
@@ -515,10 +516,10 @@ __global__ void __launch_bounds__(kTile) k_kick_tiled_merged(Dev D, const Work* 
       for (int k = 0; k < cnt; k++) {
         const FastSrc& SB = tile[k];
         const int i = c + k;
-        double dx = SB.x - pos.x, dy = SB.y - pos.y, dz = SB.z - pos.z;
-        double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+        double dx = fsub(D.u, SB.x, pos.x), dy = fsub(D.u, SB.y, pos.y), dz = fsub(D.u, SB.z, pos.z);
+        double r2 = fma(dx, dx, fma(dy, dy, fmul(D.u, dz, dz)));
         if (hi_word(r2) > max(SB.rc2_hi, thr_unpack(tileA[k][3])) && i != self && seed_in_range(r2)) {
-          double w = SB.m * inv_softened_r3(r2, r2 + soft2);
+          double w = fmul(D.u, SB.m, inv_softened_r3(D.u, r2, fadd(D.u, r2, soft2)));
           accB.x = fma(w, dx, accB.x);
           accB.y = fma(w, dy, accB.y);
           accB.z = fma(w, dz, accB.z);
@@ -526,13 +527,13 @@ __global__ void __launch_bounds__(kTile) k_kick_tiled_merged(Dev D, const Work* 
           accA.y = fma(w, dy, accA.y);
           accA.z = fma(w, dz, accA.z);
         } else {
-          pair_fast<false>(pos, self, i, SB, soft2, accB);
+          pair_fast<false>(D.u, pos, self, i, SB, soft2, accB);
           FastSrc SA = SB;
           SA.rc = tileA[k][0];
           SA.rc01 = tileA[k][1];
           SA.rc09 = tileA[k][2];
           SA.rc2_hi = thr_unpack(tileA[k][3]);
-          pair_fast<false>(pos, self, i, SA, soft2, accA);
+          pair_fast<false>(D.u, pos, self, i, SA, soft2, accA);
         }
       }
     }
@@ -690,12 +691,13 @@ __global__ void __launch_bounds__(32 * kSymWarps) k_sym(Dev D, const SymTask* __
           if (mB && h <= A.thr && sqrt(r2) < rc[4 * (size_t)(b0 + A.idx)]) bitsB = 1u;
         }
       } else {
-        const double dx = B.x - A.x, dy = B.y - A.y, dz = B.z - A.z;
-        const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+        const FU& U = D.u;
+        const double dx = fsub(U, B.x, A.x), dy = fsub(U, B.y, A.y), dz = fsub(U, B.z, A.z);
+        const double r2 = fma(dx, dx, fma(dy, dy, fmul(U, dz, dz)));
         const int h = __double2hiint(r2);
         if (h > max(A.thr, B.thr) && seed_in_range(r2)) {
-          const double u = inv_softened_r3(r2, r2 + soft2);
-          const double wa = B.m * u, wb = A.m * u;
+          const double u = inv_softened_r3(U, r2, fadd(U, r2, soft2));
+          const double wa = fmul(U, B.m, u), wb = fmul(U, A.m, u);
           accA.x = fma(wa, dx, accA.x);
           accA.y = fma(wa, dy, accA.y);
           accA.z = fma(wa, dz, accA.z);
@@ -961,7 +963,7 @@ __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, doubl
         w = warm_features(pos, vel, dt);
         if (mlp && w.f[0] >= kWarmMinX1) s0 = warm_guess(blob, w);
       }
-      UD u = universal_drift(pos, vel, dt, s0, tol, max_iter);
+      UD u = universal_drift(D.u, pos, vel, dt, s0, tol, max_iter);
       store3(D.xo, n, j, u.out.pos);
       store3(D.vo, n, j, u.out.vel);
       its = u.iters;
@@ -1012,8 +1014,8 @@ struct FastVelTotal {
   double soft2;
   __device__ __forceinline__ d3 operator()(const d3& pos, const d3& vel, double dt) const {
     d3 acc = {0.0, 0.0, 0.0};
-    for (int i = 0; i < nm; i++) pair_fast<true>(pos, self, i, load_src(*D, rc, b0 + i), soft2, acc);
-    d3 sa = sun_accel(pos, soft2);
+    for (int i = 0; i < nm; i++) pair_fast<true>(D->u, pos, self, i, load_src(*D, rc, b0 + i), soft2, acc);
+    d3 sa = sun_accel(D->u, pos, soft2);
     d3 nv;
     nv.x = fma(sa.x, dt, fma(acc.x, dt, vel.x));
     nv.y = fma(sa.y, dt, fma(acc.y, dt, vel.y));
@@ -1048,7 +1050,7 @@ struct BlockVelTotal {
   __device__ __forceinline__ d3 operator()(const d3& pos, const d3& vel, double dt) const {
     d3 acc = {0.0, 0.0, 0.0};
     for (int i = threadIdx.x; i < nm; i += blockDim.x)
-      pair_fast<true>(pos, self, i, load_src(*D, rc, b0 + i), soft2, acc);
+      pair_fast<true>(D->u, pos, self, i, load_src(*D, rc, b0 + i), soft2, acc);
     const int t = threadIdx.x, B = blockDim.x;
     __syncthreads();
     red[t] = acc.x;
@@ -1064,7 +1066,7 @@ struct BlockVelTotal {
       __syncthreads();
     }
     acc = {red[0], red[B], red[2 * B]};
-    d3 sa = sun_accel(pos, soft2);
+    d3 sa = sun_accel(D->u, pos, soft2);
     d3 nv;
     nv.x = fma(sa.x, dt, fma(acc.x, dt, vel.x));
     nv.y = fma(sa.y, dt, fma(acc.y, dt, vel.y));
@@ -1099,11 +1101,12 @@ __global__ void __launch_bounds__(kEncThreads) k_encounter_big(Dev D, const doub
 __device__ __forceinline__ bool bs_fast_term(const Dev& D, const double* __restrict__ rc, int b0, int self, int i,
                                              const d3& pos, double soft2, d3& acc) {
   const int g = b0 + i;
-  const double dx = __ldg(D.x + g) - pos.x, dy = __ldg(D.x + D.n + g) - pos.y, dz = __ldg(D.x + 2 * D.n + g) - pos.z;
-  const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+  const double dx = fsub(D.u, __ldg(D.x + g), pos.x), dy = fsub(D.u, __ldg(D.x + D.n + g), pos.y),
+               dz = fsub(D.u, __ldg(D.x + 2 * D.n + g), pos.z);
+  const double r2 = fma(dx, dx, fma(dy, dy, fmul(D.u, dz, dz)));
   const bool far = hi_word(r2) > thr_unpack(__ldg(rc + 4 * (size_t)g + 3)) && i != self && seed_in_range(r2);
-  const double u = inv_softened_r3(r2, r2 + soft2);
-  const double w = far ? __ldg(D.m + g) * u : 0.0;
+  const double u = inv_softened_r3(D.u, r2, fadd(D.u, r2, soft2));
+  const double w = far ? fmul(D.u, __ldg(D.m + g), u) : 0.0;
   acc.x = fma(w, dx, acc.x);
   acc.y = fma(w, dy, acc.y);
   acc.z = fma(w, dz, acc.z);
@@ -1133,7 +1136,7 @@ __device__ __forceinline__ d3 warp_source_sum(const Dev& D, const double* __rest
       slow &= slow - 1ull;
       const int src = base + lane + 32 * q;
       if (src == self)
-        bs_self_term(pos, self, load_src(D, rc, b0 + src), soft2, ae);
+        bs_self_term(D.u, pos, self, load_src(D, rc, b0 + src), soft2, ae);
       else
         pair_exact<true>(pos, self, src, load_src(D, rc, b0 + src), soft2, ae);
     }
@@ -1180,7 +1183,7 @@ struct ClusterVelTotal {
       acc.z += rs[2];
     }
     (*parity)++;
-    d3 sa = sun_accel(pos, soft2);
+    d3 sa = sun_accel(D->u, pos, soft2);
     d3 nv;
     nv.x = fma(sa.x, dt, fma(acc.x, dt, vel.x));
     nv.y = fma(sa.y, dt, fma(acc.y, dt, vel.y));
@@ -1238,8 +1241,8 @@ struct MidRow {
     z0 = c.pos;
     vel = c.vel;
   }
-  __device__ __forceinline__ void finish_eval(const d3& acc, double soft2) {
-    const d3 sa = sun_accel(z1, soft2);
+  __device__ __forceinline__ void finish_eval(const FU& U, const d3& acc, double soft2) {
+    const d3 sa = sun_accel(U, z1, soft2);
     vel = {fma(sa.x, h, fma(acc.x, h, vel.x)), fma(sa.y, h, fma(acc.y, h, vel.y)),
            fma(sa.z, h, fma(acc.z, h, vel.z))};
     if (++done < N) {
@@ -1318,7 +1321,7 @@ __global__ void __cluster_dims__(kRowCluster, 1, 1) __launch_bounds__(32 * kRowB
           acc.y += rs[1];
           acc.z += rs[2];
         }
-        m.finish_eval(acc, soft2);
+        m.finish_eval(D.u, acc, soft2);
       } else {
         if (row == 1) {
           const double* ra = cl.map_shared_rank(&slot[buf][w][0], 4);
@@ -1335,7 +1338,7 @@ __global__ void __cluster_dims__(kRowCluster, 1, 1) __launch_bounds__(32 * kRowB
             acc.y += q[r].y;
             acc.z += q[r].z;
           }
-          m.finish_eval(acc, soft2);
+          m.finish_eval(D.u, acc, soft2);
         }
       }
     }

@@ -103,10 +103,11 @@ struct SmemVelTotal {  // encounter sub-step velocity update, sources in shared 
   const double *X, *M, *T;
   int nmax, nm, self;
   double soft2;
+  FU U;
   __device__ __forceinline__ d3 operator()(const d3& pos, const d3& vel, double dt) const {
     d3 acc = {0.0, 0.0, 0.0};
-    for (int i = 0; i < nm; i++) pair_fast<true>(pos, self, i, smem_src(X, M, T, nmax, i), soft2, acc);
-    d3 sa = sun_accel(pos, soft2);
+    for (int i = 0; i < nm; i++) pair_fast<true>(U, pos, self, i, smem_src(X, M, T, nmax, i), soft2, acc);
+    d3 sa = sun_accel(U, pos, soft2);
     d3 nv;
     nv.x = fma(sa.x, dt, fma(acc.x, dt, vel.x));
     nv.y = fma(sa.y, dt, fma(acc.y, dt, vel.y));
@@ -141,7 +142,7 @@ __global__ void k_sweep_persistent(SweepArgs A) {
       ce = ce || (ce_maybe(pf, h.F1[i], h.R1[i]) && pair_ce(pos, self, i, smem_src(h.X1, M, h.T1, nh, i)));
     PV out;
     if (ce) {
-      SmemVelTotal vt{h.X1, M, h.T1, nh, nm, self, A.soft2};
+      SmemVelTotal vt{h.X1, M, h.T1, nh, nm, self, A.soft2, D.u};
       out = richardson(PV{pos, vel}, vt, A.dt, A.rows);
       my_ce++;
     } else {
@@ -150,7 +151,7 @@ __global__ void k_sweep_persistent(SweepArgs A) {
         const WarmIn w = warm_features(pos, vel, A.dt);
         if (w.f[0] >= kWarmMinX1) s0 = warm_guess(blob, w);
       }
-      UD u = universal_drift(pos, vel, A.dt, s0, A.tol, A.max_iter);
+      UD u = universal_drift(D.u, pos, vel, A.dt, s0, A.tol, A.max_iter);
       out = u.out;
       my_it += u.iters;
       my_sol++;
@@ -165,7 +166,7 @@ __global__ void k_sweep_persistent(SweepArgs A) {
   };
   auto kick_sum = [&](const d3& pos, int self, const double* Xs, const double* Ts, int nm) {
     d3 acc = {0.0, 0.0, 0.0};
-    for (int i = 0; i < nm; i++) pair_fast<false>(pos, self, i, smem_src(Xs, M, Ts, nh, i), A.soft2, acc);
+    for (int i = 0; i < nm; i++) pair_fast<false>(D.u, pos, self, i, smem_src(Xs, M, Ts, nh, i), A.soft2, acc);
     return acc;
   };
   auto step_flags = [&](uint32_t f, const d3& pos, const d3& vel) {
@@ -330,10 +331,10 @@ __global__ void k_sweep_persistent(SweepArgs A) {
           for (int i = 0; i < nm; i++) {
             const FastSrc SB = smem_src(h.X2, M, h.T2, nh, i);
             const int thrA = thr_unpack(h.TN[4 * i + 3]);
-            const double dx = SB.x - pos.x, dy = SB.y - pos.y, dz = SB.z - pos.z;
-            const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+            const double dx = fsub(D.u, SB.x, pos.x), dy = fsub(D.u, SB.y, pos.y), dz = fsub(D.u, SB.z, pos.z);
+            const double r2 = fma(dx, dx, fma(dy, dy, fmul(D.u, dz, dz)));
             if (!last && hi_word(r2) > max(SB.rc2_hi, thrA) && i != self && seed_in_range(r2)) {
-              const double w = SB.m * inv_softened_r3(r2, r2 + A.soft2);
+              const double w = fmul(D.u, SB.m, inv_softened_r3(D.u, r2, fadd(D.u, r2, A.soft2)));
               accB.x = fma(w, dx, accB.x);
               accB.y = fma(w, dy, accB.y);
               accB.z = fma(w, dz, accB.z);
@@ -341,8 +342,8 @@ __global__ void k_sweep_persistent(SweepArgs A) {
               accA.y = fma(w, dy, accA.y);
               accA.z = fma(w, dz, accA.z);
             } else {
-              pair_fast<false>(pos, self, i, SB, A.soft2, accB);
-              if (!last) pair_fast<false>(pos, self, i, smem_src(h.X2, M, h.TN, nh, i), A.soft2, accA);
+              pair_fast<false>(D.u, pos, self, i, SB, A.soft2, accB);
+              if (!last) pair_fast<false>(D.u, pos, self, i, smem_src(h.X2, M, h.TN, nh, i), A.soft2, accA);
             }
           }
           vel.x = fma(accB.x, hdt, vel.x);
