@@ -139,8 +139,19 @@ __device__ __forceinline__ d3 sun_accel(const FU& U, const d3& pos, double soft2
   return {-(pos.x / denom), -(pos.y / denom), -(pos.z / denom)};
 }
 
+// x as an FP32 number by integer operations on the high word (sign, exponent
+// rebias, the top 20 mantissa bits; no conversion on the FP64 pipe): within
+// 2^-20 of x relative, 0 below the FP32 normal range (|x| < 2^-126), NaN above
+// it and for infinities and NaN (so that the prefilter answers "maybe").
+__device__ __forceinline__ float f32_trunc(double x) {
+  const int h = __double2hiint(x), m = h & 0x7fffffff;
+  if (m < 0x38100000) return 0.0f;
+  if (m >= 0x47F00000) return __int_as_float(0x7fc00000);
+  return __int_as_float((h & (int)0x80000000) | ((m - 0x38000000) << 3));
+}
+
 // FP32 positions of a body for the encounter prefilter: float copies and the
-// largest component magnitude (the scale of their rounding error).
+// largest component magnitude (the scale of their truncation error).
 struct F4 {
   float x, y, z, sc;
 };
@@ -149,14 +160,16 @@ __device__ __forceinline__ F4 f4_of(float x, float y, float z) {
 }
 
 // FP32 prefilter of the encounter test: false only when the pair is certainly
-// farther apart than r_crit.  The float copies are off by at most 2^-24 of each
-// coordinate, the difference and its square add a few 2^-24 relative
-// roundings, so |d| >= |d_f| (1 - 2e-7) - 2.1e-7 (sc_s + sc_t); the limit
-// r_crit (1 + 1e-6) + 1e-6 (sc_s + sc_t) covers that with room.  NaN -> maybe.
+// farther apart than r_crit.  The float copies (f32_trunc) are off by at most
+// 2^-20 of the body's largest coordinate (2^-126 below the normal range), the
+// difference and its square add a few 2^-24 relative roundings, so |d| >=
+// |d_f| (1 - 3e-7) - 1.7e-6 (sc_s + sc_t) - 4e-38, and r_crit in FP32 is at
+// most 2^-20 below r_crit; the limit r_crit (1 + 1e-5) + 1e-5 (sc_s + sc_t) +
+// 1e-37 covers that with room.  NaN anywhere -> maybe.
 __device__ __forceinline__ bool ce_maybe(const F4& t, const F4& s, float rc) {
   float dx = s.x - t.x, dy = s.y - t.y, dz = s.z - t.z;
   float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-  float lim = fmaf(rc, 1.000001f, 1e-6f * (s.sc + t.sc));
+  float lim = fmaf(rc, 1.00001f, fmaf(1e-5f, s.sc + t.sc, 1e-37f));
   return !(r2 > lim * lim && lim > 0.0f);
 }
 
@@ -172,7 +185,7 @@ __device__ __forceinline__ bool pair_ce(const d3& pos, int self, int i, const Fa
 // The same test behind the FP32 prefilter (no FP64 work for far pairs).
 __device__ __forceinline__ bool pair_ce_f(const d3& pos, const F4& tf, int self, int i, const FastSrc& S,
                                           const F4& sf) {
-  if (!ce_maybe(tf, sf, (float)S.rc)) return false;
+  if (!ce_maybe(tf, sf, f32_trunc(S.rc))) return false;
   return pair_ce(pos, self, i, S);
 }
 

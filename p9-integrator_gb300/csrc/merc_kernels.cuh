@@ -345,9 +345,9 @@ __global__ void __launch_bounds__(kJumpThreads) k_jump(Dev D, const double* __re
   x.y = fma(py, hdt, x.y);
   x.z = fma(pz, hdt, x.z);
   store3(D.x, n, j, x);
-  D.xf[j] = (float)x.x;
-  D.xf[n + j] = (float)x.y;
-  D.xf[2 * n + j] = (float)x.z;
+  D.xf[j] = f32_trunc(x.x);
+  D.xf[n + j] = f32_trunc(x.y);
+  D.xf[2 * n + j] = f32_trunc(x.z);
   d3 v;
   if (vsrc) {
     v = load3(vsrc, n, j);
@@ -654,7 +654,7 @@ __global__ void __launch_bounds__(32 * kSymWarps) k_sym(Dev D, const SymTask* __
   A.thr = iv ? (KICK ? far_thr[b0 + i] : thr_unpack(rc[4 * (size_t)(b0 + i) + 3])) : 0x7fffffff;
   A.idx = i;
   A.f = (!KICK && iv) ? load_f4(D, b0 + i) : F4{0.f, 0.f, 0.f, 0.f};
-  A.rcf = (!KICK && iv) ? (float)rc[4 * (size_t)(b0 + i)] : 0.f;
+  A.rcf = (!KICK && iv) ? f32_trunc(rc[4 * (size_t)(b0 + i)]) : 0.f;
   const int j0 = 32 * T.J + lane;
   const bool jv0 = j0 < nm;
   B.x = jv0 ? D.x[b0 + j0] : 0.0;
@@ -664,7 +664,7 @@ __global__ void __launch_bounds__(32 * kSymWarps) k_sym(Dev D, const SymTask* __
   B.thr = jv0 ? (KICK ? far_thr[b0 + j0] : thr_unpack(rc[4 * (size_t)(b0 + j0) + 3])) : 0x7fffffff;
   B.idx = jv0 ? j0 : -1;
   B.f = (!KICK && jv0) ? load_f4(D, b0 + j0) : F4{0.f, 0.f, 0.f, 0.f};
-  B.rcf = (!KICK && jv0) ? (float)rc[4 * (size_t)(b0 + j0)] : 0.f;
+  B.rcf = (!KICK && jv0) ? f32_trunc(rc[4 * (size_t)(b0 + j0)]) : 0.f;
   d3 accA = {0.0, 0.0, 0.0}, accB = {0.0, 0.0, 0.0};
   // KICK: near-pair bits (bit q: source 32 J + q for A, 32 I + q for B);
   // !KICK: encounter flags

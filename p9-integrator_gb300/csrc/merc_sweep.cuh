@@ -136,7 +136,7 @@ __global__ void k_sweep_persistent(SweepArgs A) {
   unsigned long long my_ce = 0, my_it = 0, my_sol = 0, my_nc = 0, my_simt = 0;
   // Kepler drift or encounter sub-step of one body whose sources are (Xs, Ts)
   auto drift = [&](d3& pos, d3& vel, int self, const Hist& h, int nm, bool& ce) {
-    const F4 pf = f4_of((float)pos.x, (float)pos.y, (float)pos.z);
+    const F4 pf = f4_of(f32_trunc(pos.x), f32_trunc(pos.y), f32_trunc(pos.z));
     ce = false;
     for (int i = 0; i < nm; i++)
       ce = ce || (ce_maybe(pf, h.F1[i], h.R1[i]) && pair_ce(pos, self, i, smem_src(h.X1, M, h.T1, nh, i)));
@@ -275,8 +275,8 @@ __global__ void k_sweep_persistent(SweepArgs A) {
           jump(h.P1);
           record(h.X1, h.T1);
           if (act) {
-            h.F1[lane] = f4_of((float)h.X1[lane], (float)h.X1[nh + lane], (float)h.X1[2 * nh + lane]);
-            h.R1[lane] = (float)h.T1[4 * lane];
+            h.F1[lane] = f4_of(f32_trunc(h.X1[lane]), f32_trunc(h.X1[nh + lane]), f32_trunc(h.X1[2 * nh + lane]));
+            h.R1[lane] = f32_trunc(h.T1[4 * lane]);
           }
           __syncwarp();
           if (act) {
