@@ -528,7 +528,9 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       }
     }
     const float* mlp = (p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) ? ctx->d_mlp : nullptr;
-    launch(k_drift_universal, (unsigned)((D.n + kDriftThreads - 1) / kDriftThreads), kDriftThreads, D, rcB, p.dt,
+    // one-warp blocks when kDriftThreads-blocks would leave SMs idle
+    const int dthr = (D.n + kDriftThreads - 1) / kDriftThreads < ctx->sms ? 32 : kDriftThreads;
+    launch(k_drift_universal, (unsigned)((D.n + dthr - 1) / dthr), dthr, D, rcB, p.dt,
            p.compat_block, p.kepler_tol, p.kepler_max_iter, guess_of(p), mlp, ctx->d_log, ctx->d_log_count,
            ctx->log_cap);
     nk++;

@@ -270,6 +270,10 @@ __global__ void k_momentum(Dev D, const double* __restrict__ vsrc, int skip_big)
 #define MERC_JUMP_THREADS 128
 #endif
 constexpr int kJumpThreads = MERC_JUMP_THREADS;  // block of the universal-path jumps
+#ifndef MERC_JUMP_BATCH
+#define MERC_JUMP_BATCH 8
+#endif
+constexpr int kJumpBatch = MERC_JUMP_BATCH;  // momentum terms loaded per thread before they are added
 template <bool BIG_P, bool CLEAR>
 __global__ void __launch_bounds__(kJumpThreads) k_jump(Dev D, const double* __restrict__ xsrc,
                                                       const double* __restrict__ vsrc, double* rc_out, double hdt) {
@@ -295,12 +299,27 @@ __global__ void __launch_bounds__(kJumpThreads) k_jump(Dev D, const double* __re
       if (!D.big[q]) continue;  // the same for every thread of the block
       const int b0 = D.off[q], nm = D.nm[q];
       double px = 0.0, py = 0.0, pz = 0.0;
-#pragma unroll 4
-      for (int i = threadIdx.x; i < nm; i += blockDim.x) {
-        const double mi = D.m[b0 + i];
-        px = fma(mi, vv[b0 + i], px);
-        py = fma(mi, vv[n + b0 + i], py);
-        pz = fma(mi, vv[2 * n + b0 + i], pz);
+      // kJumpBatch bodies' loads in flight before their products are added
+      // (same order of additions as one body at a time)
+      for (int i0 = threadIdx.x; i0 < nm; i0 += kJumpBatch * (int)blockDim.x) {
+        double mb[kJumpBatch], xb[kJumpBatch], yb[kJumpBatch], zb[kJumpBatch];
+#pragma unroll
+        for (int u = 0; u < kJumpBatch; u++) {
+          const int i = i0 + u * (int)blockDim.x;
+          const bool ok = i < nm;
+          mb[u] = ok ? D.m[b0 + i] : 0.0;
+          xb[u] = ok ? vv[b0 + i] : 0.0;
+          yb[u] = ok ? vv[n + b0 + i] : 0.0;
+          zb[u] = ok ? vv[2 * n + b0 + i] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < kJumpBatch; u++) {
+          if (i0 + u * (int)blockDim.x < nm) {
+            px = fma(mb[u], xb[u], px);
+            py = fma(mb[u], yb[u], py);
+            pz = fma(mb[u], zb[u], pz);
+          }
+        }
       }
       for (int o = 16; o > 0; o >>= 1) {
         px += __shfl_xor_sync(0xffffffffu, px, o);
@@ -601,14 +620,12 @@ struct RotSrc {
   float rcf;  // r_crit in FP32 (encounter prefilter)
 };
 
+// KICK rotates the FP64 source and the reverse accumulators; the encounter
+// test rotates the FP32 copies only (the rare pairs that pass its prefilter
+// read the FP64 position and r_crit of the source from memory)
 template <bool KICK>
 __device__ __forceinline__ void rotate(RotSrc& r, d3& acc, uint32_t& bits) {
   const int src = (threadIdx.x + 1) & 31;
-  r.x = __shfl_sync(0xffffffffu, r.x, src);
-  r.y = __shfl_sync(0xffffffffu, r.y, src);
-  r.z = __shfl_sync(0xffffffffu, r.z, src);
-  r.m = __shfl_sync(0xffffffffu, r.m, src);
-  r.thr = __shfl_sync(0xffffffffu, r.thr, src);
   r.idx = __shfl_sync(0xffffffffu, r.idx, src);
   if (!KICK) {
     r.f.x = __shfl_sync(0xffffffffu, r.f.x, src);
@@ -617,6 +634,11 @@ __device__ __forceinline__ void rotate(RotSrc& r, d3& acc, uint32_t& bits) {
     r.f.sc = __shfl_sync(0xffffffffu, r.f.sc, src);
     r.rcf = __shfl_sync(0xffffffffu, r.rcf, src);
   } else {
+    r.x = __shfl_sync(0xffffffffu, r.x, src);
+    r.y = __shfl_sync(0xffffffffu, r.y, src);
+    r.z = __shfl_sync(0xffffffffu, r.z, src);
+    r.m = __shfl_sync(0xffffffffu, r.m, src);
+    r.thr = __shfl_sync(0xffffffffu, r.thr, src);
     acc.x = __shfl_sync(0xffffffffu, acc.x, src);
     acc.y = __shfl_sync(0xffffffffu, acc.y, src);
     acc.z = __shfl_sync(0xffffffffu, acc.z, src);
@@ -650,18 +672,18 @@ __global__ void __launch_bounds__(32 * kSymWarps) k_sym(Dev D, const SymTask* __
   A.x = iv ? D.x[b0 + i] : 0.0;
   A.y = iv ? D.x[D.n + b0 + i] : 0.0;
   A.z = iv ? D.x[2 * D.n + b0 + i] : 0.0;
-  A.m = iv ? D.m[b0 + i] : 0.0;
+  A.m = (KICK && iv) ? D.m[b0 + i] : 0.0;
   A.thr = iv ? (KICK ? far_thr[b0 + i] : thr_unpack(rc[4 * (size_t)(b0 + i) + 3])) : 0x7fffffff;
   A.idx = i;
   A.f = (!KICK && iv) ? load_f4(D, b0 + i) : F4{0.f, 0.f, 0.f, 0.f};
   A.rcf = (!KICK && iv) ? f32_trunc(rc[4 * (size_t)(b0 + i)]) : 0.f;
   const int j0 = 32 * T.J + lane;
   const bool jv0 = j0 < nm;
-  B.x = jv0 ? D.x[b0 + j0] : 0.0;
-  B.y = jv0 ? D.x[D.n + b0 + j0] : 0.0;
-  B.z = jv0 ? D.x[2 * D.n + b0 + j0] : 0.0;
-  B.m = jv0 ? D.m[b0 + j0] : 0.0;
-  B.thr = jv0 ? (KICK ? far_thr[b0 + j0] : thr_unpack(rc[4 * (size_t)(b0 + j0) + 3])) : 0x7fffffff;
+  B.x = (KICK && jv0) ? D.x[b0 + j0] : 0.0;
+  B.y = (KICK && jv0) ? D.x[D.n + b0 + j0] : 0.0;
+  B.z = (KICK && jv0) ? D.x[2 * D.n + b0 + j0] : 0.0;
+  B.m = (KICK && jv0) ? D.m[b0 + j0] : 0.0;
+  B.thr = (KICK && jv0) ? far_thr[b0 + j0] : 0x7fffffff;
   B.idx = jv0 ? j0 : -1;
   B.f = (!KICK && jv0) ? load_f4(D, b0 + j0) : F4{0.f, 0.f, 0.f, 0.f};
   B.rcf = (!KICK && jv0) ? f32_trunc(rc[4 * (size_t)(b0 + j0)]) : 0.f;
@@ -684,10 +706,11 @@ __global__ void __launch_bounds__(32 * kSymWarps) k_sym(Dev D, const SymTask* __
         // the FP32 prefilter clears far pairs without FP64 work
         const bool mA = ce_maybe(A.f, B.f, B.rcf), mB = ce_maybe(B.f, A.f, A.rcf);
         if (mA || mB) {
-          const double dx = B.x - A.x, dy = B.y - A.y, dz = B.z - A.z;
+          const int g = b0 + B.idx;
+          const double dx = D.x[g] - A.x, dy = D.x[D.n + g] - A.y, dz = D.x[2 * D.n + g] - A.z;
           const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
           const int h = __double2hiint(r2);
-          if (mA && h <= B.thr && sqrt(r2) < rc[4 * (size_t)(b0 + B.idx)]) bitsA = 1u;
+          if (mA && h <= thr_unpack(rc[4 * (size_t)g + 3]) && sqrt(r2) < rc[4 * (size_t)g]) bitsA = 1u;
           if (mB && h <= A.thr && sqrt(r2) < rc[4 * (size_t)(b0 + A.idx)]) bitsB = 1u;
         }
       } else {
@@ -761,6 +784,10 @@ __global__ void __launch_bounds__(32 * kSymWarps) k_sym(Dev D, const SymTask* __
 #define MERC_RED_THREADS 16
 #endif
 constexpr int kRedThreads = MERC_RED_THREADS;  // threads per body of k_kick_reduce_sym (a power of two <= 32)
+#ifndef MERC_RED_BATCH
+#define MERC_RED_BATCH 4
+#endif
+constexpr int kRedBatch = MERC_RED_BATCH;  // partials loaded per thread before they are added
 
 // Kick of every body of a big system whose sums are in partials: massive
 // bodies add their far-field block partials (symmetric kernel, set 1 when
@@ -808,23 +835,50 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   }
   const size_t span = stride / 3;
   d3 acc = {0.0, 0.0, 0.0};
-#pragma unroll 4
-  for (int b = sub; b < count; b += kRedThreads) {
-    const double* p = base + (size_t)b * stride;
-    acc.x += p[index];
-    acc.y += p[span + index];
-    acc.z += p[2 * span + index];
+  d3 pos = {0.0, 0.0, 0.0}, vel = {0.0, 0.0, 0.0};
+  if (work) {
+    pos = load3(D.x, n, j);
+    if (sub == 0) vel = load3(D.v, n, j);
+  }
+  // kRedBatch partials' loads in flight before they are added (same order of
+  // additions as one at a time); the near-pair mask words with them
+  uint32_t words[kRedBatch];
+#pragma unroll
+  for (int u = 0; u < kRedBatch; u++) words[u] = 0u;
+  for (int b0r = sub, r = 0; b0r < count; b0r += kRedBatch * kRedThreads, r++) {
+    double px[kRedBatch], py[kRedBatch], pz[kRedBatch];
+#pragma unroll
+    for (int u = 0; u < kRedBatch; u++) {
+      const int b = b0r + u * kRedThreads;
+      const bool ok = b < count;
+      const double* p = base + (size_t)b * stride;
+      px[u] = ok ? p[index] : 0.0;
+      py[u] = ok ? p[span + index] : 0.0;
+      pz[u] = ok ? p[2 * span + index] : 0.0;
+      if (r == 0) words[u] = (ok && massive) ? mask[(size_t)b * nm + local] : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < kRedBatch; u++) {
+      if (b0r + u * kRedThreads < count) {
+        acc.x += px[u];
+        acc.y += py[u];
+        acc.z += pz[u];
+      }
+    }
   }
   d3 near = {0.0, 0.0, 0.0};
-  d3 pos = {0.0, 0.0, 0.0};
-  if (work) pos = load3(D.x, n, j);
   if (massive) {
-    for (int b = sub; b < count; b += kRedThreads) {
-      uint32_t w = mask[(size_t)b * nm + local];
-      while (w) {
-        const int q = __ffs(w) - 1;
-        w &= w - 1u;
-        const int src = 32 * b + q;
+#pragma unroll
+    for (int u = 0; u < kRedBatch; u++) {
+      const int b = sub + u * kRedThreads;
+      for (uint32_t w = words[u]; w; w &= w - 1u) {
+        const int src = 32 * b + __ffs(w) - 1;
+        pair_exact<false>(pos, local, src, load_src(D, rc, b0 + src), soft2, near);
+      }
+    }
+    for (int b = sub + kRedBatch * kRedThreads; b < count; b += kRedThreads) {
+      for (uint32_t w = mask[(size_t)b * nm + local]; w; w &= w - 1u) {
+        const int src = 32 * b + __ffs(w) - 1;
         pair_exact<false>(pos, local, src, load_src(D, rc, b0 + src), soft2, near);
       }
     }
@@ -843,7 +897,6 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
     acc.y += near.y;
     acc.z += near.z;
   }
-  d3 vel = load3(D.v, n, j);
   vel.x = fma(acc.x, hdt, vel.x);
   vel.y = fma(acc.y, hdt, vel.y);
   vel.z = fma(acc.z, hdt, vel.z);
