@@ -53,6 +53,8 @@ struct merc_ctx {
   int device = 0;
   merc_params p{};
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // second branch of the step graphs (drift beside the encounter sub-step)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::string err;
   Dev D;
   int* d_off = nullptr;
@@ -285,7 +287,7 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
       (st = dalloc(ctx, &D.v, 3 * (size_t)n)) || (st = dalloc(ctx, &D.xo, 3 * (size_t)n)) ||
       (st = dalloc(ctx, &D.xf, 3 * (size_t)n)) ||
       (st = dalloc(ctx, &D.vo, 3 * (size_t)n)) || (st = dalloc(ctx, &D.alag, n)) || (st = dalloc(ctx, &D.flags, n)) ||
-      (st = dalloc(ctx, &D.ce, n)) || (st = dalloc(ctx, &D.rc[0], rc_table_doubles(n))) ||
+      (st = dalloc(ctx, &D.ce, ((size_t)n + 3) & ~(size_t)3)) || (st = dalloc(ctx, &D.rc[0], rc_table_doubles(n))) ||
       (st = dalloc(ctx, &D.rc[1], rc_table_doubles(n))) || (st = dalloc(ctx, &D.P, 3 * (size_t)n_systems)) ||
       (st = dalloc(ctx, &D.ce_list, n)) || (st = dalloc(ctx, &D.ce_count, 2)) || (st = dalloc(ctx, &D.counters, kNumCounters)))
     return st;
@@ -530,9 +532,22 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     const float* mlp = (p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) ? ctx->d_mlp : nullptr;
     // one-warp blocks when kDriftThreads-blocks would leave SMs idle
     const int dthr = (D.n + kDriftThreads - 1) / kDriftThreads < ctx->sms ? 32 : kDriftThreads;
-    launch(k_drift_universal, (unsigned)((D.n + dthr - 1) / dthr), dthr, D, rcB, p.dt,
-           p.compat_block, p.kepler_tol, p.kepler_max_iter, guess_of(p), mlp, ctx->d_log, ctx->d_log_count,
-           ctx->log_cap);
+    // Without small systems the drift (bodies not in encounter) and the big
+    // systems' encounter sub-step (the list built by the encounter test) are
+    // independent: the drift runs on a second branch beside it.
+    const bool fork = !ctx->has_small && ctx->has_big;
+    if (fork) {
+      CK(cudaEventRecord(ctx->ev_fork, s));
+      CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+      k_drift_universal<<<(unsigned)((D.n + dthr - 1) / dthr), dthr, 0, ctx->side>>>(
+          D, rcB, p.dt, p.compat_block, p.kepler_tol, p.kepler_max_iter, guess_of(p), mlp, ctx->d_log,
+          ctx->d_log_count, ctx->log_cap);
+      CK(cudaGetLastError());
+      CK(cudaEventRecord(ctx->ev_join, ctx->side));
+    } else {
+      launch(k_drift_universal, (unsigned)((D.n + dthr - 1) / dthr), dthr, D, rcB, p.dt, p.compat_block,
+             p.kepler_tol, p.kepler_max_iter, guess_of(p), mlp, ctx->d_log, ctx->d_log_count, ctx->log_cap);
+    }
     nk++;
     if (ctx->has_small) {
       launch(k_encounter_small, ctx->enc_blocks, 64, D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2);
@@ -547,6 +562,7 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
                p.softening2);
       nk++;
     }
+    if (fork) CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
     momentum(D.vo);
     launch(k_jump<true, false>, njb, kJumpThreads, D, D.xo, D.vo, rcB, hdt);
     nk++;
@@ -780,6 +796,9 @@ int merc_create(int device, const merc_params* p, merc_ctx** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) {
@@ -802,6 +821,9 @@ int merc_destroy(merc_ctx* ctx) {
   for (cudaEvent_t e : ctx->kick_ev) cudaEventDestroy(e);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->side) cudaStreamDestroy(ctx->side);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return MERC_OK;
@@ -1692,11 +1714,11 @@ extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodi
     kick(rcA, nullptr, 0);
     momentum(D.v);
     k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt);
+    CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
     if (big) {
       CK(cudaMemsetAsync(D.ce, 0, n, s));
       k_ce_tiled<<<(unsigned)work.size(), kTile, 0, s>>>(D, d_work, rcB, p->compat_block);
     }
-    CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
     k_drift_universal<<<nb, kThreads, 0, s>>>(D, rcB, p->dt, p->compat_block, p->kepler_tol, p->kepler_max_iter,
                                               guess_of(*p), nullptr, nullptr, nullptr, 0);
     if (!big)

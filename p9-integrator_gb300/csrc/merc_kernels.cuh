@@ -377,6 +377,15 @@ __global__ void __launch_bounds__(kJumpThreads) k_jump(Dev D, const double* __re
   if (j - D.off[s] < D.nm[s]) write_rc(rc_out, n, j, x, v, D.hc[j]);
 }
 
+// Sets body j's encounter flag (one byte of D.ce, by an atomic OR on its
+// aligned 32-bit word; the flag array is allocated in whole words); true for
+// the first caller of the step, which appends the body to the list.
+__device__ __forceinline__ bool mark_ce(unsigned char* ce, int j) {
+  unsigned* w = (unsigned*)(ce + (j & ~3));
+  const unsigned bit = 1u << (8 * (j & 3));
+  return !(atomicOr(w, bit) & bit);
+}
+
 // warp-aggregated append to an encounter list (ballot + prefix count)
 __device__ __forceinline__ void append_ce(bool flag, int j, int* list, int* count, unsigned long long* tally) {
   const int lane = threadIdx.x & 31;
@@ -775,8 +784,11 @@ __global__ void __launch_bounds__(32 * kSymWarps) k_sym(Dev D, const SymTask* __
       }
     }
   } else {
-    if (iv && bitsA) D.ce[b0 + i] = 1;
-    if (jv0 && bitsB) D.ce[b0 + j0] = 1;
+    // flags and the big-system encounter list (each body once)
+    const bool fa = iv && bitsA && mark_ce(D.ce, b0 + i);
+    const bool fb = jv0 && bitsB && mark_ce(D.ce, b0 + j0);
+    append_ce(fa, b0 + i, D.ce_list_big, &D.ce_count[1], &D.counters[0]);
+    append_ce(fb, b0 + j0, D.ce_list_big, &D.ce_count[1], &D.counters[0]);
   }
 }
 
@@ -905,7 +917,8 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
 }
 
 // Tiled encounter test of the big systems: any source of the chunk within
-// r_crit sets ce[j] (the flags were cleared before the launch).
+// r_crit sets ce[j] (the flags were cleared before the launch) and appends j
+// to the big-system encounter list once.
 __global__ void __launch_bounds__(kTile) k_ce_tiled(Dev D, const Work* __restrict__ work,
                                                     const double* __restrict__ rc_in, int compat_block) {
   griddep_enter();
@@ -928,7 +941,8 @@ __global__ void __launch_bounds__(kTile) k_ce_tiled(Dev D, const Work* __restric
     if (active)
       for (int k = 0; k < cnt; k++) ce = ce || pair_ce_f(pos, pf, self, c + k, tile[k], tilef[k]);
   }
-  if (active && ce) D.ce[j] = 1;
+  const bool first = active && ce && mark_ce(D.ce, j);
+  append_ce(first, j, D.ce_list_big, &D.ce_count[1], &D.counters[0]);
 }
 
 // Momentum of each big system: block per system, strided partial sums and a
@@ -966,7 +980,9 @@ __global__ void __launch_bounds__(kMomThreads) k_momentum_big(Dev D, const int* 
 }
 
 // Encounter test (small systems inline, big systems from ce[]) and universal
-// drift of every body not in encounter; encounter bodies go to the lists.
+// drift of every body not in encounter; encounter bodies of small systems go
+// to the small list (the big systems' list was built by their encounter test,
+// so this kernel may run beside the big systems' encounter sub-step).
 // guess: kGuessPlain or kGuessSeries (universal_drift); mlp != nullptr:
 // learned warm start of the solve (merc_mlp.cuh).  log_data
 // != nullptr: every solve with x1 >= kWarmMinX1 appends its features and
@@ -989,7 +1005,7 @@ __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, doubl
   }
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
-  bool ce_small = false, ce_big = false, logit = false;
+  bool ce_small = false, logit = false;
   int its = 0, nonconv = 0, solved = 0;
   float rec[5];
   if (j < D.n) {
@@ -998,7 +1014,6 @@ __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, doubl
     bool is_ce;
     if (D.big[s]) {
       is_ce = D.ce[j] != 0;
-      ce_big = is_ce;
     } else {
       const int self = self_index(j - b0, compat_block);
       const F4 pf = load_f4(D, j);
@@ -1033,7 +1048,6 @@ __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, doubl
     }
   }
   append_ce(ce_small, j, D.ce_list, &D.ce_count[0], &D.counters[0]);
-  append_ce(ce_big, j, D.ce_list_big, &D.ce_count[1], &D.counters[0]);
   if (log_data) {
     unsigned mask = __ballot_sync(0xffffffffu, logit);
     if (mask) {
