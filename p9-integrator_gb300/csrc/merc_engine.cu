@@ -513,7 +513,13 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     momentum(D.v);
     // also clears the encounter flags and list counts of this step
     const unsigned njb = (unsigned)((D.n + kJumpThreads - 1) / kJumpThreads);
-    launch(k_jump<true, true>, njb, kJumpThreads, D, D.x, nullptr, rcB, hdt);
+    // one big system: the momentum is split over the blocks of a cluster
+    const bool jump_cl = D.nsys == 1 && ctx->has_big;
+    const unsigned njc = (njb + kJumpCluster - 1) / kJumpCluster * kJumpCluster;
+    if (jump_cl)
+      launch(k_jump_cluster<true>, njc, kJumpThreads, D, D.x, (const double*)nullptr, rcB, hdt);
+    else
+      launch(k_jump<true, true>, njb, kJumpThreads, D, D.x, nullptr, rcB, hdt);
     nk++;
     if (ctx->has_big) {
       if (use_sym) {
@@ -564,7 +570,10 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     }
     if (fork) CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
     momentum(D.vo);
-    launch(k_jump<true, false>, njb, kJumpThreads, D, D.xo, D.vo, rcB, hdt);
+    if (jump_cl)
+      launch(k_jump_cluster<false>, njc, kJumpThreads, D, (const double*)D.xo, (const double*)D.vo, rcB, hdt);
+    else
+      launch(k_jump<true, false>, njb, kJumpThreads, D, D.xo, D.vo, rcB, hdt);
     nk++;
     if ((st = kick(rcB, rcA, 1, 2))) return st;
     if (lerr != cudaSuccess) return fail(ctx, MERC_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(lerr));

@@ -377,6 +377,107 @@ __global__ void __launch_bounds__(kJumpThreads) k_jump(Dev D, const double* __re
   if (j - D.off[s] < D.nm[s]) write_rc(rc_out, n, j, x, v, D.hc[j]);
 }
 
+// Solar jump of a single big system (system 0 holds every body) by clusters
+// of kJumpCluster blocks: block r of a cluster sums the momentum of massive
+// bodies [r nm / 8, (r + 1) nm / 8) (thread t adds bodies t, t + B, ...; a
+// fixed butterfly per warp; warp sums in warp order), the cluster exchanges
+// the eight partials through distributed shared memory and every block adds
+// them in rank order, so every cluster gets the same bits with one eighth of
+// the momentum work per block.  Then as k_jump: x = xsrc + dt/2 P, v copied
+// from vsrc when given, new r_crit of massive bodies; CLEAR also clears the
+// encounter flags and list counts.  The grid is a whole number of clusters.
+constexpr int kJumpCluster = 8;
+template <bool CLEAR>
+__global__ void __cluster_dims__(kJumpCluster, 1, 1) __launch_bounds__(kJumpThreads)
+    k_jump_cluster(Dev D, const double* __restrict__ xsrc, const double* __restrict__ vsrc, double* rc_out,
+                   double hdt) {
+  griddep_enter();
+  namespace cg = cooperative_groups;
+  __shared__ double wsum[kJumpThreads / 32][3];
+  __shared__ double part[3];
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j == 0) {
+    if (D.gate) *D.gate = 0;  // the last merged kick has read it
+    if (CLEAR) D.ce_count[0] = D.ce_count[1] = 0;
+  }
+  const int n = D.n, nm = D.nm[0];
+  const double* vv = vsrc ? vsrc : D.v;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int i0 = (int)((int64_t)rank * nm / kJumpCluster), i1 = (int)((int64_t)(rank + 1) * nm / kJumpCluster);
+  double px = 0.0, py = 0.0, pz = 0.0;
+  for (int c = i0 + (int)threadIdx.x; c < i1; c += kJumpBatch * (int)blockDim.x) {
+    double mb[kJumpBatch], xb[kJumpBatch], yb[kJumpBatch], zb[kJumpBatch];
+#pragma unroll
+    for (int u = 0; u < kJumpBatch; u++) {
+      const int i = c + u * (int)blockDim.x;
+      const bool ok = i < i1;
+      mb[u] = ok ? D.m[i] : 0.0;
+      xb[u] = ok ? vv[i] : 0.0;
+      yb[u] = ok ? vv[n + i] : 0.0;
+      zb[u] = ok ? vv[2 * n + i] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kJumpBatch; u++) {
+      if (c + u * (int)blockDim.x < i1) {
+        px = fma(mb[u], xb[u], px);
+        py = fma(mb[u], yb[u], py);
+        pz = fma(mb[u], zb[u], pz);
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    px += __shfl_xor_sync(0xffffffffu, px, o);
+    py += __shfl_xor_sync(0xffffffffu, py, o);
+    pz += __shfl_xor_sync(0xffffffffu, pz, o);
+  }
+  if (lane == 0) {
+    wsum[warp][0] = px;
+    wsum[warp][1] = py;
+    wsum[warp][2] = pz;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int w = 0; w < nw; w++) {
+      sx += wsum[w][0];
+      sy += wsum[w][1];
+      sz += wsum[w][2];
+    }
+    part[0] = sx;
+    part[1] = sy;
+    part[2] = sz;
+  }
+  cl.sync();
+  double Px = 0.0, Py = 0.0, Pz = 0.0;
+  for (int r = 0; r < kJumpCluster; r++) {
+    const double* q = cl.map_shared_rank(part, r);
+    Px += q[0];
+    Py += q[1];
+    Pz += q[2];
+  }
+  cl.sync();  // no block leaves while another may still read its partial
+  if (j >= n) return;
+  if (CLEAR) D.ce[j] = 0;
+  d3 x = load3(xsrc, n, j);
+  x.x = fma(Px, hdt, x.x);
+  x.y = fma(Py, hdt, x.y);
+  x.z = fma(Pz, hdt, x.z);
+  store3(D.x, n, j, x);
+  D.xf[j] = f32_trunc(x.x);
+  D.xf[n + j] = f32_trunc(x.y);
+  D.xf[2 * n + j] = f32_trunc(x.z);
+  d3 v;
+  if (vsrc) {
+    v = load3(vsrc, n, j);
+    store3(D.v, n, j, v);
+  } else {
+    v = load3(D.v, n, j);
+  }
+  if (j < nm) write_rc(rc_out, n, j, x, v, D.hc[j]);
+}
+
 // Sets body j's encounter flag (one byte of D.ce, by an atomic OR on its
 // aligned 32-bit word; the flag array is allocated in whole words); true for
 // the first caller of the step, which appends the body to the list.
