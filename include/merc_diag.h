@@ -56,6 +56,16 @@ int merc_diag_far_recomputes(merc_ctx* ctx, int64_t* count);
  * depend on it.  Takes effect when the step graphs are next captured. */
 int merc_diag_pdl(merc_ctx* ctx, int on);
 
+/* Check of the bounded waits of the encounter sub-step (big systems): runs the
+ * encounter task kernel once for the first body of the first big system with
+ * the tasks of its first evaluation of row 2 skipped, so the later
+ * evaluations of that row wait for a state that is never published, with a
+ * short wait limit.  *gave_up = 1 when the kernel reported that a wait gave up
+ * (the expected outcome).  The body's state is not touched; the step state
+ * of the encounter kernel is cleared afterwards.  MERC_ERR_STATE without a
+ * loaded big system. */
+int merc_diag_encounter_wait(merc_ctx* ctx, int32_t* gave_up);
+
 #ifdef __cplusplus
 }
 #endif

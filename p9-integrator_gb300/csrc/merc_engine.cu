@@ -278,6 +278,16 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
       (st = dalloc(ctx, &D.part_sym, 2 * (size_t)sym_set)) || (st = dalloc(ctx, &D.near_mask, 2 * (size_t)(sym_set / 3))) ||
       (st = dalloc(ctx, &D.gate, 1)) || (st = dalloc(ctx, &D.far_recomputes, 1)))
     return st;
+  {
+    // encounter task kernel state (every body of a big system may be listed)
+    const size_t ne = ctx->has_big ? (size_t)n : 1;
+    if ((st = dalloc(ctx, &D.enc_q, 84 * ne)) || (st = dalloc(ctx, &D.enc_st, 27 * ne)) ||
+        (st = dalloc(ctx, &D.enc_res, 18 * ne)) || (st = dalloc(ctx, &D.enc_cnt, 11 * ne)) ||
+        (st = dalloc(ctx, &D.enc_head, 2)))
+      return st;
+    CK(cudaMemsetAsync(D.enc_cnt, 0, sizeof(int) * 11 * ne, ctx->stream));
+    CK(cudaMemsetAsync(D.enc_head, 0, sizeof(int) * 2, ctx->stream));
+  }
   D.sym_set = sym_set;
   CK(cudaMemsetAsync(D.gate, 0, sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(D.far_recomputes, 0, sizeof(unsigned long long), ctx->stream));
@@ -561,8 +571,8 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     }
     if (ctx->has_big) {
       if (p.bs_rows == 3)
-        launch(k_encounter_rows, (ctx->enc_blocks / 4) * kRowCluster, 32 * kRowBodies, D, rcB, p.dt,
-               p.compat_block, p.softening2);
+        launch(k_encounter_tasks, ctx->sms * kEncBlocksPerSM, 32 * kEncTaskWarps, D, rcB, p.dt, p.compat_block,
+               p.softening2, kEncSpin);
       else
         launch(k_encounter_cluster, ctx->enc_blocks * 2, 32, D, rcB, p.dt, p.compat_block, p.bs_rows,
                p.softening2);
@@ -971,6 +981,14 @@ int merc_step(merc_ctx* ctx, int64_t n_steps) {
   CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   ctx->last_ms = ms;
   ctx->steps_done += n_steps;
+  if (ctx->has_big && ctx->D.enc_head) {
+    int gave_up = 0;
+    CK(cudaMemcpy(&gave_up, ctx->D.enc_head + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    if (gave_up) {
+      ctx->loaded = false;  // the encounter state is incomplete: load again
+      return fail(ctx, MERC_ERR_TIMEOUT, "encounter sub-step: a bounded device wait gave up");
+    }
+  }
   return MERC_OK;
 }
 
@@ -1827,6 +1845,39 @@ int merc_diag_pdl(merc_ctx* ctx, int on) {
   if (!ctx) return MERC_ERR_CONFIG;
   ctx->pdl = on != 0;
   drop_graphs(ctx);
+  return MERC_OK;
+}
+
+int merc_diag_encounter_wait(merc_ctx* ctx, int32_t* gave_up) {
+  if (!ctx || !gave_up) return MERC_ERR_CONFIG;
+  if (!ctx->loaded || !ctx->has_big) return fail(ctx, MERC_ERR_STATE, "no big system loaded");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  Dev& D = ctx->D;
+  int body = 0;
+  for (int s = 0; s < D.nsys; s++)
+    if (ctx->h_nm[s] > kSmallNm) {
+      body = (int)ctx->h_off[s];
+      break;
+    }
+  // one listed body; tasks start at the second unit (the first unit, row 2's
+  // evaluation 0 of every listed body, is skipped)
+  const int one = 1, head[2] = {4, 0};
+  CK(cudaMemcpy(D.ce_list_big, &body, sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(D.ce_count + 1, &one, sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(D.enc_head, head, sizeof head, cudaMemcpyHostToDevice));
+  CK(cudaMemset(D.enc_cnt, 0, 11 * sizeof(int)));
+  k_encounter_tasks<<<ctx->sms * kEncBlocksPerSM, 32 * kEncTaskWarps, 0, ctx->stream>>>(
+      D, D.rc[ctx->rc_cur], ctx->p.dt, ctx->p.compat_block, ctx->p.softening2, 4096);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  int h[2] = {0, 0};
+  CK(cudaMemcpy(h, D.enc_head, sizeof h, cudaMemcpyDeviceToHost));
+  *gave_up = h[1] != 0;
+  // the step state of the encounter kernel back to zero
+  CK(cudaMemset(D.enc_cnt, 0, 11 * sizeof(int)));
+  CK(cudaMemset(D.enc_head, 0, 2 * sizeof(int)));
+  CK(cudaMemset(D.ce_count, 0, 2 * sizeof(int)));
   return MERC_OK;
 }
 

@@ -69,6 +69,13 @@ struct Dev {
   int* ce_count = nullptr;           // [0] small list, [1] big list
   unsigned long long* counters = nullptr;  // kNumCounters: CE body-steps, Kepler iterations, solves,
                                            // non-converged, iterations executed per warp (SIMT)
+  // encounter task kernel, per entry of the big-system encounter list:
+  double* enc_q = nullptr;    // 84: quarter sums of the 7 evaluations (4 x 3 each)
+  double* enc_st = nullptr;   // 27: per row z0, z1, vel after its last published evaluation
+  double* enc_res = nullptr;  // 18: per row the sub-step result (position, velocity)
+  int* enc_cnt = nullptr;     // 11: quarters done per evaluation (7), evaluations published per row (3),
+                              //     rows done (1); zero between steps
+  int* enc_head = nullptr;    // [0] next task (cleared by the first jump), [1] a bounded wait gave up
 };
 
 __device__ __forceinline__ SrcView src_view(const Dev& D, const double* rc, int b0) {
@@ -284,6 +291,7 @@ __global__ void __launch_bounds__(kJumpThreads) k_jump(Dev D, const double* __re
   if (j == 0) {
     if (D.gate) *D.gate = 0;  // the last merged kick has read it
     if (CLEAR) D.ce_count[0] = D.ce_count[1] = 0;
+    if (CLEAR && D.enc_head) D.enc_head[0] = 0;
   }
   const int n = D.n;
   const int j0 = blockIdx.x * blockDim.x, j1 = min(n, j0 + (int)blockDim.x);
@@ -401,6 +409,7 @@ __global__ void __cluster_dims__(kJumpCluster, 1, 1) __launch_bounds__(kJumpThre
   if (j == 0) {
     if (D.gate) *D.gate = 0;  // the last merged kick has read it
     if (CLEAR) D.ce_count[0] = D.ce_count[1] = 0;
+    if (CLEAR && D.enc_head) D.enc_head[0] = 0;
   }
   const int n = D.n, nm = D.nm[0];
   const double* vv = vsrc ? vsrc : D.v;
@@ -1428,112 +1437,167 @@ struct MidRow {
   }
 };
 
-// Encounter sub-step with three Richardson rows (N = 1, 2, 4) run side by
-// side: a cluster of 7 blocks serves kRowBodies bodies, warp w of every block
-// working on body w; ranks 0-3 run row 2, ranks 4-5 row 1, rank 6 row 0.  The
-// rows are independent until the final extrapolation, so the critical path is
-// row 2's four evaluations instead of seven in sequence.  Every evaluation is
-// the sum of four quarter sums of the sources (warp_source_sum over quarter q,
-// added in q order), exactly as in k_encounter_cluster; the work is spread
-// over four rounds with one cluster barrier each: in round k row 2's rank r
-// sums quarter r of evaluation k, row 1's ranks sum quarters 2 (k mod 2) +
-// {0, 1} of evaluation k / 2 + 1, and row 0's rank sums quarter k of its
-// single evaluation.  Measured on a 2002-body disk with 150-190 encounter
-// bodies per step: two bodies per cluster (64-thread blocks) beat one, three
-// and four by 8-12%.  Results are bit for bit those of k_encounter_cluster
-// with rows = 3.
-constexpr int kRowCluster = 7;
-constexpr int kRowBodies = 2;
-__global__ void __cluster_dims__(kRowCluster, 1, 1) __launch_bounds__(32 * kRowBodies)
-    k_encounter_rows(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, double soft2) {
+
+// Encounter sub-step of the big systems (three Richardson rows, N = 1, 2, 4)
+// as a persistent task kernel.  The work of an encounter body is 28 quarter
+// sums: evaluations 0-3 of row 2 (N = 4 sub-steps), 0-1 of row 1 (N = 2) and
+// 0 of row 0 (N = 1), each over the four quarters of the sources
+// (warp_source_sum).  The rows are independent until the final
+// extrapolation, so the critical path is row 2's four evaluations.  Warps take
+// tasks from one atomic counter in units of one (row, evaluation) for every
+// body, in the order kEncOrder, where every unit follows the one it depends
+// on: a task's predecessors were all handed out before it, to warps that are
+// running, and a warp whose evaluation e > 0 is not yet published waits for
+// it (bounded; then it sets enc_head[1] and every warp stops).  The warp that
+// completes the fourth quarter of an evaluation (atomic count) adds the
+// quarter sums in quarter order, advances the row's modified midpoint
+// (MidRow) and publishes its state; the warp that completes the last row
+// combines the three rows (Richardson) and clears the body's counters for the
+// next step.  The sums and their order are those of the sequential scheme
+// with quarter sums (k_encounter_cluster with rows = 3 gives the same bits).
+// Measured on the 2002-body disk (~190 encounter bodies per step): 138 us per
+// step against 155 us for a cluster of 7 blocks per two bodies running the
+// rows side by side with one cluster barrier per evaluation round; two blocks
+// of four warps per SM (one or three or four: slower, more warps lengthen
+// every task on the shared FP64 unit); the waits poll with the whole warp
+// (a wait by lane 0 alone, the other lanes parked in a shuffle, slowed the
+// working warps of the SM 2-3 times).
+constexpr int kEncTaskWarps = 4;       // warps per block
+constexpr int kEncSpin = 1 << 20;      // polls of a dependency wait in a step (about two seconds)
+constexpr int kEncBlocksPerSM = 2;     // more warps lengthen every task on the shared FP64 unit
+// Hand-out order of the seven (row, evaluation) units of 4 x count tasks, 4
+// bits each (row | e << 2), every unit after the unit it depends on: the
+// critical row 2 first, the other rows' units as filler between its
+// evaluations.
+constexpr unsigned enc_unit(int row, int e) { return (unsigned)(row | e << 2); }
+constexpr unsigned kEncOrder = enc_unit(2, 0) | enc_unit(1, 0) << 4 | enc_unit(2, 1) << 8 | enc_unit(0, 0) << 12 |
+                               enc_unit(2, 2) << 16 | enc_unit(1, 1) << 20 | enc_unit(2, 3) << 24;
+__device__ __forceinline__ int enc_slot(int row, int e) { return row == 2 ? e : (row == 1 ? 4 + e : 6); }
+
+// The whole warp polls *flag >= want (one load of the same address; the
+// lanes stay converged, so no lane waits in a warp-synchronous instruction
+// while another polls); bounded, and it stops early when another warp gave
+// up (the shared give-up flag is read every 64th poll).  The sleep between
+// polls doubles from 128 ns to 2 us.  False when the wait gave up.
+__device__ __forceinline__ bool enc_wait(const int* flag, int want, int* err, int spin) {
+  unsigned ns = 128;
+  for (int it = 0; it < spin; it++) {
+    if (__all_sync(0xffffffffu, *(volatile const int*)flag >= want)) {
+      __threadfence();
+      return true;
+    }
+    if ((it & 63) == 63 && __any_sync(0xffffffffu, *(volatile const int*)err != 0)) return false;
+    __nanosleep(ns);
+    ns = ns < 2048 ? 2 * ns : ns;
+  }
+  if ((threadIdx.x & 31) == 0) atomicExch(err, 1);
+  return false;
+}
+
+__global__ void __launch_bounds__(32 * kEncTaskWarps)
+    k_encounter_tasks(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, double soft2,
+                      int spin) {
   griddep_enter();
-  namespace cg = cooperative_groups;
-  __shared__ double slot[2][kRowBodies][4];  // quarter sum of each warp, by round parity
-  __shared__ double res[kRowBodies][8];      // final position and velocity of row 0 (rank 6) or row 1 (rank 4)
-  cg::cluster_group cl = cg::this_cluster();
-  const int rank = (int)cl.block_rank();
-  const int w = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
-  const int row = rank < 4 ? 2 : (rank < 6 ? 1 : 0);
-  const int cid = blockIdx.x / kRowCluster, ncl = gridDim.x / kRowCluster;
+  const int lane = (int)(threadIdx.x & 31);
   const int count = D.ce_count[1];
-  int parity = 0;
-  // every warp of the cluster runs the same number of iterations and barriers
-  for (int base = cid * kRowBodies; base < count; base += ncl * kRowBodies) {
-    const int k = base + w;
-    const bool active = k < count;
-    const int j = active ? D.ce_list_big[k] : 0;
+  const int total = 28 * count;
+  int* err = D.enc_head + 1;
+  for (;;) {
+    int t = 0;
+    if (lane == 0) t = atomicAdd(D.enc_head, 1);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= total || *(volatile const int*)err) break;
+    // seven units of 4 count tasks, (row, evaluation) in hand-out order
+    const int unit = t / (4 * count), u = t - unit * 4 * count;
+    const int k = u >> 2, q = u & 3;
+    const int row = (kEncOrder >> (4 * unit)) & 3, e = (kEncOrder >> (4 * unit + 2)) & 3;
+    const int j = D.ce_list_big[k];
     const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
     const int self = self_index(j - b0, compat_block);
-    const PV c = {load3(D.x, n, j), load3(D.v, n, j)};
+    int* cnt = D.enc_cnt + 11 * (size_t)k;
+    double* st = D.enc_st + 27 * (size_t)k + 9 * row;
+    const int N = 1 << row, slot = enc_slot(row, e);
     MidRow m;
-    m.start(c, dt, 1 << row);
-    d3 q[4];
-    for (int round = 0; round < 4; round++) {
-      const int quarter = row == 2 ? rank : (row == 1 ? 2 * (round & 1) + (rank - 4) : round);
-      const int c0 = (int)((int64_t)quarter * nm / 4), c1 = (int)((int64_t)(quarter + 1) * nm / 4);
-      d3 S = {0.0, 0.0, 0.0};
-      if (active) S = warp_source_sum(D, rc_in, b0, c0, c1, self, m.z1, soft2);
-      const int buf = parity & 1;
+    if (e == 0) {
+      m.start(PV{load3(D.x, n, j), load3(D.v, n, j)}, dt, N);
+    } else {
+      if (!enc_wait(cnt + 7 + row, e, err, spin)) break;
+      m.N = N;
+      m.h = dt * inv_pow2(N);
+      m.h2 = 2.0 * m.h;
+      m.done = e;
+      m.z0 = {__ldcg(st), __ldcg(st + 1), __ldcg(st + 2)};
+      m.z1 = {__ldcg(st + 3), __ldcg(st + 4), __ldcg(st + 5)};
+      m.vel = {__ldcg(st + 6), __ldcg(st + 7), __ldcg(st + 8)};
+    }
+    const int c0 = (int)((int64_t)q * nm / 4), c1 = (int)((int64_t)(q + 1) * nm / 4);
+    const d3 S = warp_source_sum(D, rc_in, b0, c0, c1, self, m.z1, soft2);
+    double* qs = D.enc_q + 84 * (size_t)k + 12 * slot;
+    int last = 0;
+    if (lane == 0) {
+      qs[3 * q] = S.x;
+      qs[3 * q + 1] = S.y;
+      qs[3 * q + 2] = S.z;
+      __threadfence();
+      last = atomicAdd(cnt + slot, 1) == 3;
+    }
+    if (!__shfl_sync(0xffffffffu, last, 0)) continue;
+    __threadfence();
+    // fourth quarter: finish evaluation e of the row
+    d3 acc = {0.0, 0.0, 0.0};
+    for (int r = 0; r < 4; r++) {
+      acc.x += __ldcg(qs + 3 * r);
+      acc.y += __ldcg(qs + 3 * r + 1);
+      acc.z += __ldcg(qs + 3 * r + 2);
+    }
+    m.finish_eval(D.u, acc, soft2);
+    if (m.done < N) {
       if (lane == 0) {
-        slot[buf][w][0] = S.x;
-        slot[buf][w][1] = S.y;
-        slot[buf][w][2] = S.z;
+        st[0] = m.z0.x;
+        st[1] = m.z0.y;
+        st[2] = m.z0.z;
+        st[3] = m.z1.x;
+        st[4] = m.z1.y;
+        st[5] = m.z1.z;
+        st[6] = m.vel.x;
+        st[7] = m.vel.y;
+        st[8] = m.vel.z;
+        __threadfence();
+        atomicExch(cnt + 7 + row, e + 1);
       }
-      cl.sync();
-      parity++;
-      if (row == 2) {
-        d3 acc = {0.0, 0.0, 0.0};
-        for (int r = 0; r < 4; r++) {
-          const double* rs = cl.map_shared_rank(&slot[buf][w][0], r);
-          acc.x += rs[0];
-          acc.y += rs[1];
-          acc.z += rs[2];
-        }
-        m.finish_eval(D.u, acc, soft2);
-      } else {
-        if (row == 1) {
-          const double* ra = cl.map_shared_rank(&slot[buf][w][0], 4);
-          const double* rb = cl.map_shared_rank(&slot[buf][w][0], 5);
-          q[2 * (round & 1)] = {ra[0], ra[1], ra[2]};
-          q[2 * (round & 1) + 1] = {rb[0], rb[1], rb[2]};
-        } else {
-          q[round] = S;
-        }
-        if ((row == 1 && (round & 1)) || round == 3) {
-          d3 acc = {0.0, 0.0, 0.0};
-          for (int r = 0; r < 4; r++) {
-            acc.x += q[r].x;
-            acc.y += q[r].y;
-            acc.z += q[r].z;
-          }
-          m.finish_eval(D.u, acc, soft2);
-        }
-      }
+      continue;
     }
     const PV mine = m.result();
-    if ((rank == 4 || rank == 6) && lane == 0) {
-      res[w][0] = mine.pos.x;
-      res[w][1] = mine.pos.y;
-      res[w][2] = mine.pos.z;
-      res[w][3] = mine.vel.x;
-      res[w][4] = mine.vel.y;
-      res[w][5] = mine.vel.z;
+    double* res = D.enc_res + 18 * (size_t)k;
+    int fin = 0;
+    if (lane == 0) {
+      double* rs = res + 6 * row;
+      rs[0] = mine.pos.x;
+      rs[1] = mine.pos.y;
+      rs[2] = mine.pos.z;
+      rs[3] = mine.vel.x;
+      rs[4] = mine.vel.y;
+      rs[5] = mine.vel.z;
+      __threadfence();
+      fin = atomicAdd(cnt + 10, 1) == 2;
     }
-    cl.sync();
-    if (rank == 0 && lane == 0 && active) {
-      const double* r0 = cl.map_shared_rank(&res[w][0], 6);
-      const double* r1 = cl.map_shared_rank(&res[w][0], 4);
-      const PV b00 = {{r0[0], r0[1], r0[2]}, {r0[3], r0[4], r0[5]}};
-      const PV b10 = {{r1[0], r1[1], r1[2]}, {r1[3], r1[4], r1[5]}};
+    if (!__shfl_sync(0xffffffffu, fin, 0)) continue;
+    __threadfence();
+    if (lane == 0) {
+      PV b[3];
+      for (int r = 0; r < 3; r++) {
+        const double* rs = res + 6 * r;
+        b[r] = {{__ldcg(rs), __ldcg(rs + 1), __ldcg(rs + 2)}, {__ldcg(rs + 3), __ldcg(rs + 4), __ldcg(rs + 5)}};
+      }
       PV b11, b21, b22;
-      rich_combine(b11, b10, b00, 4.0);
-      rich_combine(b21, mine, b10, 4.0);
+      rich_combine(b11, b[1], b[0], 4.0);
+      rich_combine(b21, b[2], b[1], 4.0);
       rich_combine(b22, b21, b11, 16.0);
       store3(D.xo, n, j, b22.pos);
       store3(D.vo, n, j, b22.vel);
     }
+    if (lane < 11) cnt[lane] = 0;  // every task of this body is done
   }
-  cl.sync();  // no block leaves while another may still read its slots
 }
 
 // ---------------------------------------------------------------------------

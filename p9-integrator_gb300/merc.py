@@ -134,6 +134,7 @@ def lib() -> C.CDLL:
     L.merc_diag_kick_ms.argtypes = [vp, _f64p, _i32p]
     L.merc_diag_far_recomputes.argtypes = [vp, C.POINTER(C.c_int64)]
     L.merc_diag_pdl.argtypes = [vp, C.c_int]
+    L.merc_diag_encounter_wait.argtypes = [vp, C.POINTER(C.c_int32)]
     _LIB = L
     return L
 
@@ -350,6 +351,14 @@ class Integrator:
         c = C.c_int64()
         self._check(self.L.merc_diag_far_recomputes(self.h, C.byref(c)))
         return c.value
+
+    def encounter_wait_check(self) -> bool:
+        """Runs the encounter task kernel with a dependency that is never
+        published and a short wait limit; True when the kernel reported that
+        the wait gave up (merc_diag_encounter_wait)."""
+        g = C.c_int32()
+        self._check(self.L.merc_diag_encounter_wait(self.h, C.byref(g)))
+        return bool(g.value)
 
 
 MLP_BLOB = 1267

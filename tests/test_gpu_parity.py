@@ -253,6 +253,29 @@ def test_programmatic_launches_do_not_change_results():
         assert np.array_equal(out[0][2], out[1][2])
 
 
+def test_encounter_wait_limit_is_reported_and_leaves_the_state_alone():
+    """A bounded wait of the encounter task kernel that runs out (its
+    predecessor's tasks skipped) is reported, and the integration continues
+    with the same bits as without the check."""
+    sysm = systems.embryo_disk(seed=11, n_embryos=300)
+    kw = dict(dt=sysm.dt, hill_factor=sysm.hill_factor, drift=merc.DRIFT_UNIVERSAL)
+    out = []
+    for check in (True, False):
+        g = merc.Integrator(merc.default_params(**kw))
+        g.load_systems(sysm)
+        g.step(3)
+        if check:
+            assert g.encounter_wait_check()
+        g.step(9)
+        st = g.state()
+        out.append((st.pos, st.vel, st.flags, g.stats().ce_body_steps))
+        g.close()
+    assert out[0][3] > 0
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2], out[1][2])
+
+
 @pytest.mark.parametrize("steps", [20])
 def test_large_small_system_parity(oracle, steps):
     """A batch of small systems whose largest system does not fit in one
