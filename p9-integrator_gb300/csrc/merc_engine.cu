@@ -281,7 +281,7 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
   {
     // encounter task kernel state (every body of a big system may be listed)
     const size_t ne = ctx->has_big ? (size_t)n : 1;
-    if ((st = dalloc(ctx, &D.enc_q, 84 * ne)) || (st = dalloc(ctx, &D.enc_st, 27 * ne)) ||
+    if ((st = dalloc(ctx, &D.enc_q, kEncQ * ne)) || (st = dalloc(ctx, &D.enc_st, 27 * ne)) ||
         (st = dalloc(ctx, &D.enc_res, 18 * ne)) || (st = dalloc(ctx, &D.enc_cnt, 11 * ne)) ||
         (st = dalloc(ctx, &D.enc_head, 2)))
       return st;
@@ -1862,7 +1862,7 @@ int merc_diag_encounter_wait(merc_ctx* ctx, int32_t* gave_up) {
     }
   // one listed body; tasks start at the second unit (the first unit, row 2's
   // evaluation 0 of every listed body, is skipped)
-  const int one = 1, head[2] = {4, 0};
+  const int one = 1, head[2] = {kEncParts, 0};
   CK(cudaMemcpy(D.ce_list_big, &body, sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(D.ce_count + 1, &one, sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(D.enc_head, head, sizeof head, cudaMemcpyHostToDevice));

@@ -70,7 +70,7 @@ struct Dev {
   unsigned long long* counters = nullptr;  // kNumCounters: CE body-steps, Kepler iterations, solves,
                                            // non-converged, iterations executed per warp (SIMT)
   // encounter task kernel, per entry of the big-system encounter list:
-  double* enc_q = nullptr;    // 84: quarter sums of the 7 evaluations (4 x 3 each)
+  double* enc_q = nullptr;    // 84: quarter sums of the 7 evaluations (kEncParts x 3 each)
   double* enc_st = nullptr;   // 27: per row z0, z1, vel after its last published evaluation
   double* enc_res = nullptr;  // 18: per row the sub-step result (position, velocity)
   int* enc_cnt = nullptr;     // 11: quarters done per evaluation (7), evaluations published per row (3),
@@ -1465,6 +1465,10 @@ struct MidRow {
 constexpr int kEncTaskWarps = 4;       // warps per block
 constexpr int kEncSpin = 1 << 20;      // polls of a dependency wait in a step (about two seconds)
 constexpr int kEncBlocksPerSM = 2;     // more warps lengthen every task on the shared FP64 unit
+// parts of the sources per evaluation, one task each (6, 8 and 16 parts:
+// the per-task overheads outweigh the shorter tasks)
+constexpr int kEncParts = 4;
+constexpr int kEncQ = 7 * 3 * kEncParts;  // part sums per encounter body
 // Hand-out order of the seven (row, evaluation) units of 4 x count tasks, 4
 // bits each (row | e << 2), every unit after the unit it depends on: the
 // critical row 2 first, the other rows' units as filler between its
@@ -1500,7 +1504,7 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
   griddep_enter();
   const int lane = (int)(threadIdx.x & 31);
   const int count = D.ce_count[1];
-  const int total = 28 * count;
+  const int total = 7 * kEncParts * count;
   int* err = D.enc_head + 1;
   for (;;) {
     int t = 0;
@@ -1508,8 +1512,8 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= total || *(volatile const int*)err) break;
     // seven units of 4 count tasks, (row, evaluation) in hand-out order
-    const int unit = t / (4 * count), u = t - unit * 4 * count;
-    const int k = u >> 2, q = u & 3;
+    const int unit = t / (kEncParts * count), u = t - unit * kEncParts * count;
+    const int k = u / kEncParts, q = u % kEncParts;
     const int row = (kEncOrder >> (4 * unit)) & 3, e = (kEncOrder >> (4 * unit + 2)) & 3;
     const int j = D.ce_list_big[k];
     const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
@@ -1530,22 +1534,22 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
       m.z1 = {__ldcg(st + 3), __ldcg(st + 4), __ldcg(st + 5)};
       m.vel = {__ldcg(st + 6), __ldcg(st + 7), __ldcg(st + 8)};
     }
-    const int c0 = (int)((int64_t)q * nm / 4), c1 = (int)((int64_t)(q + 1) * nm / 4);
+    const int c0 = (int)((int64_t)q * nm / kEncParts), c1 = (int)((int64_t)(q + 1) * nm / kEncParts);
     const d3 S = warp_source_sum(D, rc_in, b0, c0, c1, self, m.z1, soft2);
-    double* qs = D.enc_q + 84 * (size_t)k + 12 * slot;
+    double* qs = D.enc_q + kEncQ * (size_t)k + 3 * kEncParts * slot;
     int last = 0;
     if (lane == 0) {
       qs[3 * q] = S.x;
       qs[3 * q + 1] = S.y;
       qs[3 * q + 2] = S.z;
       __threadfence();
-      last = atomicAdd(cnt + slot, 1) == 3;
+      last = atomicAdd(cnt + slot, 1) == kEncParts - 1;
     }
     if (!__shfl_sync(0xffffffffu, last, 0)) continue;
     __threadfence();
     // fourth quarter: finish evaluation e of the row
     d3 acc = {0.0, 0.0, 0.0};
-    for (int r = 0; r < 4; r++) {
+    for (int r = 0; r < kEncParts; r++) {
       acc.x += __ldcg(qs + 3 * r);
       acc.y += __ldcg(qs + 3 * r + 1);
       acc.z += __ldcg(qs + 3 * r + 2);
