@@ -1469,8 +1469,8 @@ constexpr int kEncBlocksPerSM = 2;     // more warps lengthen every task on the 
 // the per-task overheads outweigh the shorter tasks)
 constexpr int kEncParts = 4;
 constexpr int kEncQ = 7 * 3 * kEncParts;  // part sums per encounter body
-// Hand-out order of the seven (row, evaluation) units of 4 x count tasks, 4
-// bits each (row | e << 2), every unit after the unit it depends on: the
+// Hand-out order of the seven (row, evaluation) units of kEncParts x count
+// tasks, 4 bits each (row | e << 2), every unit after the unit it depends on: the
 // critical row 2 first, the other rows' units as filler between its
 // evaluations.
 constexpr unsigned enc_unit(int row, int e) { return (unsigned)(row | e << 2); }
@@ -1511,7 +1511,7 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
     if (lane == 0) t = atomicAdd(D.enc_head, 1);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= total || *(volatile const int*)err) break;
-    // seven units of 4 count tasks, (row, evaluation) in hand-out order
+    // seven units of kEncParts x count tasks, (row, evaluation) in hand-out order
     const int unit = t / (kEncParts * count), u = t - unit * kEncParts * count;
     const int k = u / kEncParts, q = u % kEncParts;
     const int row = (kEncOrder >> (4 * unit)) & 3, e = (kEncOrder >> (4 * unit + 2)) & 3;
@@ -1547,7 +1547,7 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
     }
     if (!__shfl_sync(0xffffffffu, last, 0)) continue;
     __threadfence();
-    // fourth quarter: finish evaluation e of the row
+    // last part: finish evaluation e of the row
     d3 acc = {0.0, 0.0, 0.0};
     for (int r = 0; r < kEncParts; r++) {
       acc.x += __ldcg(qs + 3 * r);
