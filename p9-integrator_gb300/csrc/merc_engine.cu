@@ -447,8 +447,12 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       nk++;
     };
     auto reduce = [&](const double* rc_in, const int* gate, double* rc_out, int last, int massive_only, int check) {
-      launch(k_kick_reduce_sym, nred, kThreads, D, rc_in, gate, rc_out, hdt, p.softening2, p.hill_factor, ej2,
-             last, massive_only, check);
+      if (D.nsys == 1)
+        launch(k_kick_reduce_sym<true>, nred, kThreads, D, rc_in, gate, rc_out, hdt, p.softening2, p.hill_factor,
+               ej2, last, massive_only, check);
+      else
+        launch(k_kick_reduce_sym<false>, nred, kThreads, D, rc_in, gate, rc_out, hdt, p.softening2, p.hill_factor,
+               ej2, last, massive_only, check);
       nk++;
     };
     // far-field pass of the massive bodies (timed as the kick kernel)

@@ -120,14 +120,17 @@ __device__ __forceinline__ int far_threshold(double rc, const d3& x, double hc) 
   return rc2_threshold(R > rc ? R : rc);
 }
 
-// r_crit table entries of massive body j; hc = cbrt(m_j / 3) * hill_factor
-__device__ __forceinline__ void write_rc(double* rc, int n, int j, const d3& x, const d3& v, double hc) {
+// r_crit table entries of massive body j; hc = cbrt(m_j / 3) * hill_factor;
+// returns the far-field threshold it wrote
+__device__ __forceinline__ int write_rc(double* rc, int n, int j, const d3& x, const d3& v, double hc) {
   double r = rcrit_hc(x, v, hc);
   rc[4 * (size_t)j] = r;
   rc[4 * (size_t)j + 1] = 0.1 * r;
   rc[4 * (size_t)j + 2] = 0.9 * r;
   rc[4 * (size_t)j + 3] = thr_pack(rc2_threshold(r));
-  rc_far_thr(rc, n)[j] = far_threshold(r, x, hc);
+  const int far = far_threshold(r, x, hc);
+  rc_far_thr(rc, n)[j] = far;
+  return far;
 }
 
 __device__ __forceinline__ F4 load_f4(const Dev& D, int g) {
@@ -413,6 +416,11 @@ __global__ void __cluster_dims__(kJumpCluster, 1, 1) __launch_bounds__(kJumpThre
   }
   const int n = D.n, nm = D.nm[0];
   const double* vv = vsrc ? vsrc : D.v;
+  // this thread's body, loaded before the momentum (it does not depend on it)
+  const bool mine = j < n;
+  const d3 x0 = mine ? load3(xsrc, n, j) : d3{0.0, 0.0, 0.0};
+  const d3 v = mine ? load3(vv, n, j) : d3{0.0, 0.0, 0.0};
+  const double hc_j = (mine && j < nm) ? D.hc[j] : 0.0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int i0 = (int)((int64_t)rank * nm / kJumpCluster), i1 = (int)((int64_t)(rank + 1) * nm / kJumpCluster);
   double px = 0.0, py = 0.0, pz = 0.0;
@@ -467,24 +475,15 @@ __global__ void __cluster_dims__(kJumpCluster, 1, 1) __launch_bounds__(kJumpThre
     Pz += q[2];
   }
   cl.sync();  // no block leaves while another may still read its partial
-  if (j >= n) return;
+  if (!mine) return;
   if (CLEAR) D.ce[j] = 0;
-  d3 x = load3(xsrc, n, j);
-  x.x = fma(Px, hdt, x.x);
-  x.y = fma(Py, hdt, x.y);
-  x.z = fma(Pz, hdt, x.z);
+  const d3 x = {fma(Px, hdt, x0.x), fma(Py, hdt, x0.y), fma(Pz, hdt, x0.z)};
   store3(D.x, n, j, x);
   D.xf[j] = f32_trunc(x.x);
   D.xf[n + j] = f32_trunc(x.y);
   D.xf[2 * n + j] = f32_trunc(x.z);
-  d3 v;
-  if (vsrc) {
-    v = load3(vsrc, n, j);
-    store3(D.v, n, j, v);
-  } else {
-    v = load3(D.v, n, j);
-  }
-  if (j < nm) write_rc(rc_out, n, j, x, v, D.hc[j]);
+  if (vsrc) store3(D.v, n, j, v);
+  if (j < nm) write_rc(rc_out, n, j, x, v, hc_j);
 }
 
 // Sets body j's encounter flag (one byte of D.ce, by an atomic OR on its
@@ -921,6 +920,7 @@ constexpr int kRedBatch = MERC_RED_BATCH;  // partials loaded per thread before 
 // depend on scheduling.  check: after writing rc_out, set *D.gate if a massive body's
 // far-field threshold in rc_out differs from the one in rc (the far field of
 // the next kick must then be recomputed).
+template <bool ONE>
 __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const int* __restrict__ gate,
                                   double* __restrict__ rc_out, double hdt, double soft2, double hill,
                                   double eject_r2, int last, int massive_only, int check) {
@@ -929,10 +929,17 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   const int j = t / kRedThreads, sub = t % kRedThreads;
   const bool valid = j < D.n;
   const int n = D.n;
-  const int s = valid ? D.sys[j] : 0;
-  bool work = valid && D.big[s];
-  const int b0 = work ? D.off[s] : 0, nm = work ? D.nm[s] : 0, local = j - b0;
+  // ONE: a single system, big (no per-body system lookups)
+  const int s = ONE ? 0 : (valid ? D.sys[j] : 0);
+  bool work = valid && (ONE || D.big[s]);
+  const int b0 = (ONE || !work) ? 0 : D.off[s], nm = work ? D.nm[s] : 0, local = j - b0;
   const bool massive = work && local < nm;
+  // the epilogue's inputs, loaded before the sums (they do not depend on them)
+  const bool lead = work && sub == 0;
+  const double hc_j = (lead && rc_out && massive) ? D.hc[j] : 0.0;
+  const uint32_t flags_j = (lead && last) ? D.flags[j] : 0u;
+  const bool ce_j = (lead && last) ? D.ce[j] != 0 : false;
+  const int thr_j = (lead && check && massive) ? rc_far_thr_c(rc, n)[j] : 0;
   int count = 0;
   const double* base = nullptr;
   const uint32_t* mask = nullptr;
@@ -1022,8 +1029,21 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   vel.x = fma(acc.x, hdt, vel.x);
   vel.y = fma(acc.y, hdt, vel.y);
   vel.z = fma(acc.z, hdt, vel.z);
-  kick_epilogue(D, j, local, nm, pos, vel, rc_out, hill, eject_r2, last);
-  if (check && massive && rc_far_thr_c(rc_out, n)[j] != rc_far_thr_c(rc, n)[j]) atomicOr(D.gate, 1);
+  // kick_epilogue with the prefetched inputs
+  store3(D.v, n, j, vel);
+  if (rc_out && massive) {
+    const int far = write_rc(rc_out, n, j, pos, vel, hc_j);
+    if (check && far != thr_j) atomicOr(D.gate, 1);
+  }
+  if (last) {
+    uint32_t f = flags_j & ~MERC_FLAG_CE_LAST;
+    if (ce_j) f |= MERC_FLAG_CE_LAST | MERC_FLAG_CE_EVER;
+    if (eject_r2 > 0.0 && mag2(pos) > eject_r2) f |= MERC_FLAG_EJECTED;
+    bool fin = mm::isfinite_(pos.x) && mm::isfinite_(pos.y) && mm::isfinite_(pos.z) && mm::isfinite_(vel.x) &&
+               mm::isfinite_(vel.y) && mm::isfinite_(vel.z);
+    if (!fin) f |= MERC_FLAG_NONFINITE;
+    D.flags[j] = f;
+  }
 }
 
 // Tiled encounter test of the big systems: any source of the chunk within
