@@ -1483,7 +1483,8 @@ struct MidRow {
 // (a wait by lane 0 alone, the other lanes parked in a shuffle, slowed the
 // working warps of the SM 2-3 times).
 constexpr int kEncTaskWarps = 4;       // warps per block
-constexpr int kEncSpin = 1 << 20;      // polls of a dependency wait in a step (about two seconds)
+constexpr unsigned kEncSleepMax = 256;  // longest sleep between polls, ns (2 us: waiters woke later)
+constexpr int kEncSpin = 1 << 22;      // polls of a dependency wait in a step (about two seconds)
 constexpr int kEncBlocksPerSM = 2;     // more warps lengthen every task on the shared FP64 unit
 // parts of the sources per evaluation, one task each (6, 8 and 16 parts:
 // the per-task overheads outweigh the shorter tasks)
@@ -1502,7 +1503,7 @@ __device__ __forceinline__ int enc_slot(int row, int e) { return row == 2 ? e : 
 // lanes stay converged, so no lane waits in a warp-synchronous instruction
 // while another polls); bounded, and it stops early when another warp gave
 // up (the shared give-up flag is read every 64th poll).  The sleep between
-// polls doubles from 128 ns to 2 us.  False when the wait gave up.
+// polls doubles from 128 ns to kEncSleepMax.  False when the wait gave up.
 __device__ __forceinline__ bool enc_wait(const int* flag, int want, int* err, int spin) {
   unsigned ns = 128;
   for (int it = 0; it < spin; it++) {
@@ -1512,7 +1513,7 @@ __device__ __forceinline__ bool enc_wait(const int* flag, int want, int* err, in
     }
     if ((it & 63) == 63 && __any_sync(0xffffffffu, *(volatile const int*)err != 0)) return false;
     __nanosleep(ns);
-    ns = ns < 2048 ? 2 * ns : ns;
+    ns = ns < kEncSleepMax ? 2 * ns : ns;
   }
   if ((threadIdx.x & 31) == 0) atomicExch(err, 1);
   return false;
