@@ -33,11 +33,23 @@ namespace {
 
 constexpr int kSweepMaxNm = kSmallNm;  // 32
 
+// A work item of the persistent kernel: the test particles [j0, j1) (indices
+// within system s) of one system.  A system with many test particles is split
+// into several items; every item integrates the system's massive bodies
+// itself (bit for bit the same in every item), and the primary item (one
+// per system) writes them back through the staging buffers.
+struct SweepItem {
+  int s, j0, j1, primary;
+};
+
 struct SweepArgs {
   Dev D;
-  const int* order;  // systems, largest first
-  int* queue;        // work counter (zeroed before the launch)
-  int nsys, nmax;    // systems, largest system size
+  const SweepItem* items;  // largest systems first
+  int* queue;              // work counter (zeroed before the launch)
+  int nitems, nmax;        // work items, largest system size
+  const int* moff;         // per system: first staging slot of its massive bodies
+  double* stage;           // 6 per massive body: final position and velocity
+  uint32_t* stage_f;       // final flags of each massive body
   int nh;            // largest massive count of the batch (history stride)
   int chunk;         // steps per history chunk
   int steps;
@@ -182,9 +194,10 @@ __global__ void k_sweep_persistent(SweepArgs A) {
     if (tid < kNumCounters) tally[tid] = 0ull;
     __syncthreads();
     const int slot = sys_slot;
-    if (slot >= A.nsys) break;
-    const int s = A.order[slot];
-    const int b0 = D.off[s], n = D.off[s + 1] - b0, nm = D.nm[s];
+    if (slot >= A.nitems) break;
+    const SweepItem item = A.items[slot];
+    const int s = item.s;
+    const int b0 = D.off[s], nm = D.nm[s];
     // massive bodies: lane i of warp 0 owns body i
     uint32_t fm = 0;
     if (warp == 0 && lane < nm) {
@@ -201,6 +214,8 @@ __global__ void k_sweep_persistent(SweepArgs A) {
     for (int c0 = 0; c0 < A.steps; c0 += C) {
       const int cn = min(C, A.steps - c0);
       // ---- the massive bodies through the chunk, recording the history ----
+      // (counted by the primary item only)
+      const unsigned long long sv_ce = my_ce, sv_it = my_it, sv_sol = my_sol, sv_nc = my_nc, sv_simt = my_simt;
       if (warp == 0) {
         const bool act = lane < nm;
         const int self = self_index(lane, A.compat_block);
@@ -299,9 +314,16 @@ __global__ void k_sweep_persistent(SweepArgs A) {
           if (act) fm = step_flags(fm, xm(), vm());
         }
       }
+      if (!item.primary) {
+        my_ce = sv_ce;
+        my_it = sv_it;
+        my_sol = sv_sol;
+        my_nc = sv_nc;
+        my_simt = sv_simt;
+      }
       __syncthreads();  // the history of the chunk is complete
       // ---- test particles through the chunk, each in registers ----
-      for (int j = nm + tid; j < n; j += T) {
+      for (int j = item.j0 + tid; j < item.j1; j += T) {
         const int g = b0 + j, self = self_index(j, A.compat_block);
         d3 pos = {D.x[g], D.x[D.n + g], D.x[2 * D.n + g]};
         d3 vel = {D.v[g], D.v[D.n + g], D.v[2 * D.n + g]};
@@ -367,15 +389,17 @@ __global__ void k_sweep_persistent(SweepArgs A) {
       }
       __syncthreads();  // before the next chunk overwrites the history
     }
-    // write the massive bodies back, and the radii the next call's first kick uses
-    if (warp == 0 && lane < nm) {
-      const int g = b0 + lane;
-      for (int c = 0; c < 3; c++) {
-        D.x[c * D.n + g] = XM[c * kSweepMaxNm + lane];
-        D.v[c * D.n + g] = VM[c * kSweepMaxNm + lane];
+    // the primary item stages the massive bodies (k_sweep_commit writes them
+    // back after the launch: other items of the system may still read the
+    // state they started from) and writes the radii the next call's first
+    // kick uses
+    if (item.primary && warp == 0 && lane < nm) {
+      const int g = b0 + lane, c = A.moff[s] + lane;
+      for (int k = 0; k < 3; k++) {
+        A.stage[6 * (size_t)c + k] = XM[k * kSweepMaxNm + lane];
+        A.stage[6 * (size_t)c + 3 + k] = VM[k * kSweepMaxNm + lane];
       }
-      D.flags[g] = fm;
-      D.ce[g] = (fm & MERC_FLAG_CE_LAST) ? 1 : 0;
+      A.stage_f[c] = fm;
       if (A.steps > 0) {
         const Hist h = hist_at(hist, nh, (A.steps - 1) % C);
         for (int k = 0; k < 4; k++) A.rc_final[4 * (size_t)g + k] = h.TN[4 * lane + k];
@@ -391,6 +415,22 @@ __global__ void k_sweep_persistent(SweepArgs A) {
     if (tid < kNumCounters && tally[tid]) atomicAdd(&D.counters[tid], tally[tid]);
     __syncthreads();
   }
+}
+
+// The staged massive bodies of a persistent launch back into the state
+// (massive body c is global body mbody[c]).
+__global__ void k_sweep_commit(Dev D, const int* __restrict__ mbody, const double* __restrict__ stage,
+                               const uint32_t* __restrict__ stage_f, int nmass) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nmass) return;
+  const int g = mbody[c];
+  for (int k = 0; k < 3; k++) {
+    D.x[k * (size_t)D.n + g] = stage[6 * (size_t)c + k];
+    D.v[k * (size_t)D.n + g] = stage[6 * (size_t)c + 3 + k];
+  }
+  const uint32_t f = stage_f[c];
+  D.flags[g] = f;
+  D.ce[g] = (f & MERC_FLAG_CE_LAST) ? 1 : 0;
 }
 
 }  // namespace

@@ -159,11 +159,17 @@ def test_errors_are_reported_not_crashed():
     g.close()
 
 
-def test_persistent_sweep_kernel_equals_per_phase_kernels():
+@pytest.mark.parametrize("shape", ["many_small", "few_large"])
+def test_persistent_sweep_kernel_equals_per_phase_kernels(shape):
     """Small systems run in the persistent kernel (work queue, merged half
     kicks); with the drift log on they run in the per-phase kernels.  Both give
-    the same bits."""
-    sysm = systems.sweep(n_systems=320, nt_lo=8, nt_hi=120, seed=31)  # more systems than SMs
+    the same bits: many systems (more than SMs, some cut into two items) and a
+    few systems with thousands of test particles (each cut into many items that
+    integrate the massive bodies alike, the primary one writing them back)."""
+    if shape == "many_small":
+        sysm = systems.sweep(n_systems=320, nt_lo=8, nt_hi=120, seed=31)
+    else:
+        sysm = systems.sweep(n_systems=3, nt_lo=3000, nt_hi=6000, seed=32)
     kw = dict(dt=sysm.dt, hill_factor=3.0, drift=merc.DRIFT_UNIVERSAL)
     a = merc.Integrator(merc.default_params(**kw))
     a.load_systems(sysm)
