@@ -691,7 +691,7 @@ int sweep_nh(const merc_ctx* ctx) {
 }
 
 size_t sweep_smem_bytes(const merc_ctx* ctx) {
-  size_t b = 8 * hist_step_doubles(sweep_nh(ctx)) * kSweepChunk;
+  size_t b = 2 * 8 * hist_step_doubles(sweep_nh(ctx)) * kSweepChunk;  // two history buffers
   if (ctx->p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) b += 4 * (size_t)kBlob;
   return b;
 }

@@ -128,15 +128,18 @@ struct SmemVelTotal {  // encounter sub-step velocity update, sources in shared 
   }
 };
 
-__global__ void k_sweep_persistent(SweepArgs A) {
+// (at most 128 registers: the tuner's 128-thread blocks keep 4 blocks per SM;
+// 133 registers without the bound cost more than the few spills)
+__global__ void __launch_bounds__(256, 2) k_sweep_persistent(SweepArgs A) {
   extern __shared__ double sm[];
   const int nh = A.nh, C = A.chunk;
-  double* hist = sm;                                           // C steps of history
-  float* blob = (float*)(sm + hist_step_doubles(nh) * C);      // kBlob floats when warm start is on
+  double* hist = sm;                                           // 2 x C steps of history (double-buffered)
+  float* blob = (float*)(sm + 2 * hist_step_doubles(nh) * C);  // kBlob floats when warm start is on
+  auto hist_buf = [&](int b) { return hist + (size_t)b * hist_step_doubles(nh) * C; };
   __shared__ double M[kSweepMaxNm], HC[kSweepMaxNm];           // masses, cbrt(m / 3) * hill
   __shared__ double XM[3 * kSweepMaxNm], VM[3 * kSweepMaxNm];  // massive state
   __shared__ double X0[3 * kSweepMaxNm], T0[4 * kSweepMaxNm];  // positions and table of the call's first kick
-  __shared__ int sys_slot;
+  __shared__ int sys_slot, tp_next;
   __shared__ unsigned long long tally[kNumCounters];  // as Dev::counters
 
   const Dev& D = A.D;
@@ -211,10 +214,10 @@ __global__ void k_sweep_persistent(SweepArgs A) {
       fm = D.flags[g];
     }
     __syncwarp();
-    for (int c0 = 0; c0 < A.steps; c0 += C) {
+    // ---- warp 0: the massive bodies through the chunk of steps c0.., recording
+    // the history into hb (counted by the primary item only) ----
+    auto massive_chunk = [&](int c0, double* hb) {
       const int cn = min(C, A.steps - c0);
-      // ---- the massive bodies through the chunk, recording the history ----
-      // (counted by the primary item only)
       const unsigned long long sv_ce = my_ce, sv_it = my_it, sv_sol = my_sol, sv_nc = my_nc, sv_simt = my_simt;
       if (warp == 0) {
         const bool act = lane < nm;
@@ -285,7 +288,7 @@ __global__ void k_sweep_persistent(SweepArgs A) {
         }
         for (int k = 0; k < cn; k++) {
           const bool last = c0 + k == A.steps - 1;
-          Hist h = hist_at(hist, nh, k);
+          Hist h = hist_at(hb, nh, k);
           momentum(h.P1);
           jump(h.P1);
           record(h.X1, h.T1);
@@ -321,73 +324,92 @@ __global__ void k_sweep_persistent(SweepArgs A) {
         my_nc = sv_nc;
         my_simt = sv_simt;
       }
-      __syncthreads();  // the history of the chunk is complete
-      // ---- test particles through the chunk, each in registers ----
-      for (int j = item.j0 + tid; j < item.j1; j += T) {
-        const int g = b0 + j, self = self_index(j, A.compat_block);
-        d3 pos = {D.x[g], D.x[D.n + g], D.x[2 * D.n + g]};
-        d3 vel = {D.v[g], D.v[D.n + g], D.v[2 * D.n + g]};
-        uint32_t f = D.flags[g];
-        if (c0 == 0) {  // the call's first half kick
-          const d3 a = kick_sum(pos, self, X0, T0, nm);
-          vel.x = fma(a.x, hdt, vel.x);
-          vel.y = fma(a.y, hdt, vel.y);
-          vel.z = fma(a.z, hdt, vel.z);
-        }
-        for (int k = 0; k < cn; k++) {
-          const bool last = c0 + k == A.steps - 1;
-          const Hist h = hist_at(hist, nh, k);
-          pos.x = fma(h.P1[0], hdt, pos.x);
-          pos.y = fma(h.P1[1], hdt, pos.y);
-          pos.z = fma(h.P1[2], hdt, pos.z);
-          bool ce;
-          drift(pos, vel, self, h, nm, ce);
-          f &= ~MERC_FLAG_CE_LAST;
-          if (ce) f |= MERC_FLAG_CE_LAST | MERC_FLAG_CE_EVER;
-          pos.x = fma(h.P2[0], hdt, pos.x);
-          pos.y = fma(h.P2[1], hdt, pos.y);
-          pos.z = fma(h.P2[2], hdt, pos.z);
-          // the second half kick of this step and (unless this is the last
-          // step of the call) the first of the next, in one pass
-          d3 accB = {0.0, 0.0, 0.0}, accA = {0.0, 0.0, 0.0};
-          for (int i = 0; i < nm; i++) {
-            const FastSrc SB = smem_src(h.X2, M, h.T2, nh, i);
-            const int thrA = thr_unpack(h.TN[4 * i + 3]);
-            const double dx = fsub(D.u, SB.x, pos.x), dy = fsub(D.u, SB.y, pos.y), dz = fsub(D.u, SB.z, pos.z);
-            const double r2 = fma(dx, dx, fma(dy, dy, fmul(D.u, dz, dz)));
-            if (!last && hi_word(r2) > max(SB.rc2_hi, thrA) && i != self && seed_in_range(r2)) {
-              const double w = fmul(D.u, SB.m, inv_softened_r3(D.u, r2, fadd(D.u, r2, A.soft2)));
-              accB.x = fma(w, dx, accB.x);
-              accB.y = fma(w, dy, accB.y);
-              accB.z = fma(w, dz, accB.z);
-              accA.x = fma(w, dx, accA.x);
-              accA.y = fma(w, dy, accA.y);
-              accA.z = fma(w, dz, accA.z);
-            } else {
-              pair_fast<false>(D.u, pos, self, i, SB, A.soft2, accB);
-              if (!last) pair_fast<false>(D.u, pos, self, i, smem_src(h.X2, M, h.TN, nh, i), A.soft2, accA);
+    };
+    if (A.steps > 0) massive_chunk(0, hist_buf(0));
+    for (int c0 = 0, ci = 0; c0 < A.steps; c0 += C, ci++) {
+      const int cn = min(C, A.steps - c0);
+      double* cur = hist_buf(ci & 1);
+      if (tid == 0) tp_next = 0;
+      __syncthreads();  // the chunk's history is complete, the other buffer free
+      // warp 0 runs one chunk ahead: the next chunk's history into the other
+      // buffer, then it joins the test particles of this chunk
+      if (c0 + C < A.steps) massive_chunk(c0 + C, hist_buf((ci + 1) & 1));
+      // ---- test particles through the chunk, each in registers; warps take
+      // 32 at a time from the block's counter ----
+      for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&tp_next, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (item.j0 + base >= item.j1) break;
+        const int j = item.j0 + base + lane;
+        // lanes past the end skip the body (no lane waits in a shuffle while
+        // the others integrate)
+        if (j < item.j1) {
+          const int g = b0 + j, self = self_index(j, A.compat_block);
+          d3 pos = {D.x[g], D.x[D.n + g], D.x[2 * D.n + g]};
+          d3 vel = {D.v[g], D.v[D.n + g], D.v[2 * D.n + g]};
+          uint32_t f = D.flags[g];
+          if (c0 == 0) {  // the call's first half kick
+            const d3 a = kick_sum(pos, self, X0, T0, nm);
+            vel.x = fma(a.x, hdt, vel.x);
+            vel.y = fma(a.y, hdt, vel.y);
+            vel.z = fma(a.z, hdt, vel.z);
+          }
+          for (int k = 0; k < cn; k++) {
+            const bool last = c0 + k == A.steps - 1;
+            const Hist h = hist_at(cur, nh, k);
+            pos.x = fma(h.P1[0], hdt, pos.x);
+            pos.y = fma(h.P1[1], hdt, pos.y);
+            pos.z = fma(h.P1[2], hdt, pos.z);
+            bool ce;
+            drift(pos, vel, self, h, nm, ce);
+            f &= ~MERC_FLAG_CE_LAST;
+            if (ce) f |= MERC_FLAG_CE_LAST | MERC_FLAG_CE_EVER;
+            pos.x = fma(h.P2[0], hdt, pos.x);
+            pos.y = fma(h.P2[1], hdt, pos.y);
+            pos.z = fma(h.P2[2], hdt, pos.z);
+            // the second half kick of this step and (unless this is the last
+            // step of the call) the first of the next, in one pass
+            d3 accB = {0.0, 0.0, 0.0}, accA = {0.0, 0.0, 0.0};
+            for (int i = 0; i < nm; i++) {
+              const FastSrc SB = smem_src(h.X2, M, h.T2, nh, i);
+              const int thrA = thr_unpack(h.TN[4 * i + 3]);
+              const double dx = fsub(D.u, SB.x, pos.x), dy = fsub(D.u, SB.y, pos.y), dz = fsub(D.u, SB.z, pos.z);
+              const double r2 = fma(dx, dx, fma(dy, dy, fmul(D.u, dz, dz)));
+              if (!last && hi_word(r2) > max(SB.rc2_hi, thrA) && i != self && seed_in_range(r2)) {
+                const double w = fmul(D.u, SB.m, inv_softened_r3(D.u, r2, fadd(D.u, r2, A.soft2)));
+                accB.x = fma(w, dx, accB.x);
+                accB.y = fma(w, dy, accB.y);
+                accB.z = fma(w, dz, accB.z);
+                accA.x = fma(w, dx, accA.x);
+                accA.y = fma(w, dy, accA.y);
+                accA.z = fma(w, dz, accA.z);
+              } else {
+                pair_fast<false>(D.u, pos, self, i, SB, A.soft2, accB);
+                if (!last) pair_fast<false>(D.u, pos, self, i, smem_src(h.X2, M, h.TN, nh, i), A.soft2, accA);
+              }
             }
+            vel.x = fma(accB.x, hdt, vel.x);
+            vel.y = fma(accB.y, hdt, vel.y);
+            vel.z = fma(accB.z, hdt, vel.z);
+            if (!last) {
+              vel.x = fma(accA.x, hdt, vel.x);
+              vel.y = fma(accA.y, hdt, vel.y);
+              vel.z = fma(accA.z, hdt, vel.z);
+            }
+            f = step_flags(f, pos, vel);
           }
-          vel.x = fma(accB.x, hdt, vel.x);
-          vel.y = fma(accB.y, hdt, vel.y);
-          vel.z = fma(accB.z, hdt, vel.z);
-          if (!last) {
-            vel.x = fma(accA.x, hdt, vel.x);
-            vel.y = fma(accA.y, hdt, vel.y);
-            vel.z = fma(accA.z, hdt, vel.z);
-          }
-          f = step_flags(f, pos, vel);
+          D.x[g] = pos.x;
+          D.x[D.n + g] = pos.y;
+          D.x[2 * D.n + g] = pos.z;
+          D.v[g] = vel.x;
+          D.v[D.n + g] = vel.y;
+          D.v[2 * D.n + g] = vel.z;
+          D.flags[g] = f;
+          if (c0 + cn == A.steps) D.ce[g] = (f & MERC_FLAG_CE_LAST) ? 1 : 0;
         }
-        D.x[g] = pos.x;
-        D.x[D.n + g] = pos.y;
-        D.x[2 * D.n + g] = pos.z;
-        D.v[g] = vel.x;
-        D.v[D.n + g] = vel.y;
-        D.v[2 * D.n + g] = vel.z;
-        D.flags[g] = f;
-        if (c0 + cn == A.steps) D.ce[g] = (f & MERC_FLAG_CE_LAST) ? 1 : 0;
       }
-      __syncthreads();  // before the next chunk overwrites the history
+      __syncthreads();  // before the next chunk overwrites this history
     }
     // the primary item stages the massive bodies (k_sweep_commit writes them
     // back after the launch: other items of the system may still read the
@@ -401,7 +423,7 @@ __global__ void k_sweep_persistent(SweepArgs A) {
       }
       A.stage_f[c] = fm;
       if (A.steps > 0) {
-        const Hist h = hist_at(hist, nh, (A.steps - 1) % C);
+        const Hist h = hist_at(hist_buf(((A.steps - 1) / C) & 1), nh, (A.steps - 1) % C);
         for (int k = 0; k < 4; k++) A.rc_final[4 * (size_t)g + k] = h.TN[4 * lane + k];
       }
     }
