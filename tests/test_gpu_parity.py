@@ -159,7 +159,7 @@ def test_errors_are_reported_not_crashed():
     g.close()
 
 
-@pytest.mark.parametrize("shape", ["many_small", "few_large"])
+@pytest.mark.parametrize("shape", ["many_small", "few_large", "few_test_particles"])
 def test_persistent_sweep_kernel_equals_per_phase_kernels(shape):
     """Small systems run in the persistent kernel (work queue, merged half
     kicks); with the drift log on they run in the per-phase kernels.  Both give
@@ -168,8 +168,10 @@ def test_persistent_sweep_kernel_equals_per_phase_kernels(shape):
     integrate the massive bodies alike, the primary one writing them back)."""
     if shape == "many_small":
         sysm = systems.sweep(n_systems=320, nt_lo=8, nt_hi=120, seed=31)
-    else:
+    elif shape == "few_large":
         sysm = systems.sweep(n_systems=3, nt_lo=3000, nt_hi=6000, seed=32)
+    else:  # some systems without test particles
+        sysm = systems.sweep(n_systems=200, nt_lo=0, nt_hi=3, seed=33)
     kw = dict(dt=sysm.dt, hill_factor=3.0, drift=merc.DRIFT_UNIVERSAL)
     a = merc.Integrator(merc.default_params(**kw))
     a.load_systems(sysm)
@@ -318,6 +320,21 @@ def test_ejection_and_encounter_flags_match_oracle(oracle, which, eject_r, drift
     assert np.all(ej[r > eject_r])
     if which == "embryo":
         assert np.any(st.flags & merc.FLAG_CE_EVER)
+
+
+def test_dense_encounters_match_oracle(oracle):
+    """A big system in which about half of the bodies are in an encounter
+    every step (changeover at 30 Hill radii): the encounter list built by the
+    test kernel from many duplicate flags, and the encounter task kernel with
+    ~28 x 60 tasks per step, agree with the oracle."""
+    sysm = systems.embryo_disk(n_embryos=120, seed=26)
+    steps = 20
+    st, gs, alag, (op, ov, oal, of, ost) = run_both(oracle, sysm, steps, drift=merc.DRIFT_UNIVERSAL,
+                                                    hill_factor=30.0)
+    assert gs.ce_body_steps > 0.4 * sysm.n_total * steps
+    assert rel_err(st.pos, op).max() <= 1e-12
+    assert rel_err(st.vel, ov).max() <= 1e-12
+    assert np.array_equal(st.flags, of)
 
 
 def test_nonfinite_flag_matches_oracle(oracle):
