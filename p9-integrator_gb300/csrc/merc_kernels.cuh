@@ -641,7 +641,10 @@ __global__ void __launch_bounds__(kTile) k_kick_tiled_merged(Dev D, const Work* 
   const bool active = j < b1;
   const int local = j - b0, self = self_index(local, compat_block);
   d3 pos = active ? load3(D.x, n, j) : d3{0.0, 0.0, 0.0};
+  // accA repeats accB's operations until the first pair that is not far in
+  // both kicks, so one accumulator serves both until then (same bits)
   d3 accB = {0.0, 0.0, 0.0}, accA = {0.0, 0.0, 0.0};
+  bool split = false;
   for (int c = W.c0; c < W.c1; c += kSrcTile) {
     const int cnt = min(kSrcTile, W.c1 - c);
     __syncthreads();
@@ -660,10 +663,16 @@ __global__ void __launch_bounds__(kTile) k_kick_tiled_merged(Dev D, const Work* 
           accB.x = fma(w, dx, accB.x);
           accB.y = fma(w, dy, accB.y);
           accB.z = fma(w, dz, accB.z);
-          accA.x = fma(w, dx, accA.x);
-          accA.y = fma(w, dy, accA.y);
-          accA.z = fma(w, dz, accA.z);
+          if (split) {
+            accA.x = fma(w, dx, accA.x);
+            accA.y = fma(w, dy, accA.y);
+            accA.z = fma(w, dz, accA.z);
+          }
         } else {
+          if (!split) {
+            accA = accB;
+            split = true;
+          }
           pair_fast<false>(D.u, pos, self, i, SB, soft2, accB);
           FastSrc SA = SB;
           SA.rc = tileA[k][0];
@@ -676,6 +685,7 @@ __global__ void __launch_bounds__(kTile) k_kick_tiled_merged(Dev D, const Work* 
     }
   }
   if (!active) return;
+  if (!split) accA = accB;
   d3 vel = load3(D.v, n, j);
   vel.x = fma(accB.x, hdt, vel.x);
   vel.y = fma(accB.y, hdt, vel.y);

@@ -370,7 +370,10 @@ __global__ void __launch_bounds__(256, 2) k_sweep_persistent(SweepArgs A) {
             pos.z = fma(h.P2[2], hdt, pos.z);
             // the second half kick of this step and (unless this is the last
             // step of the call) the first of the next, in one pass
+            // accA repeats accB's operations until the first pair that is not
+            // far in both kicks, so one accumulator serves both until then
             d3 accB = {0.0, 0.0, 0.0}, accA = {0.0, 0.0, 0.0};
+            bool split = false;
             for (int i = 0; i < nm; i++) {
               const FastSrc SB = smem_src(h.X2, M, h.T2, nh, i);
               const int thrA = thr_unpack(h.TN[4 * i + 3]);
@@ -381,14 +384,21 @@ __global__ void __launch_bounds__(256, 2) k_sweep_persistent(SweepArgs A) {
                 accB.x = fma(w, dx, accB.x);
                 accB.y = fma(w, dy, accB.y);
                 accB.z = fma(w, dz, accB.z);
-                accA.x = fma(w, dx, accA.x);
-                accA.y = fma(w, dy, accA.y);
-                accA.z = fma(w, dz, accA.z);
+                if (split) {
+                  accA.x = fma(w, dx, accA.x);
+                  accA.y = fma(w, dy, accA.y);
+                  accA.z = fma(w, dz, accA.z);
+                }
               } else {
+                if (!split) {
+                  accA = accB;
+                  split = true;
+                }
                 pair_fast<false>(D.u, pos, self, i, SB, A.soft2, accB);
                 if (!last) pair_fast<false>(D.u, pos, self, i, smem_src(h.X2, M, h.TN, nh, i), A.soft2, accA);
               }
             }
+            if (!split) accA = accB;
             vel.x = fma(accB.x, hdt, vel.x);
             vel.y = fma(accB.y, hdt, vel.y);
             vel.z = fma(accB.z, hdt, vel.z);
