@@ -173,6 +173,19 @@ __device__ __forceinline__ bool ce_maybe(const F4& t, const F4& s, float rc) {
   return !(r2 > lim * lim && lim > 0.0f);
 }
 
+// ce_maybe of a pair in both directions (t vs source s with r_crit rc_s, s vs
+// source t with rc_t), the distance computed once: the same answers as two
+// ce_maybe calls (the difference changes sign exactly, the scale sum is
+// commutative).
+__device__ __forceinline__ void ce_maybe2(const F4& t, const F4& s, float rc_s, float rc_t, bool& m_t, bool& m_s) {
+  float dx = s.x - t.x, dy = s.y - t.y, dz = s.z - t.z;
+  float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  const float pad = fmaf(1e-5f, s.sc + t.sc, 1e-37f);
+  const float lt = fmaf(rc_s, 1.00001f, pad), ls = fmaf(rc_t, 1.00001f, pad);
+  m_t = !(r2 > lt * lt && lt > 0.0f);
+  m_s = !(r2 > ls * ls && ls > 0.0f);
+}
+
 // Encounter test of one pair, exact: sqrt(r^2) < r_crit and not self
 // (sim.cuh:602-609); the sqrt is skipped when r^2 is clearly above r_crit^2.
 __device__ __forceinline__ bool pair_ce(const d3& pos, int self, int i, const FastSrc& S) {

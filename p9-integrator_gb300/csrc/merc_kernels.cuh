@@ -832,7 +832,8 @@ __global__ void __launch_bounds__(32 * kSymWarps) k_sym(Dev D, const SymTask* __
       if (!KICK) {
         // encounter of i with source j uses r_crit(j), of j with i uses r_crit(i);
         // the FP32 prefilter clears far pairs without FP64 work
-        const bool mA = ce_maybe(A.f, B.f, B.rcf), mB = ce_maybe(B.f, A.f, A.rcf);
+        bool mA, mB;
+        ce_maybe2(A.f, B.f, B.rcf, A.rcf, mA, mB);
         if (mA || mB) {
           const int g = b0 + B.idx;
           const double dx = D.x[g] - A.x, dy = D.x[D.n + g] - A.y, dz = D.x[2 * D.n + g] - A.z;
