@@ -64,19 +64,6 @@ __device__ __forceinline__ double rcrit_hc(const d3& r, const d3& v, double hc) 
   return a * hc;
 }
 
-__device__ __forceinline__ double rcrit(const d3& r, const d3& v, double m, double hill) {
-  d3 h = {fma(r.y, v.z, -r.z * v.y), fma(r.z, v.x, -r.x * v.z), fma(r.x, v.y, -r.y * v.x)};
-  double h2 = mag2(h);
-  double rmag = sqrt(mag2(r));
-  double v2 = mag2(v);
-  double rdv = fma(r.x, v.x, fma(r.y, v.y, r.z * v.z));
-  double factor = v2 - 1.0 / rmag;
-  d3 ev = {fma(factor, r.x, -rdv * v.x), fma(factor, r.y, -rdv * v.y), fma(factor, r.z, -rdv * v.z)};
-  double e2 = mag2(ev);
-  double a = h2 / (1.0 - e2);
-  return a * (mm::cbrt(m / 3.0) * hill);
-}
-
 // Changeover weight K(y), y = (r_ij - 0.1 rc) / (0.9 rc) (sim.cuh:176-183).
 // The common cases y > 1 (K = 1) and y < 0 (K = 0) give the same bits as the
 // branch-free formula; everything else takes the formula.
