@@ -17,8 +17,9 @@ ours:       K timed steps on the GPU through libmerc.so.  One bench step is one
             over device time (CUDA events), `e2e` is host wall time of the
             public C-ABI call sequence set_state (H2D, pinned) -> step -> get_state
             (D2H) per bench step.  Also reported: kick-kernel roofline against the
-            measured FP64 FMA peak, the CPU oracle on the host cores, and the
-            element-drift (reference-compat) path.
+            measured FP64 FMA peak, the same for the encounter sub-step kernel
+            (timed in three more calls), the CPU oracle on the host cores, and
+            the element-drift (reference-compat) path.
 reference:  the CPU restatement of the reference step (oracle/, OpenMP over all
             host cores), same workload and metric; the reference itself is CUDA
             only and ships no CPU path.
@@ -376,6 +377,23 @@ def run_ours(args, world, rank, local, dist):
     traffic = load_traffic().get("kick_bytes_per_launch")
     st = g.stats()
 
+    # the encounter sub-step (the largest share of the step at this encounter
+    # density): a few more timed calls with events around its kernel
+    g.time_kicks(False)
+    g.time_encounter(True)
+    enc_ms, enc_n, ce0, enc_calls = 0.0, 0, g.stats().ce_body_steps, 3
+    for _ in range(enc_calls):
+        g.flush_l2(512 << 20)
+        g.step(S)
+        em, ec = g.encounter_ms()
+        enc_ms += em * ec
+        enc_n += ec
+    enc_avg_ms = enc_ms / max(enc_n, 1)
+    ce_per_step = (g.stats().ce_body_steps - ce0) / (enc_calls * S)
+    enc_pairs = ce_per_step * 7 * nm  # 7 evaluations of the sub-step, each over every massive source
+    enc_achieved = FLOPS_PER_PAIR * enc_pairs / (enc_avg_ms * 1e-3) / 1e12
+    g.time_encounter(False)
+
     # end to end through the C ABI with host buffers (pinned) and copies
     e2e_steps = max(3, min(args.steps, 20))
     host = g.state()
@@ -431,6 +449,11 @@ def run_ours(args, world, rank, local, dist):
                      "peak_source": "measured FP64 FMA loop on this GPU (merc_diag_fp64_peak)",
                      "kick_ms": kick_avg_ms, "kick_launches": kick_n, "pairs_per_launch": pairs_per_kick,
                      "flops_per_pair": FLOPS_PER_PAIR},
+        "roofline_encounter": {"bound": "fp64", "kernel": "k_encounter_tasks (encounter sub-step)",
+                               "achieved": enc_achieved, "peak": peak, "unit": "TFLOP/s",
+                               "frac": enc_achieved / peak, "encounter_ms": enc_avg_ms, "launches": enc_n,
+                               "encounter_bodies_per_step": ce_per_step, "pairs_per_launch": enc_pairs,
+                               "flops_per_pair": FLOPS_PER_PAIR},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 7 * 8 * n,
                 "d2h_bytes_per_step": 6 * 8 * n + 4 * n, "steps": e2e_steps},

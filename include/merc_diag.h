@@ -44,6 +44,13 @@ int merc_diag_flush_l2(merc_ctx* ctx, int64_t bytes);
 int merc_diag_time_kicks(merc_ctx* ctx, int on);
 int merc_diag_kick_ms(merc_ctx* ctx, double* avg_ms, int32_t* n_launches);
 
+/* on != 0: record CUDA events around the big systems' encounter sub-step
+ * kernel when the step graph is next captured.  merc_diag_encounter_ms
+ * returns its mean duration over the most recent graph replays and the number
+ * of launches it averaged. */
+int merc_diag_time_encounter(merc_ctx* ctx, int on);
+int merc_diag_encounter_ms(merc_ctx* ctx, double* avg_ms, int32_t* n_launches);
+
 /* Kicks of big systems sum the far field once for the two kicks around a step
  * boundary inside a step graph; when a source's far-field radius moved between
  * them (orbits with e > 1/3) the second far-field pass runs.  *count: how many

@@ -87,6 +87,8 @@ struct merc_ctx {
   std::vector<cudaEvent_t> kick_ev;  // start/end pairs recorded around kicks inside the graph
   std::vector<char> kick_ev_used;    // slots recorded by the captured graphs
   bool time_kicks = false;
+  std::vector<cudaEvent_t> enc_ev;  // start/end pairs around the big systems' encounter sub-step
+  bool time_encounter = false;
   bool pdl = true;  // programmatic dependent launches inside the step graphs
   int smem_optin = 0;  // largest dynamic shared memory per block (opt-in)
   int sms = 0;         // multiprocessors of the device
@@ -599,12 +601,17 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       nk++;
     }
     if (ctx->has_big) {
+      // (encounter timing: events on the step stream around the launch; the
+      // drift runs on the second branch, outside the interval)
+      const bool enc_ev = ctx->time_encounter && !ctx->enc_ev.empty();
+      if (enc_ev) CK(cudaEventRecordWithFlags(ctx->enc_ev[2 * step_in_graph], s, cudaEventRecordExternal));
       if (p.bs_rows == 3)
         launch(k_encounter_tasks, ctx->sms * kEncBlocksPerSM, 32 * kEncTaskWarps, D, rcB, p.dt, p.compat_block,
                p.softening2, kEncSpin);
       else
         launch(k_encounter_cluster, ctx->enc_blocks * 2, 32, D, rcB, p.dt, p.compat_block, p.bs_rows,
                p.softening2);
+      if (enc_ev) CK(cudaEventRecordWithFlags(ctx->enc_ev[2 * step_in_graph + 1], s, cudaEventRecordExternal));
       nk++;
     }
     if (fork) CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
@@ -671,6 +678,13 @@ int build_graphs(merc_ctx* ctx) {
       ctx->kick_ev.push_back(e);
     }
     ctx->kick_ev_used.assign(kKickSlots, 0);
+  }
+  if (ctx->time_encounter) {
+    while (ctx->enc_ev.size() < (size_t)(kKickSlots / 2)) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      ctx->enc_ev.push_back(e);
+    }
   }
   for (int k = 0; k < 5; k++) {
     int st = capture(ctx, kKindSteps[k], ctx->time_kicks, kKindSlot[k], kKindFirstAlone[k], kKindLastAlone[k],
@@ -908,6 +922,7 @@ int merc_destroy(merc_ctx* ctx) {
   if (ctx->d_log) cudaFree(ctx->d_log);
   if (ctx->d_log_count) cudaFree(ctx->d_log_count);
   for (cudaEvent_t e : ctx->kick_ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->enc_ev) cudaEventDestroy(e);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
@@ -1955,6 +1970,37 @@ int merc_diag_time_kicks(merc_ctx* ctx, int on) {
   if (!ctx) return MERC_ERR_CONFIG;
   ctx->time_kicks = on != 0;
   drop_graphs(ctx);
+  return MERC_OK;
+}
+
+int merc_diag_time_encounter(merc_ctx* ctx, int on) {
+  if (!ctx) return MERC_ERR_CONFIG;
+  ctx->time_encounter = on != 0;
+  drop_graphs(ctx);
+  return MERC_OK;
+}
+
+int merc_diag_encounter_ms(merc_ctx* ctx, double* avg_ms, int32_t* n_launches) {
+  if (!ctx || !avg_ms) return MERC_ERR_CONFIG;
+  if (!ctx->time_encounter || !ctx->has_big || ctx->graph_steps == 0 || ctx->last_graph_steps == 0)
+    return fail(ctx, MERC_ERR_STATE, "encounter timing is off, no big system, or no step ran since it was turned on");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  double sum = 0.0;
+  int cnt = 0;
+  // the last replay of every graph kind that the last call used
+  for (int kind = 0; kind < 5; kind++) {
+    if (!(ctx->last_kinds & (1u << kind))) continue;
+    for (int k = 0; k < kKindSteps[kind]; k++) {
+      const int slot = 2 * (kKindSlot[kind] / 4 + k);
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, ctx->enc_ev[slot], ctx->enc_ev[slot + 1]));
+      sum += ms;
+      cnt++;
+    }
+  }
+  *avg_ms = cnt ? sum / cnt : 0.0;
+  if (n_launches) *n_launches = cnt;
   return MERC_OK;
 }
 

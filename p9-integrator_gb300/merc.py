@@ -135,6 +135,8 @@ def lib() -> C.CDLL:
     L.merc_diag_far_recomputes.argtypes = [vp, C.POINTER(C.c_int64)]
     L.merc_diag_pdl.argtypes = [vp, C.c_int]
     L.merc_diag_encounter_wait.argtypes = [vp, C.POINTER(C.c_int32)]
+    L.merc_diag_time_encounter.argtypes = [vp, C.c_int]
+    L.merc_diag_encounter_ms.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int32)]
     _LIB = L
     return L
 
@@ -351,6 +353,17 @@ class Integrator:
         c = C.c_int64()
         self._check(self.L.merc_diag_far_recomputes(self.h, C.byref(c)))
         return c.value
+
+    def time_encounter(self, on: bool = True):
+        """Record CUDA events around the big systems' encounter sub-step."""
+        self._check(self.L.merc_diag_time_encounter(self.h, 1 if on else 0))
+
+    def encounter_ms(self):
+        """Mean encounter sub-step duration (ms) of the last call and the
+        number of launches averaged."""
+        ms, cnt = C.c_double(), C.c_int32()
+        self._check(self.L.merc_diag_encounter_ms(self.h, C.byref(ms), C.byref(cnt)))
+        return ms.value, cnt.value
 
     def encounter_wait_check(self) -> bool:
         """Runs the encounter task kernel with a dependency that is never
