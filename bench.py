@@ -137,7 +137,7 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def cpu_baseline(sysm, params_kw, budget_s=12.0):
+def cpu_baseline(sysm, params_kw, sample_s=12.0):
     """The oracle on this host's cores, timed on a bounded number of steps."""
     from oracle import Oracle
     from oracle import default_params as oparams
@@ -148,7 +148,7 @@ def cpu_baseline(sysm, params_kw, budget_s=12.0):
     t0 = time.perf_counter()
     pos, vel, alag, fl, _ = O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag, steps=1)
     one = time.perf_counter() - t0
-    steps = int(max(1, min(5000, budget_s / max(one, 1e-6))))
+    steps = int(max(1, min(5000, sample_s / max(one, 1e-6))))
     t0 = time.perf_counter()
     O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag, flags=fl, steps=steps)
     dt = time.perf_counter() - t0

@@ -1,6 +1,6 @@
 // Host stand-in for <cooperative_groups.h>: enough of the cluster API for the
-// reference's get_mapped_block and kernel body to compile as host code.  The
-// driver never calls the kernel; get_mapped_block is not used either.
+// reference's get_mapped_block and kernel body to compile as host code.
+// refhost_driver.cpp never calls the kernel; get_mapped_block is not used either.
 // TEST INFRASTRUCTURE.
 #pragma once
 namespace cooperative_groups {

@@ -17,7 +17,7 @@
 struct double3 { double x, y, z; };
 static inline double3 make_double3(double x, double y, double z) { return double3{x, y, z}; }
 struct merc_dim3 { unsigned x, y, z; };
-// threadIdx / blockDim of the emulated thread (set by the driver)
+// threadIdx / blockDim of the emulated thread (set by refhost_driver.cpp)
 extern thread_local merc_dim3 threadIdx;
 extern thread_local merc_dim3 blockDim;
 

@@ -3,7 +3,7 @@
 Tolerances: the element drift path is compared bit for bit with the oracle
 evaluated with the same elementary-function library (precision 2), because
 that drift amplifies rounding by ~1e6 in 100 steps; the universal path is
-compared at relative 1e-12 per body after 100 steps (the spec bar).
+compared at relative 1e-12 per body after 100 steps.
 Encounter flags must be identical in both.
 """
 import numpy as np
