@@ -284,8 +284,9 @@ def warm_start_section(merc, args, local):
     """Learned warm start of the universal drift: log ~1e7 (drift input ->
     converged anomaly) pairs from the embryo disk and the sweep integrated
     together in one context, train the FP32 MLP on the GPU, then integrate each
-    workload from the same initial state with the plain guess dt/r0, the
-    learned guess and the third-order series guess (the default).  Reported
+    workload (and the planetesimal disk) from the same initial state with the
+    plain guess dt/r0, the learned guess and the third-order series guess (the
+    default).  Reported
     per guess: Newton iterations per solve, and the iterations the warps
     executed per solve (a warp runs as many iterations as its slowest lane)."""
     c1, c2 = systems.embryo_disk(), systems.sweep()
@@ -311,12 +312,15 @@ def warm_start_section(merc, args, local):
            "loss_first_last": [float(loss[0]), float(loss[-1])]}
     steps = max(3, min(args.steps, 20))
     guesses = (("plain", merc.WARM_PLAIN), ("learned", merc.WARM_MLP), ("series", merc.WARM_SERIES))
-    for name, sysm in (("embryo_disk", c1), ("sweep", c2)):
+    # the large single system with the learned drift: 8196 planetesimals +
+    # 131072 test particles (the network is the one trained above)
+    c4 = systems.planetesimal_disk()
+    for name, sysm in (("embryo_disk", c1), ("sweep", c2), ("planetesimal_disk", c4)):
         res = {}
         states = {}
         for key, warm in guesses:
-            gi = merc.Integrator(merc.default_params(dt=sysm.dt, hill_factor=3.0, drift=merc.DRIFT_UNIVERSAL,
-                                                     warm_start=warm), device=local)
+            gi = merc.Integrator(merc.default_params(dt=sysm.dt, hill_factor=sysm.hill_factor,
+                                                     drift=merc.DRIFT_UNIVERSAL, warm_start=warm), device=local)
             gi.load_systems(sysm)
             if warm == merc.WARM_MLP:
                 gi.mlp_set_weights(w)
