@@ -417,17 +417,28 @@ __device__ __forceinline__ float abs_f32_trunc(double x) {
 // Initial guesses of the universal anomaly (the s0 argument of universal_drift)
 constexpr double kGuessPlain = 0.0;    // s0 = dt / r0
 constexpr double kGuessSeries = -1.0;  // third-order series in dt (below)
+constexpr double kGuessRel = -2.0;     // s0 = (dt / r0) (1 + rel), rel from the learned guess
+
+// x as a double by integer operations on its bits (exact for normal floats
+// and zero; a denormal gives zero; not for infinities or NaN), so that no
+// conversion runs on the FP64 pipe
+__device__ __forceinline__ double f64_of_f32(float x) {
+  const int b = __float_as_int(x), m = b & 0x7fffffff;
+  if (m < 0x00800000) return 0.0;
+  return __hiloint2double((b & (int)0x80000000) | ((m >> 3) + 0x38000000), m << 29);
+}
 
 // Universal Kepler drift with mu = 1 from initial guess s0 (kGuessPlain: dt /
 // r0; kGuessSeries: the universal Kepler equation t = r0 s + eta s^2/2 + zeta
 // s^3/6 + O(s^4) inverted to third order, s = s0 (1 - (eta / 2 r0) s0 + ((3
 // eta^2 - r0 zeta) / 6 r0^2) s0^2) with s0 = dt / r0, kept when within a factor
-// 2 of s0): Newton on r0 s + eta G2 + zeta G3 = dt; after each update the
+// 2 of s0; kGuessRel: s0 (1 + rel), kept under the same condition): Newton on
+// r0 s + eta G2 + zeta G3 = dt; after each update the
 // Newton error estimate |f''/(2 f')| ds^2 of the new s is compared with tol |s|
 // (trusted once |ds| <= 1e-3 |s|), in FP32 on truncated copies (the decision
 // needs no more than a factor of 2); f and g at the final s.
 __device__ __forceinline__ UD universal_drift(const FU& U, const d3& x0, const d3& v0, double dt, double s0,
-                                              double tol, int max_iter) {
+                                              double tol, int max_iter, float rel = 0.0f) {
   const double rr = fma(x0.x, x0.x, fma(x0.y, x0.y, fmul(U, x0.z, x0.z)));
   const double ir0 = rsqrt_fast(U, rr);
   const double r0 = fmul(U, rr, ir0);
@@ -443,6 +454,9 @@ __device__ __forceinline__ UD universal_drift(const FU& U, const d3& x0, const d
       const double a2 = fmul(U, fmul(U, fma(fmul(U, 3.0, eta), eta, -fmul(U, r0, zeta)), fmul(U, ir0, ir0)),
                              1.0 / 6.0);
       const double q = fmul(U, p0, fma(p0, fma(p0, a2, -a1), 1.0));
+      if (q > 0.5 * p0 && q < 2.0 * p0) g = q;
+    } else if (s0 == kGuessRel) {
+      const double q = fma(p0, f64_of_f32(rel), p0);
       if (q > 0.5 * p0 && q < 2.0 * p0) g = q;
     }
     s0 = g;

@@ -1612,10 +1612,23 @@ __global__ void k_mlp_probe(int n, const double* pos, const double* vel, double 
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   d3 x = {pos[j], pos[n + j], pos[2 * n + j]}, v = {vel[j], vel[n + j], vel[2 * n + j]};
-  WarmIn w = warm_features(x, v, dt);
-  double s0 = (blob && w.f[0] >= kWarmMinX1) ? warm_guess(blob, w) : w.s0;
-  guess[j] = s0;
-  UD u = universal_drift(FU{1.0, -0.0}, x, v, dt, s0, tol, max_iter);
+  // as the drift kernels: FP32 features, the network's relative correction
+  double s0 = kGuessPlain;
+  float rel = 0.0f;
+  if (blob) {
+    float f[4];
+    warm_features_f32(x, v, f32_trunc(dt), f);
+    if (f[0] >= kWarmMinX1) {
+      const float d = warm_delta(blob, f);
+      if (d == d) {
+        s0 = kGuessRel;
+        rel = d;
+      }
+    }
+  }
+  const double p0 = dt / sqrt(mag2(x));
+  guess[j] = s0 == kGuessRel ? p0 * (1.0 + (double)rel) : p0;
+  UD u = universal_drift(FU{1.0, -0.0}, x, v, dt, s0, tol, max_iter, rel);
   solved[j] = u.s;
   iters[j] = u.iters;
 }

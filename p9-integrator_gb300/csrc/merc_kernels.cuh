@@ -1168,11 +1168,20 @@ __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, doubl
       d3 vel = load3(D.v, n, j);
       WarmIn w;
       double s0 = guess;  // kGuessPlain or kGuessSeries unless the network guesses
-      if (mlp || log_data) {
-        w = warm_features(pos, vel, dt);
-        if (mlp && w.f[0] >= kWarmMinX1) s0 = warm_guess(blob, w);
+      float rel = 0.0f;
+      if (log_data) w = warm_features(pos, vel, dt);  // the logged features in FP64
+      if (mlp) {
+        float f[4];
+        warm_features_f32(pos, vel, f32_trunc(dt), f);
+        if (f[0] >= kWarmMinX1) {
+          const float d = warm_delta(blob, f);
+          if (d == d) {
+            s0 = kGuessRel;
+            rel = d;
+          }
+        }
       }
-      UD u = universal_drift(D.u, pos, vel, dt, s0, tol, max_iter);
+      UD u = universal_drift(D.u, pos, vel, dt, s0, tol, max_iter, rel);
       store3(D.xo, n, j, u.out.pos);
       store3(D.vo, n, j, u.out.vel);
       its = u.iters;

@@ -6,7 +6,9 @@
 //   delta = -x1 x3 / 2 + x1^2 y,
 //   x1 = dt / r0^1.5,  x2 = r0 v0^2,  x3 = eta / sqrt(r0),  x4 = sign of the energy.
 // The network predicts y (the part of delta beyond its first-order term),
-// from the features normalised by the training set's mean and spread.  The
+// from the features normalised by the training set's mean and spread.  At
+// inference the features and delta are computed in FP32 (warm_features_f32,
+// warm_delta) and the drift forms s0 (1 + delta) from its own FP64 s0.  The
 // FP64 Newton solve that follows is unchanged; the guess only moves its
 // starting point.  Outside the feature box seen in training the plain guess
 // is used.
@@ -43,6 +45,22 @@ __device__ __forceinline__ WarmIn warm_features(const d3& x0, const d3& v0, doub
   return w;
 }
 
+// The same features in FP32 from the high-word truncations of x0, v0 and dt
+// (each within 2^-20): no FP64 square root, division or conversion.  The
+// guess they feed needs ~1e-6; the FP64 Newton solve that follows is
+// unchanged.
+__device__ __forceinline__ void warm_features_f32(const d3& x0, const d3& v0, float dtf, float f[4]) {
+  const float x = f32_trunc(x0.x), y = f32_trunc(x0.y), z = f32_trunc(x0.z);
+  const float vx = f32_trunc(v0.x), vy = f32_trunc(v0.y), vz = f32_trunc(v0.z);
+  const float r2 = fmaf(x, x, fmaf(y, y, z * z));
+  const float ir = rsqrtf(r2), r0 = r2 * ir, isr = sqrtf(ir);  // 1/r0, r0, 1/sqrt(r0)
+  const float v2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz)), eta = fmaf(x, vx, fmaf(y, vy, z * vz));
+  f[0] = dtf * ir * isr;
+  f[1] = r0 * v2;
+  f[2] = eta * isr;
+  f[3] = (2.0f - r0 * v2) < 0.0f ? 1.0f : -1.0f;
+}
+
 __device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
 
 // forward pass on normalised inputs; p points at the blob (shared or global)
@@ -66,19 +84,17 @@ __device__ __forceinline__ float mlp_forward(const float* __restrict__ p, const 
   return y;
 }
 
-// Learned guess of s, or the plain guess outside the trained feature box.
-__device__ __forceinline__ double warm_guess(const float* __restrict__ p, const WarmIn& w) {
+// Relative correction of the plain guess, s = (dt / r0) (1 + delta), from
+// FP32 features; NaN outside the trained feature box.
+__device__ __forceinline__ float warm_delta(const float* __restrict__ p, const float f[4]) {
   float xn[4];
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    if (!(w.f[k] >= p[kBoxLo + k] && w.f[k] <= p[kBoxHi + k])) return w.s0;
-    xn[k] = (w.f[k] - p[kInMean + k]) * p[kInScale + k];
+    if (!(f[k] >= p[kBoxLo + k] && f[k] <= p[kBoxHi + k])) return __int_as_float(0x7fc00000);
+    xn[k] = (f[k] - p[kInMean + k]) * p[kInScale + k];
   }
-  float yn = mlp_forward(p, xn);
-  double y = (double)(yn / p[kOutScale] + p[kOutMean]);
-  double x1 = (double)w.f[0], x3 = (double)w.f[2];
-  double delta = x1 * fma(x1, y, -0.5 * x3);
-  return w.s0 * (1.0 + delta);
+  const float y = mlp_forward(p, xn) / p[kOutScale] + p[kOutMean];
+  return f[0] * fmaf(f[0], y, -0.5f * f[2]);
 }
 
 // training target y of a solved drift: (s/s0 - 1 + x1 x3 / 2) / x1^2

@@ -162,11 +162,19 @@ __global__ void __launch_bounds__(256, 2) k_sweep_persistent(SweepArgs A) {
       my_ce++;
     } else {
       double s0 = A.guess;  // kGuessPlain or kGuessSeries unless the network guesses
+      float rel = 0.0f;
       if (A.mlp) {
-        const WarmIn w = warm_features(pos, vel, A.dt);
-        if (w.f[0] >= kWarmMinX1) s0 = warm_guess(blob, w);
+        float f[4];
+        warm_features_f32(pos, vel, f32_trunc(A.dt), f);
+        if (f[0] >= kWarmMinX1) {
+          const float d = warm_delta(blob, f);
+          if (d == d) {
+            s0 = kGuessRel;
+            rel = d;
+          }
+        }
       }
-      UD u = universal_drift(D.u, pos, vel, A.dt, s0, A.tol, A.max_iter);
+      UD u = universal_drift(D.u, pos, vel, A.dt, s0, A.tol, A.max_iter, rel);
       out = u.out;
       my_it += u.iters;
       my_sol++;
