@@ -96,7 +96,14 @@ def mixed_batch():
     return out
 
 
-@pytest.mark.parametrize("which", ["outer", "embryo", "sweep", "mixed"])
+def two_big_batch():
+    """Two big systems (the momentum summed per block, the generic reduce, the
+    encounter list over both) and a small one."""
+    return systems.concat([systems.embryo_disk(n_embryos=120, seed=41), systems.embryo_disk(n_embryos=70, seed=42),
+                           systems.sweep(n_systems=1, nt_lo=10, nt_hi=10, seed=43)])
+
+
+@pytest.mark.parametrize("which", ["outer", "embryo", "sweep", "mixed", "two_big"])
 def test_universal_parity(oracle, which):
     if which == "outer":
         sysm = systems.outer_solar_system()
@@ -104,8 +111,10 @@ def test_universal_parity(oracle, which):
         sysm = systems.embryo_disk(n_embryos=254)
     elif which == "sweep":  # more systems than SMs: the persistent kernel
         sysm = systems.sweep(n_systems=300, nt_lo=4, nt_hi=24)
-    else:
+    elif which == "mixed":
         sysm = mixed_batch()
+    else:
+        sysm = two_big_batch()
     st, gs, alag, (op, ov, oal, of, ost) = run_both(oracle, sysm, 100, drift=merc.DRIFT_UNIVERSAL)
     assert rel_err(st.pos, op).max() <= 1e-12
     assert rel_err(st.vel, ov).max() <= 1e-12
@@ -118,13 +127,15 @@ def test_universal_parity(oracle, which):
 
 
 @pytest.mark.parametrize("drift,which", [(merc.DRIFT_ELEMENTS, "embryo"), (merc.DRIFT_UNIVERSAL, "embryo"),
-                                         (merc.DRIFT_UNIVERSAL, "sweep")])
+                                         (merc.DRIFT_UNIVERSAL, "sweep"), (merc.DRIFT_UNIVERSAL, "two_big")])
 def test_split_steps_and_resume_are_exact(drift, which):
     """Steps in one call or several (graph replays of 8 and of 1 step, or
     persistent launches with merged half kicks for small systems) give the
     same bits; so does saving the state and resuming it in a new context."""
     if which == "embryo":
         sysm = systems.embryo_disk(n_embryos=94, seed=12)
+    elif which == "two_big":
+        sysm = two_big_batch()
     else:  # more systems than SMs: the persistent kernel
         sysm = systems.sweep(n_systems=320, nt_lo=8, nt_hi=60, seed=12)
     kw = dict(dt=sysm.dt, hill_factor=3.0, drift=drift)
