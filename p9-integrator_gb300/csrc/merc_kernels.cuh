@@ -70,10 +70,10 @@ struct Dev {
   unsigned long long* counters = nullptr;  // kNumCounters: CE body-steps, Kepler iterations, solves,
                                            // non-converged, iterations executed per warp (SIMT)
   // encounter task kernel, per entry of the big-system encounter list:
-  double* enc_q = nullptr;    // 84: quarter sums of the 7 evaluations (kEncParts x 3 each)
+  double* enc_q = nullptr;    // kEncQ: part sums of the 7 evaluations (enc_parts(row) x 3 each)
   double* enc_st = nullptr;   // 27: per row z0, z1, vel after its last published evaluation
   double* enc_res = nullptr;  // 18: per row the sub-step result (position, velocity)
-  int* enc_cnt = nullptr;     // 11: quarters done per evaluation (7), evaluations published per row (3),
+  int* enc_cnt = nullptr;     // 11: parts done per evaluation (7), evaluations published per row (3),
                               //     rows done (1); zero between steps
   int* enc_head = nullptr;    // [0] next task (cleared by the first jump), [1] a bounded wait gave up
 };
@@ -1479,22 +1479,22 @@ struct MidRow {
 
 
 // Encounter sub-step of the big systems (three Richardson rows, N = 1, 2, 4)
-// as a persistent task kernel.  The work of an encounter body is 28 quarter
+// as a persistent task kernel.  The work of an encounter body is 29 part
 // sums: evaluations 0-3 of row 2 (N = 4 sub-steps), 0-1 of row 1 (N = 2) and
-// 0 of row 0 (N = 1), each over the four quarters of the sources
-// (warp_source_sum).  The rows are independent until the final
+// 0 of row 0 (N = 1), each over enc_parts(row) contiguous parts of the
+// sources (warp_source_sum).  The rows are independent until the final
 // extrapolation, so the critical path is row 2's four evaluations.  Warps take
 // tasks from one atomic counter in units of one (row, evaluation) for every
 // body, in the order kEncOrder, where every unit follows the one it depends
 // on: a task's predecessors were all handed out before it, to warps that are
 // running, and a warp whose evaluation e > 0 is not yet published waits for
 // it (bounded; then it sets enc_head[1] and every warp stops).  The warp that
-// completes the fourth quarter of an evaluation (atomic count) adds the
-// quarter sums in quarter order, advances the row's modified midpoint
-// (MidRow) and publishes its state; the warp that completes the last row
-// combines the three rows (Richardson) and clears the body's counters for the
-// next step.  The sums and their order are those of the sequential scheme
-// with quarter sums (k_encounter_cluster with rows = 3 gives the same bits).
+// completes the last part of an evaluation (atomic count) adds the part sums
+// in part order, advances the row's modified midpoint (MidRow) and publishes
+// its state; the warp that completes the last row combines the three rows
+// (Richardson) and clears the body's counters for the next step.  The sums
+// and their order are fixed (the parts of a row and their order do not depend
+// on the schedule), so the results do not depend on which warp runs what.
 // Measured on the 2002-body disk (~190 encounter bodies per step): 138 us per
 // step against 155 us for a cluster of 7 blocks per two bodies running the
 // rows side by side with one cluster barrier per evaluation round; two blocks
@@ -1506,11 +1506,16 @@ constexpr int kEncTaskWarps = 4;       // warps per block
 constexpr unsigned kEncSleepMax = 256;  // longest sleep between polls, ns (2 us: waiters woke later)
 constexpr int kEncSpin = 1 << 22;      // polls of a dependency wait in a step (about two seconds)
 constexpr int kEncBlocksPerSM = 2;     // more warps lengthen every task on the shared FP64 unit
-// parts of the sources per evaluation, one task each (6, 8 and 16 parts:
-// the per-task overheads outweigh the shorter tasks)
-constexpr int kEncParts = 4;
-constexpr int kEncQ = 7 * 3 * kEncParts;  // part sums per encounter body
-// Hand-out order of the seven (row, evaluation) units of kEncParts x count
+// parts of the sources per evaluation of rows 0, 1 and 2, one task each.
+// Measured on the 2002-body disk (ms per step at ~150 / ~190 encounter
+// bodies): 3, 3, 5 parts 0.2695 / 0.2836; 4, 4, 4 0.2757 / 0.2880; 4, 4, 8
+// 0.2821 / 0.2998; 2, 2, 2 0.331 / 0.347.  Shorter tasks on the critical
+// row, longer ones (fewer per-task costs) on the filler rows.
+constexpr int kEncP0 = 3, kEncP1 = 3, kEncP2 = 5;
+__host__ __device__ constexpr int enc_parts(int row) { return row == 2 ? kEncP2 : (row == 1 ? kEncP1 : kEncP0); }
+// part sums per encounter body: 3 per part of the seven evaluations
+constexpr int kEncQ = 3 * (4 * kEncP2 + 2 * kEncP1 + kEncP0);
+// Hand-out order of the seven (row, evaluation) units of enc_parts(row) x count
 // tasks, 4 bits each (row | e << 2), every unit after the unit it depends on: the
 // critical row 2 first, the other rows' units as filler between its
 // evaluations.
@@ -1518,6 +1523,11 @@ constexpr unsigned enc_unit(int row, int e) { return (unsigned)(row | e << 2); }
 constexpr unsigned kEncOrder = enc_unit(2, 0) | enc_unit(1, 0) << 4 | enc_unit(2, 1) << 8 | enc_unit(0, 0) << 12 |
                                enc_unit(2, 2) << 16 | enc_unit(1, 1) << 20 | enc_unit(2, 3) << 24;
 __device__ __forceinline__ int enc_slot(int row, int e) { return row == 2 ? e : (row == 1 ? 4 + e : 6); }
+// first part sum of an evaluation slot within a body's kEncQ
+__device__ __forceinline__ int enc_qoff(int slot) {
+  return slot < 4 ? 3 * kEncP2 * slot
+                  : (slot < 6 ? 3 * (4 * kEncP2 + kEncP1 * (slot - 4)) : 3 * (4 * kEncP2 + 2 * kEncP1));
+}
 
 // The whole warp polls *flag >= want (one load of the same address; the
 // lanes stay converged, so no lane waits in a warp-synchronous instruction
@@ -1545,17 +1555,22 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
   griddep_enter();
   const int lane = (int)(threadIdx.x & 31);
   const int count = D.ce_count[1];
-  const int total = 7 * kEncParts * count;
+  const int total = (4 * kEncP2 + 2 * kEncP1 + kEncP0) * count;
   int* err = D.enc_head + 1;
   for (;;) {
     int t = 0;
     if (lane == 0) t = atomicAdd(D.enc_head, 1);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= total || *(volatile const int*)err) break;
-    // seven units of kEncParts x count tasks, (row, evaluation) in hand-out order
-    const int unit = t / (kEncParts * count), u = t - unit * kEncParts * count;
-    const int k = u / kEncParts, q = u % kEncParts;
+    // seven units of enc_parts(row) x count tasks, (row, evaluation) in hand-out order
+    int unit = 0, u = t;
+    while (u >= enc_parts((kEncOrder >> (4 * unit)) & 3) * count) {
+      u -= enc_parts((kEncOrder >> (4 * unit)) & 3) * count;
+      unit++;
+    }
     const int row = (kEncOrder >> (4 * unit)) & 3, e = (kEncOrder >> (4 * unit + 2)) & 3;
+    const int P = enc_parts(row);
+    const int k = u / P, q = u % P;
     const int j = D.ce_list_big[k];
     const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
     const int self = self_index(j - b0, compat_block);
@@ -1575,22 +1590,22 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
       m.z1 = {__ldcg(st + 3), __ldcg(st + 4), __ldcg(st + 5)};
       m.vel = {__ldcg(st + 6), __ldcg(st + 7), __ldcg(st + 8)};
     }
-    const int c0 = (int)((int64_t)q * nm / kEncParts), c1 = (int)((int64_t)(q + 1) * nm / kEncParts);
+    const int c0 = (int)((int64_t)q * nm / P), c1 = (int)((int64_t)(q + 1) * nm / P);
     const d3 S = warp_source_sum(D, rc_in, b0, c0, c1, self, m.z1, soft2);
-    double* qs = D.enc_q + kEncQ * (size_t)k + 3 * kEncParts * slot;
+    double* qs = D.enc_q + kEncQ * (size_t)k + enc_qoff(slot);
     int last = 0;
     if (lane == 0) {
       qs[3 * q] = S.x;
       qs[3 * q + 1] = S.y;
       qs[3 * q + 2] = S.z;
       __threadfence();
-      last = atomicAdd(cnt + slot, 1) == kEncParts - 1;
+      last = atomicAdd(cnt + slot, 1) == P - 1;
     }
     if (!__shfl_sync(0xffffffffu, last, 0)) continue;
     __threadfence();
     // last part: finish evaluation e of the row
     d3 acc = {0.0, 0.0, 0.0};
-    for (int r = 0; r < kEncParts; r++) {
+    for (int r = 0; r < P; r++) {
       acc.x += __ldcg(qs + 3 * r);
       acc.y += __ldcg(qs + 3 * r + 1);
       acc.z += __ldcg(qs + 3 * r + 2);
