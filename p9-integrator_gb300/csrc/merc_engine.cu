@@ -285,7 +285,8 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
       (st = dalloc(ctx, &ctx->d_sym, std::max(1, ctx->n_sym))) ||
       (st = dalloc(ctx, &ctx->d_sym_base, n_systems)) ||
       (st = dalloc(ctx, &D.part_sym, 2 * (size_t)sym_set)) || (st = dalloc(ctx, &D.near_mask, 2 * (size_t)(sym_set / 3))) ||
-      (st = dalloc(ctx, &D.gate, 1)) || (st = dalloc(ctx, &D.far_recomputes, 1)))
+      (st = dalloc(ctx, &D.gate, 1)) || (st = dalloc(ctx, &D.far_recomputes, 1)) ||
+      (st = dalloc(ctx, &D.far_acc, ctx->has_big ? 3 * (size_t)n : 1)))
     return st;
   {
     // encounter task kernel state (every body of a big system may be listed)
@@ -473,13 +474,14 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
              p.compat_block, p.hill_factor, ej2, last);
       nk++;
     };
-    auto reduce = [&](const double* rc_in, const int* gate, double* rc_out, int last, int massive_only, int check) {
+    auto reduce = [&](const double* rc_in, const int* gate, double* rc_out, int last, int massive_only, int check,
+                      int far_mode) {
       if (D.nsys == 1)
         launch(k_kick_reduce_sym<true>, nred, kThreads, D, rc_in, gate, rc_out, hdt, p.softening2, p.hill_factor,
-               ej2, last, massive_only, check);
+               ej2, last, massive_only, check, far_mode);
       else
         launch(k_kick_reduce_sym<false>, nred, kThreads, D, rc_in, gate, rc_out, hdt, p.softening2, p.hill_factor,
-               ej2, last, massive_only, check);
+               ej2, last, massive_only, check, far_mode);
       nk++;
     };
     // far-field pass of the massive bodies (timed as the kick kernel)
@@ -508,18 +510,18 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
           if (!first_in_graph) return MERC_OK;
           if ((st2 = far(rc_in, 0, nullptr, ev))) return st2;
           if (ctx->n_work_tp) tp_kick(rc_in, nullptr, 0);
-          reduce(rc_in, nullptr, nullptr, 0, 0, 0);
+          reduce(rc_in, nullptr, nullptr, 0, 0, 0, 0);
         } else if (last_in_graph) {
           if ((st2 = far(rc_in, 0, nullptr, ev))) return st2;
           if (ctx->n_work_tp) tp_kick(rc_in, rc_out, 1);
-          reduce(rc_in, nullptr, rc_out, 1, 0, 0);
+          reduce(rc_in, nullptr, rc_out, 1, 0, 0, 0);
         } else {
           // this kick and the next step's first kick (same positions): the
           // far field is summed once unless a far-field threshold moved
           // between them (the reduce sets the gate, the second pass runs)
           if ((st2 = far(rc_in, 0, nullptr, ev))) return st2;
           if (ctx->n_work_tp && !merge_tp) tp_kick(rc_in, rc_out, 1);
-          reduce(rc_in, nullptr, rc_out, 1, merge_tp ? 1 : 0, 1);
+          reduce(rc_in, nullptr, rc_out, 1, merge_tp ? 1 : 0, 1, 1);
           if ((st2 = far(rc_out, 1, D.gate, -1))) return st2;
           if (merge_tp) {
             // rc_out holds the next step's radii (written by the reduce)
@@ -529,7 +531,7 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
           } else if (ctx->n_work_tp) {
             tp_kick(rc_out, nullptr, 0);
           }
-          reduce(rc_out, D.gate, nullptr, 0, merge_tp ? 1 : 0, 0);
+          reduce(rc_out, D.gate, nullptr, 0, merge_tp ? 1 : 0, 0, 2);
         }
         return MERC_OK;
       } else if (ctx->has_big) {

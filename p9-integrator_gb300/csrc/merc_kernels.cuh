@@ -63,6 +63,8 @@ struct Dev {
   const long long* sym_base = nullptr;  // per system: offset of its block partials in a set (-1: none)
   long long sym_set = 0;             // doubles per partial set (the mask set has sym_set / 3 words)
   int* gate = nullptr;               // set when a merged kick must recompute the far field
+  double* far_acc = nullptr;         // 3 n: far-field sum of each massive body of a big system, kept by
+                                     //     the first reduce of a merged kick for the second
   unsigned long long* far_recomputes = nullptr;  // gated far-field passes that ran
   int* ce_list = nullptr;            // encounter bodies of small systems
   int* ce_list_big = nullptr;        // encounter bodies of big systems
@@ -934,7 +936,7 @@ constexpr int kRedBatch = MERC_RED_BATCH;  // partials loaded per thread before 
 template <bool ONE>
 __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const int* __restrict__ gate,
                                   double* __restrict__ rc_out, double hdt, double soft2, double hill,
-                                  double eject_r2, int last, int massive_only, int check) {
+                                  double eject_r2, int last, int massive_only, int check, int far_mode) {
   griddep_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = t / kRedThreads, sub = t % kRedThreads;
@@ -956,8 +958,14 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   const uint32_t* mask = nullptr;
   size_t stride = 0;
   int index = 0;
+  // far_mode 1: keep the far-field sum of each massive body in D.far_acc;
+  // 2: take it from there when the gate is clear (the far field of the
+  // second kick of a merged pair is then the first's, the same partials in
+  // the same order)
+  bool reuse = false;
   if (massive) {
     const int set = (gate && *gate) ? 1 : 0;
+    reuse = far_mode == 2 && set == 0;
     count = (nm + 31) / 32;
     base = D.part_sym + (size_t)set * D.sym_set + D.sym_base[s];
     mask = D.near_mask + (size_t)set * (D.sym_set / 3) + D.sym_base[s] / 3;
@@ -985,7 +993,16 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   uint32_t words[kRedBatch];
 #pragma unroll
   for (int u = 0; u < kRedBatch; u++) words[u] = 0u;
-  for (int b0r = sub, r = 0; b0r < count; b0r += kRedBatch * kRedThreads, r++) {
+  d3 far_j = {0.0, 0.0, 0.0};
+  if (reuse) {
+    if (sub == 0) far_j = load3(D.far_acc, n, j);
+#pragma unroll
+    for (int u = 0; u < kRedBatch; u++) {
+      const int b = sub + u * kRedThreads;
+      words[u] = b < count ? mask[(size_t)b * nm + local] : 0u;
+    }
+  }
+  for (int b0r = sub, r = 0; !reuse && b0r < count; b0r += kRedBatch * kRedThreads, r++) {
     double px[kRedBatch], py[kRedBatch], pz[kRedBatch];
 #pragma unroll
     for (int u = 0; u < kRedBatch; u++) {
@@ -1033,6 +1050,10 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   }
   if (!work || sub != 0) return;
   if (massive) {
+    if (reuse)
+      acc = far_j;
+    else if (far_mode == 1)
+      store3(D.far_acc, n, j, acc);
     acc.x += near.x;
     acc.y += near.y;
     acc.z += near.z;
