@@ -607,9 +607,12 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       // drift runs on the second branch, outside the interval)
       const bool enc_ev = ctx->time_encounter && !ctx->enc_ev.empty();
       if (enc_ev) CK(cudaEventRecordWithFlags(ctx->enc_ev[2 * step_in_graph], s, cudaEventRecordExternal));
-      if (p.bs_rows == 3)
-        launch(k_encounter_tasks, ctx->sms * kEncBlocksPerSM, 32 * kEncTaskWarps, D, rcB, p.dt, p.compat_block,
-               p.softening2, kEncSpin);
+      if (p.bs_rows == 3 && D.nsys == 1)
+        launch(k_encounter_tasks<true>, ctx->sms * kEncBlocksPerSM, 32 * kEncTaskWarps, D, rcB, p.dt,
+               p.compat_block, p.softening2, kEncSpin);
+      else if (p.bs_rows == 3)
+        launch(k_encounter_tasks<false>, ctx->sms * kEncBlocksPerSM, 32 * kEncTaskWarps, D, rcB, p.dt,
+               p.compat_block, p.softening2, kEncSpin);
       else
         launch(k_encounter_cluster, ctx->enc_blocks * 2, 32, D, rcB, p.dt, p.compat_block, p.bs_rows,
                p.softening2);
@@ -1967,7 +1970,7 @@ int merc_diag_encounter_wait(merc_ctx* ctx, int32_t* gave_up) {
   CK(cudaMemcpy(D.ce_count + 1, &one, sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(D.enc_head, head, sizeof head, cudaMemcpyHostToDevice));
   CK(cudaMemset(D.enc_cnt, 0, 11 * sizeof(int)));
-  k_encounter_tasks<<<ctx->sms * kEncBlocksPerSM, 32 * kEncTaskWarps, 0, ctx->stream>>>(
+  k_encounter_tasks<false><<<ctx->sms * kEncBlocksPerSM, 32 * kEncTaskWarps, 0, ctx->stream>>>(
       D, D.rc[ctx->rc_cur], ctx->p.dt, ctx->p.compat_block, ctx->p.softening2, 4096);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));

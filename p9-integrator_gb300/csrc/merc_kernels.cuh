@@ -1570,6 +1570,8 @@ __device__ __forceinline__ bool enc_wait(const int* flag, int want, int* err, in
   return false;
 }
 
+// ONE: a single system (no per-task system lookups)
+template <bool ONE>
 __global__ void __launch_bounds__(32 * kEncTaskWarps)
     k_encounter_tasks(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, double soft2,
                       int spin) {
@@ -1577,6 +1579,7 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
   const int lane = (int)(threadIdx.x & 31);
   const int count = D.ce_count[1];
   const int total = (4 * kEncP2 + 2 * kEncP1 + kEncP0) * count;
+  const int nm1 = ONE ? D.nm[0] : 0;
   int* err = D.enc_head + 1;
   for (;;) {
     int t = 0;
@@ -1593,7 +1596,7 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
     const int P = enc_parts(row);
     const int k = u / P, q = u % P;
     const int j = D.ce_list_big[k];
-    const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
+    const int n = D.n, s = ONE ? 0 : D.sys[j], b0 = ONE ? 0 : D.off[s], nm = ONE ? nm1 : D.nm[s];
     const int self = self_index(j - b0, compat_block);
     int* cnt = D.enc_cnt + 11 * (size_t)k;
     double* st = D.enc_st + 27 * (size_t)k + 9 * row;
