@@ -88,23 +88,32 @@ struct SrcView {
 // K-weighted kick of one body over the system's sources in the reference's
 // order (body_interaction_kick, sim.cuh:327-382).  BS selects the encounter
 // weighting (1 - K inside r_crit, sim.cuh:357-361).
+// Term of source i in kick_exact: the weighted factor wa and the separation
+// d, accumulated as acc = fma(wa, d, acc) in source order.
+template <bool BS>
+__device__ __forceinline__ double exact_term(const d3& pos, int self, const SrcView& S, int i, double soft2,
+                                             d3& d) {
+  d = {S.x[i] - pos.x, S.y[i] - pos.y, S.z[i] - pos.z};
+  double r_sq = mag2(d);
+  double r = stable_sqrt(r_sq);
+  double rc = S.rc[4 * i], rc01 = S.rc[4 * i + 1], rc09 = S.rc[4 * i + 2];
+  double notself = (double)(self != i);
+  double r_ij = notself * r;  // norm3d of d is the same sqrt of the same fma chain
+  double K = changeover_K((r_ij - rc01) / rc09);
+  double w = K;
+  if (BS) w = (double)(r <= rc) * (1.0 - K) + (double)(r > rc) * K;
+  r_sq += notself * soft2;
+  double denom = r_sq * r;
+  return w * stable_div(S.m[i], denom);
+}
+
 template <bool BS>
 __device__ __forceinline__ d3 kick_exact(const d3& pos, d3 vel, int self, const SrcView& S, int nm, double dt,
                                          double soft2) {
   d3 acc = {0.0, 0.0, 0.0};
   for (int i = 0; i < nm; i++) {
-    d3 d = {S.x[i] - pos.x, S.y[i] - pos.y, S.z[i] - pos.z};
-    double r_sq = mag2(d);
-    double r = stable_sqrt(r_sq);
-    double rc = S.rc[4 * i], rc01 = S.rc[4 * i + 1], rc09 = S.rc[4 * i + 2];
-    double notself = (double)(self != i);
-    double r_ij = notself * r;  // norm3d of d is the same sqrt of the same fma chain
-    double K = changeover_K((r_ij - rc01) / rc09);
-    double w = K;
-    if (BS) w = (double)(r <= rc) * (1.0 - K) + (double)(r > rc) * K;
-    r_sq += notself * soft2;
-    double denom = r_sq * r;
-    double wa = w * stable_div(S.m[i], denom);
+    d3 d;
+    const double wa = exact_term<BS>(pos, self, S, i, soft2, d);
     acc.x = fma(wa, d.x, acc.x);
     acc.y = fma(wa, d.y, acc.y);
     acc.z = fma(wa, d.z, acc.z);
@@ -115,15 +124,57 @@ __device__ __forceinline__ d3 kick_exact(const d3& pos, d3 vel, int self, const 
   return vel;
 }
 
+// kick_exact by one warp (every lane calls it with the same arguments and
+// gets the same result): the terms of 32 sources at a time on the 32 lanes,
+// staged in shared memory (4 x 32 doubles per warp), then accumulated in
+// source order by lanes 0-2, one component each, with the same fma chain,
+// so the bits are those of kick_exact.
+template <bool BS>
+__device__ __forceinline__ d3 warp_kick_exact(const d3& pos, d3 vel, int self, const SrcView& S, int nm, double dt,
+                                              double soft2, double* stage) {
+  const int lane = (int)(threadIdx.x & 31);
+  double acc = 0.0;  // lane c < 3: component c
+  for (int base = 0; base < nm; base += 32) {
+    const int i = base + lane;
+    d3 d = {0.0, 0.0, 0.0};
+    const double wa = i < nm ? exact_term<BS>(pos, self, S, i, soft2, d) : 0.0;
+    stage[lane] = wa;
+    stage[32 + lane] = d.x;
+    stage[64 + lane] = d.y;
+    stage[96 + lane] = d.z;
+    __syncwarp();
+    if (lane < 3) {
+      const int cnt = min(32, nm - base);
+      const double* dc = stage + 32 * (lane + 1);
+      for (int k = 0; k < cnt; k++) acc = fma(stage[k], dc[k], acc);
+    }
+    __syncwarp();
+  }
+  const double ax = __shfl_sync(0xffffffffu, acc, 0), ay = __shfl_sync(0xffffffffu, acc, 1),
+               az = __shfl_sync(0xffffffffu, acc, 2);
+  vel.x = fma(ax, dt, vel.x);
+  vel.y = fma(ay, dt, vel.y);
+  vel.z = fma(az, dt, vel.z);
+  return vel;
+}
+
 // close_encounter_p, sim.cuh:589-613
+__device__ __forceinline__ bool ce_pair(const d3& pos, int self, const SrcView& S, int i) {
+  d3 d = {S.x[i] - pos.x, S.y[i] - pos.y, S.z[i] - pos.z};
+  double mag = sqrt(mag2(d));
+  return (mag < S.rc[4 * i]) && (self != i);
+}
 __device__ __forceinline__ bool close_encounter(const d3& pos, int self, const SrcView& S, int nm) {
   bool ce = false;
-  for (int i = 0; i < nm; i++) {
-    d3 d = {S.x[i] - pos.x, S.y[i] - pos.y, S.z[i] - pos.z};
-    double mag = sqrt(mag2(d));
-    ce = ce || ((mag < S.rc[4 * i]) && (self != i));
-  }
+  for (int i = 0; i < nm; i++) ce = ce || ce_pair(pos, self, S, i);
   return ce;
+}
+// the same test by one warp (the sources split over the lanes; an OR does
+// not depend on the order)
+__device__ __forceinline__ bool warp_close_encounter(const d3& pos, int self, const SrcView& S, int nm) {
+  bool ce = false;
+  for (int i = (int)(threadIdx.x & 31); i < nm; i += 32) ce = ce || ce_pair(pos, self, S, i);
+  return __any_sync(0xffffffffu, ce);
 }
 
 // ---- Kepler's equation, Danby/Burkardt, fixed iterations: sim.cuh:90-126 ----
@@ -256,12 +307,17 @@ __device__ __forceinline__ Elem elem_from_cart(const d3& p, const d3& v) {
 // 443) is a functor so the same Richardson scheme runs with the exact pair
 // sum of the reference order (ExactVelTotal) or with the parallel fast sums of
 // the universal path.
+// WARP: the source sum by one warp (warp_kick_exact; `stage` is its shared
+// memory), otherwise by one thread (kick_exact)
+template <bool WARP = false>
 struct ExactVelTotal {
   const SrcView* S;
   int nm, self;
   double soft2;
+  double* stage = nullptr;
   __device__ __forceinline__ d3 operator()(const d3& pos, const d3& vel, double dt) const {
-    d3 nv = kick_exact<true>(pos, vel, self, *S, nm, dt, soft2);
+    d3 nv = WARP ? warp_kick_exact<true>(pos, vel, self, *S, nm, dt, soft2, stage)
+                 : kick_exact<true>(pos, vel, self, *S, nm, dt, soft2);
     double r_sq = mag2(pos);
     double r = stable_sqrt(r_sq);
     r_sq += soft2;

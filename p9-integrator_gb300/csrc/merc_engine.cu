@@ -441,20 +441,36 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
   int st;
   if (p.drift == MERC_DRIFT_ELEMENTS) {
     // exact path: the reference operation order for every system
+    // the bodies of big systems by one warp each (same bits, same order)
+    const int bx = ctx->has_big ? 1 : 0;
+    const unsigned nbx =
+        (unsigned)std::min<int64_t>((D.n + kExactWarps - 1) / kExactWarps, (int64_t)ctx->sms * 16);
+    auto kick_exact_all = [&](const double* rc_in, double* rc_out, int last) {
+      k_kick<<<nb, kThreads, 0, s>>>(D, rc_in, rc_out, hdt, p.softening2, p.compat_block, p.hill_factor, ej2, last,
+                                     bx);
+      if (bx)
+        k_kick_big_exact<<<nbx, 32 * kExactWarps, 0, s>>>(D, rc_in, rc_out, hdt, p.softening2, p.compat_block,
+                                                          p.hill_factor, ej2, last);
+    };
     if ((st = kick_ev(0))) return st;
-    k_kick<<<nb, kThreads, 0, s>>>(D, rcA, nullptr, hdt, p.softening2, p.compat_block, p.hill_factor, ej2, 0);
+    kick_exact_all(rcA, nullptr, 0);
     if ((st = kick_ev(1))) return st;
     k_momentum<<<sb, kThreads, 0, s>>>(D, D.v, 0);
     k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt);
     CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
-    k_drift_elements<<<nb, kThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.kepler_iters);
-    k_encounter_elements<<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2);
+    if (bx) k_ce_big_exact<<<nbx, 32 * kExactWarps, 0, s>>>(D, rcB, p.compat_block);
+    k_drift_elements<<<nb, kThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.kepler_iters, bx);
+    k_encounter_elements<<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2,
+                                                         bx);
+    if (bx)
+      k_encounter_big_exact<<<ctx->sms * 4, 32 * kExactWarps, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
+                                                                      p.softening2);
     k_momentum<<<sb, kThreads, 0, s>>>(D, D.vo, 0);
     k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.xo, D.vo, rcB, hdt);
     if ((st = kick_ev(2))) return st;
-    k_kick<<<nb, kThreads, 0, s>>>(D, rcB, rcA, hdt, p.softening2, p.compat_block, p.hill_factor, ej2, 1);
+    kick_exact_all(rcB, rcA, 1);
     if ((st = kick_ev(3))) return st;
-    nk = 8;
+    nk = 8 + 4 * bx;
   } else {
     // programmatic dependent launches: a kernel may be scheduled while its
     // predecessor finishes; every kernel here waits for it (griddep_wait)

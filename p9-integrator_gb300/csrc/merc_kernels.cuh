@@ -237,17 +237,55 @@ __global__ void k_rc(Dev D, double* rc_out, double hill) {
 // ---------------------------------------------------------------------------
 // exact path (element drift): reference operation order
 // ---------------------------------------------------------------------------
-// Half kick of every body (sim.cuh:683-685, 739-741).
+// Half kick of every body (sim.cuh:683-685, 739-741); skip_big leaves the
+// bodies of big systems to k_kick_big_exact.
 __global__ void k_kick(Dev D, const double* __restrict__ rc_in, double* __restrict__ rc_out, double hdt,
-                       double soft2, int compat_block, double hill, double eject_r2, int last) {
+                       double soft2, int compat_block, double hill, double eject_r2, int last, int skip_big) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= D.n) return;
   const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
+  if (skip_big && D.big[s]) return;
   const int local = j - b0;
   SrcView S = src_view(D, rc_in, b0);
   d3 pos = load3(D.x, n, j);
   d3 vel = kick_exact<false>(pos, load3(D.v, n, j), self_index(local, compat_block), S, nm, hdt, soft2);
   kick_epilogue(D, j, local, nm, pos, vel, rc_out, hill, eject_r2, last);
+}
+
+// The exact path of the big systems, one warp per body (warp_kick_exact and
+// warp_close_encounter give the bits of the per-thread forms): the same
+// arithmetic and order, with the source terms computed 32 at a time.
+constexpr int kExactWarps = 4;  // warps per block
+__global__ void __launch_bounds__(32 * kExactWarps)
+    k_kick_big_exact(Dev D, const double* __restrict__ rc_in, double* __restrict__ rc_out, double hdt,
+                     double soft2, int compat_block, double hill, double eject_r2, int last) {
+  __shared__ double stage[kExactWarps][128];
+  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
+  for (int j = blockIdx.x * kExactWarps + warp; j < D.n; j += gridDim.x * kExactWarps) {
+    const int n = D.n, s = D.sys[j];
+    if (!D.big[s]) continue;
+    const int b0 = D.off[s], nm = D.nm[s], local = j - b0;
+    SrcView S = src_view(D, rc_in, b0);
+    const d3 pos = load3(D.x, n, j);
+    const d3 vel = warp_kick_exact<false>(pos, load3(D.v, n, j), self_index(local, compat_block), S, nm, hdt,
+                                          soft2, stage[warp]);
+    if (lane == 0) kick_epilogue(D, j, local, nm, pos, vel, rc_out, hill, eject_r2, last);
+  }
+}
+
+// Encounter flags of the bodies of big systems (close_encounter_p,
+// sim.cuh:589-613), one warp per body, for k_drift_elements.
+__global__ void __launch_bounds__(32 * kExactWarps) k_ce_big_exact(Dev D, const double* __restrict__ rc_in,
+                                                                   int compat_block) {
+  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
+  for (int j = blockIdx.x * kExactWarps + warp; j < D.n; j += gridDim.x * kExactWarps) {
+    const int n = D.n, s = D.sys[j];
+    if (!D.big[s]) continue;
+    const int b0 = D.off[s], nm = D.nm[s];
+    SrcView S = src_view(D, rc_in, b0);
+    const bool ce = warp_close_encounter(load3(D.x, n, j), self_index(j - b0, compat_block), S, nm);
+    if (lane == 0) D.ce[j] = ce;
+  }
 }
 
 // sum_i m_i v_i of each system in the reference order (main_body_kinetic,
@@ -515,8 +553,9 @@ __device__ __forceinline__ void append_ce(bool flag, int j, int* list, int* coun
 // (sim.cuh:692-713).  Bodies in encounter are appended to the encounter list;
 // every body writes its Kepler result to xo/vo (for encounter bodies it enters
 // the blend fma(0, kep, bs) of sim.cuh:718-730, completed by k_encounter).
+// ce_big: the flags of big systems' bodies were set by k_ce_big_exact.
 __global__ void k_drift_elements(Dev D, const double* __restrict__ rc_in, double dt, int compat_block,
-                                 int kep_iters) {
+                                 int kep_iters, int ce_big) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   bool is_ce = false;
   if (j < D.n) {
@@ -524,8 +563,12 @@ __global__ void k_drift_elements(Dev D, const double* __restrict__ rc_in, double
     const int self = self_index(j - b0, compat_block);
     SrcView S = src_view(D, rc_in, b0);
     d3 pos = load3(D.x, n, j), vel = load3(D.v, n, j);
-    is_ce = close_encounter(pos, self, S, nm);
-    D.ce[j] = is_ce;
+    if (ce_big && D.big[s]) {
+      is_ce = D.ce[j] != 0;
+    } else {
+      is_ce = close_encounter(pos, self, S, nm);
+      D.ce[j] = is_ce;
+    }
     const double tp = 6.283185307179586476925286766559005768394338798750211641949;
     double a = D.alag[j];
     double nmot = rsqrt_ieee(a * a * a);  // mean motion of the previous elements (sim.cuh:692)
@@ -541,22 +584,47 @@ __global__ void k_drift_elements(Dev D, const double* __restrict__ rc_in, double
 
 // Encounter sub-step (Richardson extrapolation of modified-midpoint steps
 // against sources frozen at the start of the drift, sim.cuh:701-702) in the
-// reference order; one thread per listed body, grid-stride.
+// reference order; one thread per listed body, grid-stride.  skip_big leaves
+// the bodies of big systems to k_encounter_big_exact.
+__device__ __forceinline__ void encounter_elements_store(const Dev& D, int j, PV bs) {
+  const int n = D.n;
+  d3 kp = load3(D.xo, n, j), kv = load3(D.vo, n, j);
+  bs.pos = {fma(0.0, kp.x, bs.pos.x), fma(0.0, kp.y, bs.pos.y), fma(0.0, kp.z, bs.pos.z)};
+  bs.vel = {fma(0.0, kv.x, bs.vel.x), fma(0.0, kv.y, bs.vel.y), fma(0.0, kv.z, bs.vel.z)};
+  store3(D.xo, n, j, bs.pos);
+  store3(D.vo, n, j, bs.vel);
+}
 __global__ void k_encounter_elements(Dev D, const double* __restrict__ rc_in, double dt, int compat_block,
-                                     int rows, double soft2) {
+                                     int rows, double soft2, int skip_big) {
   const int count = D.ce_count[0];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
     const int j = D.ce_list[k];
     const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
+    if (skip_big && D.big[s]) continue;
     SrcView S = src_view(D, rc_in, b0);
-    ExactVelTotal vt{&S, nm, self_index(j - b0, compat_block), soft2};
+    ExactVelTotal<false> vt{&S, nm, self_index(j - b0, compat_block), soft2};
     PV c = {load3(D.x, n, j), load3(D.v, n, j)};
-    PV bs = richardson(c, vt, dt, rows);
-    d3 kp = load3(D.xo, n, j), kv = load3(D.vo, n, j);
-    bs.pos = {fma(0.0, kp.x, bs.pos.x), fma(0.0, kp.y, bs.pos.y), fma(0.0, kp.z, bs.pos.z)};
-    bs.vel = {fma(0.0, kv.x, bs.vel.x), fma(0.0, kv.y, bs.vel.y), fma(0.0, kv.z, bs.vel.z)};
-    store3(D.xo, n, j, bs.pos);
-    store3(D.vo, n, j, bs.vel);
+    encounter_elements_store(D, j, richardson(c, vt, dt, rows));
+  }
+}
+// The same for the listed bodies of big systems, one warp per body (every
+// lane runs the Richardson scheme on the same values; warp_kick_exact sums
+// the sources).
+__global__ void __launch_bounds__(32 * kExactWarps)
+    k_encounter_big_exact(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, int rows,
+                          double soft2) {
+  __shared__ double stage[kExactWarps][128];
+  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
+  const int count = D.ce_count[0];
+  for (int k = blockIdx.x * kExactWarps + warp; k < count; k += gridDim.x * kExactWarps) {
+    const int j = D.ce_list[k];
+    const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
+    if (!D.big[s]) continue;
+    SrcView S = src_view(D, rc_in, b0);
+    ExactVelTotal<true> vt{&S, nm, self_index(j - b0, compat_block), soft2, stage[warp]};
+    PV c = {load3(D.x, n, j), load3(D.v, n, j)};
+    const PV bs = richardson(c, vt, dt, rows);
+    if (lane == 0) encounter_elements_store(D, j, bs);
   }
 }
 
