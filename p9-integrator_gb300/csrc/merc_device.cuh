@@ -99,7 +99,16 @@ __device__ __forceinline__ double exact_term(const d3& pos, int self, const SrcV
   double rc = S.rc[4 * i], rc01 = S.rc[4 * i + 1], rc09 = S.rc[4 * i + 2];
   double notself = (double)(self != i);
   double r_ij = notself * r;  // norm3d of d is the same sqrt of the same fma chain
-  double K = changeover_K((r_ij - rc01) / rc09);
+  // K = changeover_K(y), y = (r_ij - rc01) / rc09.  Without the division
+  // where y is certainly in (1, DBL_MAX), i.e. K = 1: with b = rc09 normal
+  // and t > fl(b (1 + 2^-51)) >= b (1 + 2^-52), t / b > 1 + 2^-52 rounds to
+  // a double > 1; t < fl(b 1e300) keeps it finite.
+  const double t = r_ij - rc01;
+  double K;
+  if (rc09 >= 0x1p-1000 && t > rc09 * (1.0 + 0x1p-51) && t < rc09 * 1e300)
+    K = 1.0;
+  else
+    K = changeover_K(t / rc09);
   double w = K;
   if (BS) w = (double)(r <= rc) * (1.0 - K) + (double)(r > rc) * K;
   r_sq += notself * soft2;
