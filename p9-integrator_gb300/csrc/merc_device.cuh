@@ -316,17 +316,53 @@ __device__ __forceinline__ Elem elem_from_cart(const d3& p, const d3& v) {
 // 443) is a functor so the same Richardson scheme runs with the exact pair
 // sum of the reference order (ExactVelTotal) or with the parallel fast sums of
 // the universal path.
-// WARP: the source sum by one warp (warp_kick_exact; `stage` is its shared
-// memory), otherwise by one thread (kick_exact)
-template <bool WARP = false>
+// kick_exact by one block of NT threads (every thread calls it with the same
+// arguments and gets the same result): the terms of NT sources at a time,
+// staged in shared memory (2 x 4 x NT + 3 doubles, two buffers so that the
+// next chunk's terms are computed while threads 0-2 add the current one in
+// source order with the reference's fma chain, one component each).
+template <bool BS, int NT>
+__device__ __forceinline__ d3 block_kick_exact(const d3& pos, d3 vel, int self, const SrcView& S, int nm, double dt,
+                                               double soft2, double* stage) {
+  const int tid = (int)threadIdx.x;
+  double acc = 0.0;  // thread c < 3: component c
+  for (int base = 0, c = 0; base < nm; base += NT, c ^= 1) {
+    double* buf = stage + 4 * NT * c;
+    const int i = base + tid;
+    d3 d = {0.0, 0.0, 0.0};
+    const double wa = i < nm ? exact_term<BS>(pos, self, S, i, soft2, d) : 0.0;
+    buf[tid] = wa;
+    buf[NT + tid] = d.x;
+    buf[2 * NT + tid] = d.y;
+    buf[3 * NT + tid] = d.z;
+    // this chunk's terms are visible, and the previous chunk's additions
+    // (which read the other buffer) are done
+    __syncthreads();
+    if (tid < 3) {
+      const int cnt = min(NT, nm - base);
+      const double* dc = buf + NT * (tid + 1);
+      for (int k = 0; k < cnt; k++) acc = fma(buf[k], dc[k], acc);
+    }
+  }
+  if (tid < 3) stage[8 * NT + tid] = acc;
+  __syncthreads();
+  vel.x = fma(stage[8 * NT], dt, vel.x);
+  vel.y = fma(stage[8 * NT + 1], dt, vel.y);
+  vel.z = fma(stage[8 * NT + 2], dt, vel.z);
+  return vel;
+}
+
+// NT = 1: the source sum by one thread (kick_exact); NT > 1: by a block of
+// NT threads (block_kick_exact; `stage` is its shared memory)
+template <int NT = 1>
 struct ExactVelTotal {
   const SrcView* S;
   int nm, self;
   double soft2;
   double* stage = nullptr;
   __device__ __forceinline__ d3 operator()(const d3& pos, const d3& vel, double dt) const {
-    d3 nv = WARP ? warp_kick_exact<true>(pos, vel, self, *S, nm, dt, soft2, stage)
-                 : kick_exact<true>(pos, vel, self, *S, nm, dt, soft2);
+    d3 nv = NT > 1 ? block_kick_exact<true, (NT > 1 ? NT : 32)>(pos, vel, self, *S, nm, dt, soft2, stage)
+                   : kick_exact<true>(pos, vel, self, *S, nm, dt, soft2);
     double r_sq = mag2(pos);
     double r = stable_sqrt(r_sq);
     r_sq += soft2;

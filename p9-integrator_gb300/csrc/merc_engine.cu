@@ -455,7 +455,13 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     if ((st = kick_ev(0))) return st;
     kick_exact_all(rcA, nullptr, 0);
     if ((st = kick_ev(1))) return st;
-    k_momentum<<<sb, kThreads, 0, s>>>(D, D.v, 0);
+    auto momentum_exact = [&](const double* vsrc) {
+      k_momentum<<<sb, kThreads, 0, s>>>(D, vsrc, bx);
+      if (bx)
+        k_momentum_big_exact<<<(unsigned)((D.nsys + kExactWarps - 1) / kExactWarps), 32 * kExactWarps, 0, s>>>(
+            D, vsrc);
+    };
+    momentum_exact(D.v);
     k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt);
     CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
     if (bx) k_ce_big_exact<<<nbx, 32 * kExactWarps, 0, s>>>(D, rcB, p.compat_block);
@@ -463,14 +469,14 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     k_encounter_elements<<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2,
                                                          bx);
     if (bx)
-      k_encounter_big_exact<<<ctx->sms * 4, 32 * kExactWarps, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
-                                                                      p.softening2);
-    k_momentum<<<sb, kThreads, 0, s>>>(D, D.vo, 0);
+      k_encounter_big_exact<<<ctx->sms * 2, kExactBlock, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
+                                                                 p.softening2);
+    momentum_exact(D.vo);
     k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.xo, D.vo, rcB, hdt);
     if ((st = kick_ev(2))) return st;
     kick_exact_all(rcB, rcA, 1);
     if ((st = kick_ev(3))) return st;
-    nk = 8 + 4 * bx;
+    nk = 8 + 6 * bx;
   } else {
     // programmatic dependent launches: a kernel may be scheduled while its
     // predecessor finishes; every kernel here waits for it (griddep_wait)

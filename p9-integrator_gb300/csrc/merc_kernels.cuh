@@ -288,6 +288,51 @@ __global__ void __launch_bounds__(32 * kExactWarps) k_ce_big_exact(Dev D, const 
   }
 }
 
+// sum_i m_i v_i of each big system in the reference order (main_body_kinetic,
+// sim.cuh:394-399), one warp per system: the masses and velocities of 32
+// bodies loaded at a time (the next chunk's loads issued before the current
+// chunk is added), added in body order by lanes 0-2 with the reference's fma
+// chain, one component each.
+__global__ void __launch_bounds__(32 * kExactWarps) k_momentum_big_exact(Dev D, const double* __restrict__ vsrc) {
+  __shared__ double stage[kExactWarps][128];
+  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
+  double* st = stage[warp];
+  for (int s = blockIdx.x * kExactWarps + warp; s < D.nsys; s += gridDim.x * kExactWarps) {
+    if (!D.big[s]) continue;
+    const int b0 = D.off[s], nm = D.nm[s], n = D.n;
+    double acc = 0.0;  // lane c < 3: component c
+    double m = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
+    if (lane < nm) {
+      m = D.m[b0 + lane];
+      vx = vsrc[b0 + lane];
+      vy = vsrc[n + b0 + lane];
+      vz = vsrc[2 * n + b0 + lane];
+    }
+    for (int base = 0; base < nm; base += 32) {
+      st[lane] = m;
+      st[32 + lane] = vx;
+      st[64 + lane] = vy;
+      st[96 + lane] = vz;
+      __syncwarp();
+      const int i = base + 32 + lane;
+      m = vx = vy = vz = 0.0;
+      if (i < nm) {
+        m = D.m[b0 + i];
+        vx = vsrc[b0 + i];
+        vy = vsrc[n + b0 + i];
+        vz = vsrc[2 * n + b0 + i];
+      }
+      if (lane < 3) {
+        const int cnt = min(32, nm - base);
+        const double* vc = st + 32 * (lane + 1);
+        for (int k = 0; k < cnt; k++) acc = fma(st[k], vc[k], acc);
+      }
+      __syncwarp();
+    }
+    if (lane < 3) D.P[3 * s + lane] = acc;
+  }
+}
+
 // sum_i m_i v_i of each system in the reference order (main_body_kinetic,
 // sim.cuh:394-399); `vsrc` is the velocity array to sum.  skip_big leaves the
 // big systems to k_momentum_big.
@@ -602,29 +647,29 @@ __global__ void k_encounter_elements(Dev D, const double* __restrict__ rc_in, do
     const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
     if (skip_big && D.big[s]) continue;
     SrcView S = src_view(D, rc_in, b0);
-    ExactVelTotal<false> vt{&S, nm, self_index(j - b0, compat_block), soft2};
+    ExactVelTotal<1> vt{&S, nm, self_index(j - b0, compat_block), soft2};
     PV c = {load3(D.x, n, j), load3(D.v, n, j)};
     encounter_elements_store(D, j, richardson(c, vt, dt, rows));
   }
 }
-// The same for the listed bodies of big systems, one warp per body (every
-// lane runs the Richardson scheme on the same values; warp_kick_exact sums
+// The same for the listed bodies of big systems, one block per body (every
+// thread runs the Richardson scheme on the same values; block_kick_exact sums
 // the sources).
-__global__ void __launch_bounds__(32 * kExactWarps)
+constexpr int kExactBlock = 256;
+__global__ void __launch_bounds__(kExactBlock)
     k_encounter_big_exact(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, int rows,
                           double soft2) {
-  __shared__ double stage[kExactWarps][128];
-  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
+  __shared__ double stage[8 * kExactBlock + 3];
   const int count = D.ce_count[0];
-  for (int k = blockIdx.x * kExactWarps + warp; k < count; k += gridDim.x * kExactWarps) {
+  for (int k = blockIdx.x; k < count; k += gridDim.x) {
     const int j = D.ce_list[k];
     const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
     if (!D.big[s]) continue;
     SrcView S = src_view(D, rc_in, b0);
-    ExactVelTotal<true> vt{&S, nm, self_index(j - b0, compat_block), soft2, stage[warp]};
+    ExactVelTotal<kExactBlock> vt{&S, nm, self_index(j - b0, compat_block), soft2, stage};
     PV c = {load3(D.x, n, j), load3(D.v, n, j)};
     const PV bs = richardson(c, vt, dt, rows);
-    if (lane == 0) encounter_elements_store(D, j, bs);
+    if (threadIdx.x == 0) encounter_elements_store(D, j, bs);
   }
 }
 
