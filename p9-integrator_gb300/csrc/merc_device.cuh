@@ -133,6 +133,20 @@ __device__ __forceinline__ d3 kick_exact(const d3& pos, d3 vel, int self, const 
   return vel;
 }
 
+// acc = fma(a[k], b[k], acc) for k = 0..cnt-1 in order (cnt <= NT); a full
+// chunk in unrolled blocks, so the shared-memory loads run ahead of the fma
+// chain
+template <int NT>
+__device__ __forceinline__ double chain_fma(const double* a, const double* b, int cnt, double acc) {
+  if (cnt == NT) {
+#pragma unroll 16
+    for (int k = 0; k < NT; k++) acc = fma(a[k], b[k], acc);
+  } else {
+    for (int k = 0; k < cnt; k++) acc = fma(a[k], b[k], acc);
+  }
+  return acc;
+}
+
 // kick_exact by one warp (every lane calls it with the same arguments and
 // gets the same result): the terms of 32 sources at a time on the 32 lanes,
 // staged in shared memory (4 x 32 doubles per warp), then accumulated in
@@ -155,7 +169,7 @@ __device__ __forceinline__ d3 warp_kick_exact(const d3& pos, d3 vel, int self, c
     if (lane < 3) {
       const int cnt = min(32, nm - base);
       const double* dc = stage + 32 * (lane + 1);
-      for (int k = 0; k < cnt; k++) acc = fma(stage[k], dc[k], acc);
+      acc = chain_fma<32>(stage, dc, cnt, acc);
     }
     __syncwarp();
   }
@@ -316,15 +330,18 @@ __device__ __forceinline__ Elem elem_from_cart(const d3& p, const d3& v) {
 // 443) is a functor so the same Richardson scheme runs with the exact pair
 // sum of the reference order (ExactVelTotal) or with the parallel fast sums of
 // the universal path.
-// kick_exact by one block of NT threads (every thread calls it with the same
-// arguments and gets the same result): the terms of NT sources at a time,
-// staged in shared memory (2 x 4 x NT + 3 doubles, two buffers so that the
-// next chunk's terms are computed while threads 0-2 add the current one in
-// source order with the reference's fma chain, one component each).
+// kick_exact by a group of NT threads (threads tid = 0..NT-1 of named barrier
+// `bar`; every thread of the group calls it with the same arguments and gets
+// the same result): the terms of NT sources at a time, staged in shared
+// memory (2 x 4 x NT + 3 doubles, two buffers so that the next chunk's terms
+// are computed while threads 0-2 add the current one in source order with
+// the reference's fma chain, one component each).
+__device__ __forceinline__ void group_sync(int bar, int nt) {
+  asm volatile("bar.sync %0, %1;" : : "r"(bar), "r"(nt) : "memory");
+}
 template <bool BS, int NT>
-__device__ __forceinline__ d3 block_kick_exact(const d3& pos, d3 vel, int self, const SrcView& S, int nm, double dt,
-                                               double soft2, double* stage) {
-  const int tid = (int)threadIdx.x;
+__device__ __forceinline__ d3 group_kick_exact(const d3& pos, d3 vel, int self, const SrcView& S, int nm, double dt,
+                                               double soft2, double* stage, int tid, int bar) {
   double acc = 0.0;  // thread c < 3: component c
   for (int base = 0, c = 0; base < nm; base += NT, c ^= 1) {
     double* buf = stage + 4 * NT * c;
@@ -337,31 +354,29 @@ __device__ __forceinline__ d3 block_kick_exact(const d3& pos, d3 vel, int self, 
     buf[3 * NT + tid] = d.z;
     // this chunk's terms are visible, and the previous chunk's additions
     // (which read the other buffer) are done
-    __syncthreads();
-    if (tid < 3) {
-      const int cnt = min(NT, nm - base);
-      const double* dc = buf + NT * (tid + 1);
-      for (int k = 0; k < cnt; k++) acc = fma(buf[k], dc[k], acc);
-    }
+    group_sync(bar, NT);
+    if (tid < 3) acc = chain_fma<NT>(buf, buf + NT * (tid + 1), min(NT, nm - base), acc);
   }
   if (tid < 3) stage[8 * NT + tid] = acc;
-  __syncthreads();
+  group_sync(bar, NT);
   vel.x = fma(stage[8 * NT], dt, vel.x);
   vel.y = fma(stage[8 * NT + 1], dt, vel.y);
   vel.z = fma(stage[8 * NT + 2], dt, vel.z);
   return vel;
 }
 
-// NT = 1: the source sum by one thread (kick_exact); NT > 1: by a block of
-// NT threads (block_kick_exact; `stage` is its shared memory)
+// NT = 1: the source sum by one thread (kick_exact); NT > 1: by a group of
+// NT threads (group_kick_exact; `stage` is its shared memory, tid the
+// thread's index in the group, bar its named barrier)
 template <int NT = 1>
 struct ExactVelTotal {
   const SrcView* S;
   int nm, self;
   double soft2;
   double* stage = nullptr;
+  int tid = 0, bar = 0;
   __device__ __forceinline__ d3 operator()(const d3& pos, const d3& vel, double dt) const {
-    d3 nv = NT > 1 ? block_kick_exact<true, (NT > 1 ? NT : 32)>(pos, vel, self, *S, nm, dt, soft2, stage)
+    d3 nv = NT > 1 ? group_kick_exact<true, (NT > 1 ? NT : 32)>(pos, vel, self, *S, nm, dt, soft2, stage, tid, bar)
                    : kick_exact<true>(pos, vel, self, *S, nm, dt, soft2);
     double r_sq = mag2(pos);
     double r = stable_sqrt(r_sq);
@@ -404,6 +419,23 @@ __device__ __forceinline__ void rich_combine(PV& o, const PV& a, const PV& q, do
   double den = p4 - 1.0;
   o.pos = {fma(p4, a.pos.x, -q.pos.x) / den, fma(p4, a.pos.y, -q.pos.y) / den, fma(p4, a.pos.z, -q.pos.z) / den};
   o.vel = {fma(p4, a.vel.x, -q.vel.x) / den, fma(p4, a.vel.y, -q.vel.y) / den, fma(p4, a.vel.z, -q.vel.z) / den};
+}
+
+// The Richardson tableau of richardson() from its rows' modified-midpoint
+// results (row i: N = 2^i), in the same order of operations.
+__device__ __forceinline__ PV richardson_of_rows(const PV* row, int rows) {
+  PV prev[4], cur[4];
+  prev[0] = row[0];
+  for (int i = 1; i < rows; i++) {
+    cur[0] = row[i];
+    double p4 = 1.0;
+    for (int j = 1; j <= i; j++) {
+      p4 *= 4.0;
+      rich_combine(cur[j], cur[j - 1], prev[j - 1], p4);
+    }
+    for (int j = 0; j <= i; j++) prev[j] = cur[j];
+  }
+  return prev[rows - 1];
 }
 
 // Richardson extrapolation over modified-midpoint steps N = 1, 2, 4, ...

@@ -469,8 +469,8 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     k_encounter_elements<<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2,
                                                          bx);
     if (bx)
-      k_encounter_big_exact<<<ctx->sms * 2, kExactBlock, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows,
-                                                                 p.softening2);
+      k_encounter_big_exact<<<ctx->sms, kExactRowThreads * p.bs_rows, 0, s>>>(D, rcB, p.dt, p.compat_block,
+                                                                              p.bs_rows, p.softening2);
     momentum_exact(D.vo);
     k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.xo, D.vo, rcB, hdt);
     if ((st = kick_ev(2))) return st;

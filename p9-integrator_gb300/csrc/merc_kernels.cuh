@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(32 * kExactWarps) k_momentum_big_exact(Dev D, 
       if (lane < 3) {
         const int cnt = min(32, nm - base);
         const double* vc = st + 32 * (lane + 1);
-        for (int k = 0; k < cnt; k++) acc = fma(st[k], vc[k], acc);
+        acc = chain_fma<32>(st, vc, cnt, acc);
       }
       __syncwarp();
     }
@@ -652,24 +652,31 @@ __global__ void k_encounter_elements(Dev D, const double* __restrict__ rc_in, do
     encounter_elements_store(D, j, richardson(c, vt, dt, rows));
   }
 }
-// The same for the listed bodies of big systems, one block per body (every
-// thread runs the Richardson scheme on the same values; block_kick_exact sums
-// the sources).
-constexpr int kExactBlock = 256;
-__global__ void __launch_bounds__(kExactBlock)
+// The same for the listed bodies of big systems, one block per body and one
+// group of kExactRowThreads threads per Richardson row, the rows side by side
+// (each group runs its row's modified midpoint; group_kick_exact sums the
+// sources with the group's named barrier); thread 0 combines the rows as
+// richardson() does.  Launched with kExactRowThreads x rows threads.
+constexpr int kExactRowThreads = 128;
+__global__ void __launch_bounds__(4 * kExactRowThreads)
     k_encounter_big_exact(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, int rows,
                           double soft2) {
-  __shared__ double stage[8 * kExactBlock + 3];
+  __shared__ double stage[4][8 * kExactRowThreads + 3];
+  __shared__ PV res[4];
+  const int g = (int)threadIdx.x / kExactRowThreads, tid = (int)threadIdx.x % kExactRowThreads;
   const int count = D.ce_count[0];
   for (int k = blockIdx.x; k < count; k += gridDim.x) {
     const int j = D.ce_list[k];
     const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
     if (!D.big[s]) continue;
     SrcView S = src_view(D, rc_in, b0);
-    ExactVelTotal<kExactBlock> vt{&S, nm, self_index(j - b0, compat_block), soft2, stage};
+    ExactVelTotal<kExactRowThreads> vt{&S, nm, self_index(j - b0, compat_block), soft2, stage[g], tid, 1 + g};
     PV c = {load3(D.x, n, j), load3(D.v, n, j)};
-    const PV bs = richardson(c, vt, dt, rows);
-    if (threadIdx.x == 0) encounter_elements_store(D, j, bs);
+    const PV r = mod_midpoint(c, vt, dt, 1 << g);
+    if (tid == 0) res[g] = r;
+    __syncthreads();
+    if (threadIdx.x == 0) encounter_elements_store(D, j, richardson_of_rows(res, rows));
+    __syncthreads();  // res is rewritten for the next body
   }
 }
 

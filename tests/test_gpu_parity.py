@@ -81,6 +81,18 @@ def test_elements_embryo_disk_bitwise(oracle):
     assert np.array_equal(st.vel, ov)
 
 
+@pytest.mark.parametrize("rows", [1, 2, 4])
+def test_elements_richardson_rows_bitwise(oracle, rows):
+    """The exact path's encounter sub-step with 1, 2 and 4 Richardson rows
+    (the rows of a big system's encounter body run side by side)."""
+    sysm = systems.embryo_disk(n_embryos=254, seed=5)
+    st, gs, alag, (op, ov, oal, of, ost) = run_both(oracle, sysm, 60, drift=merc.DRIFT_ELEMENTS, bs_rows=rows)
+    assert ost[0] > 0, "the case should exercise close encounters"
+    assert np.array_equal(st.flags, of)
+    assert np.array_equal(st.pos, op), rel_err(st.pos, op).max()
+    assert np.array_equal(st.vel, ov)
+
+
 def mixed_batch():
     """One big system (tiled kernels) between small ones (per-body kernels)."""
     a = systems.sweep(n_systems=3, nt_lo=16, nt_hi=40, seed=7)
