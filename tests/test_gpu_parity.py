@@ -138,6 +138,22 @@ def test_universal_parity(oracle, which):
     assert abs(gs.kepler_iterations - ost[1]) <= max(2, ost[1] // 1000)
 
 
+@pytest.mark.parametrize("which,steps", [("mixed", 60), ("two_big", 200)])
+def test_elements_batches_bitwise(oracle, which, steps):
+    """Big and small systems in one batch on the element path: the warp and
+    block kernels of the big systems and the per-thread kernels of the small
+    ones give the reference's bits (two_big: with close encounters)."""
+    sysm = mixed_batch() if which == "mixed" else two_big_batch()
+    st, gs, alag, (op, ov, oal, of, ost) = run_both(oracle, sysm, steps, drift=merc.DRIFT_ELEMENTS)
+    if which == "two_big":
+        assert ost[0] > 0, "the case should exercise close encounters"
+    assert gs.ce_body_steps == ost[0]
+    assert np.array_equal(st.flags, of)
+    assert np.array_equal(st.pos, op), rel_err(st.pos, op).max()
+    assert np.array_equal(st.vel, ov)
+    assert np.array_equal(alag, oal)
+
+
 @pytest.mark.parametrize("drift,which", [(merc.DRIFT_ELEMENTS, "embryo"), (merc.DRIFT_UNIVERSAL, "embryo"),
                                          (merc.DRIFT_UNIVERSAL, "sweep"), (merc.DRIFT_UNIVERSAL, "two_big")])
 def test_split_steps_and_resume_are_exact(drift, which):
