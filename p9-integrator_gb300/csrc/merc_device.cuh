@@ -18,11 +18,14 @@ struct d3 {
 };
 
 __device__ __forceinline__ double mag2(const d3& a) { return fma(a.x, a.x, fma(a.y, a.y, a.z * a.z)); }
+// The reference's guarded division and square root, (netz x) / (y + etz)
+// and sqrt(x (x >= 0)).  Where the guard's factor is 1 and its addend 0 they
+// change nothing (1 x = x and y + 0 = y exactly for y != 0, NaN kept), so
+// those cases skip the two operations; the others keep them.
 __device__ __forceinline__ double stable_div(double x, double y) {  // sim.cuh:81-87
-  double etz = (double)(y == 0.0), netz = (double)(y != 0.0);
-  return (netz * x) / (y + etz);
+  return y != 0.0 ? x / y : (0.0 * x) / (y + 1.0);
 }
-__device__ __forceinline__ double stable_sqrt(double x) { return sqrt(x * (double)(x >= 0.0)); }  // :35-40
+__device__ __forceinline__ double stable_sqrt(double x) { return sqrt(x >= 0.0 ? x : x * 0.0); }  // :35-40
 
 // Unit constants read at run time (kernel parameters): fma(one, a, b) and
 // fma(a, b, nz) with one = 1 and nz = -0 give exactly a + b and a * b (the
