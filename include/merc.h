@@ -232,11 +232,16 @@ int merc_mlp_get_weights(merc_ctx* ctx, float* blob);
  * fit (about 100k bodies for a system with many massive bodies) return
  * MERC_ERR_CONFIG before any work is queued.
  *
- * The first call on a device looks up the array's device address on that
- * device (cudaGetSymbolAddress); make that first call before any stream
- * capture.  All calls share the one array, and each call re-initialises the
- * parts that must start at zero, so calls that overlap on the GPU (other
- * host threads, other streams) race with each other: serialise them. */
+ * The call makes `device` current while it works and restores the calling
+ * thread's current device before it returns.  It must not be called while
+ * `stream` (or, for the legacy default stream, any stream) is being captured
+ * into a CUDA graph: it copies small tables from its own stack frame and
+ * waits for the stream before returning, so it returns MERC_ERR_STATE
+ * instead of queuing anything.  The first call on a device also looks up the
+ * array's device address on that device (cudaGetSymbolAddress).  All calls
+ * share the one array, and each call re-initialises the parts that must start
+ * at zero, so calls that overlap on the GPU (other host threads, other
+ * streams) race with each other: serialise them. */
 int merc_step_static(int device, const merc_params* p, int32_t n_bodies, int32_t n_massive, double* pos,
                      double* vel, const double* mass, uint32_t* flags, int64_t n_steps, void* stream);
 

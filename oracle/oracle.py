@@ -52,9 +52,18 @@ def default_params(**kw) -> MercParams:
 def build(quiet: bool = True) -> None:
     """Compile liboracle.so (and the reference cross-check when its sources exist)."""
     out = subprocess.DEVNULL if quiet else None
-    subprocess.check_call(["make", "-s", "-C", HERE, "all"], stdout=out)
-    if os.path.isdir("/root/reference/src"):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref"], stdout=out)
+    subprocess.check_call(["make", "-s", "-C", HERE, "all", "ref"], stdout=out)
+
+
+def ref_dir():
+    """Directory of the reference checkout (environment MERC_REF_DIR, else the
+    build recipe's default), or None where it is absent (as on a GPU host)."""
+    try:
+        out = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "refdir"], capture_output=True,
+                             text=True, check=True).stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        return None
+    return out if out and os.path.isdir(out) else None
 
 
 def _ptr(a, t):

@@ -1745,14 +1745,23 @@ struct Carve {
 
 }  // namespace
 
-extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodies, int32_t n_massive, double* pos,
-                                double* vel, const double* mass, uint32_t* flags, int64_t n_steps, void* stream) {
+static int step_static(int device, const merc_params* p, int32_t n_bodies, int32_t n_massive, double* pos,
+                       double* vel, const double* mass, uint32_t* flags, int64_t n_steps, void* stream) {
   merc_ctx* ctx = nullptr;  // errors are reported by status code only
   if (!p || !pos || !vel || !mass) return MERC_ERR_CONFIG;
   if (n_bodies <= 0 || n_massive < 0 || n_massive > n_bodies || n_steps < 0) return MERC_ERR_CONFIG;
   if (device < 0 || device >= kMaxDevices) return MERC_ERR_CONFIG;
   if (p->drift != MERC_DRIFT_UNIVERSAL || check_params(nullptr, p) != MERC_OK) return MERC_ERR_CONFIG;
   CK(cudaSetDevice(device));
+  {
+    // the call copies small tables from its own stack and waits for the
+    // stream at the end: neither may be recorded into a graph
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing((cudaStream_t)stream, &cap);
+    if (e == cudaErrorStreamCaptureImplicit || (e == cudaSuccess && cap != cudaStreamCaptureStatusNone))
+      return MERC_ERR_STATE;
+    CK(e);
+  }
   int sms = 0;
   CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   sms = std::max(1, sms);
@@ -1884,6 +1893,15 @@ extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodi
   }
   CK(cudaStreamSynchronize(s));
   return MERC_OK;
+}
+
+extern "C" int merc_step_static(int device, const merc_params* p, int32_t n_bodies, int32_t n_massive, double* pos,
+                                double* vel, const double* mass, uint32_t* flags, int64_t n_steps, void* stream) {
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+  const int st = step_static(device, p, n_bodies, n_massive, pos, vel, mass, flags, n_steps, stream);
+  if (prev >= 0) cudaSetDevice(prev);  // the caller's current device, as it was
+  return st;
 }
 
 extern "C" {

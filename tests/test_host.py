@@ -13,7 +13,15 @@ import systems
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB = os.path.join(ROOT, "p9-integrator_gb300", "libmerc.so")
-REF_EXAMPLES = "/root/reference/examples"
+
+def _ref_examples():
+    from oracle import ref_dir
+
+    d = ref_dir()
+    return os.path.join(d, "examples") if d else None
+
+
+REF_EXAMPLES = _ref_examples()
 
 
 @pytest.fixture(scope="module")
@@ -109,7 +117,7 @@ def test_json_round_trip(tmp_path):
     assert systems.count_massive(d["mass"]) == 5
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference examples not present")
+@pytest.mark.skipif(not REF_EXAMPLES or not os.path.isdir(REF_EXAMPLES), reason="reference examples not present")
 def test_reference_example_configs_parse():
     for name in ("earth_and_mars.json", "planetary_embryos.json", "p9.json"):
         d = systems.from_json(os.path.join(REF_EXAMPLES, name))

@@ -27,8 +27,9 @@ def rel_err(a, b):
     return np.max(np.abs(a - b), axis=0) / np.maximum(np.linalg.norm(b, axis=0), 1e-300)
 
 
+@pytest.mark.parametrize("steps", [1, 8])
 @pytest.mark.parametrize("which", ["embryo", "outer"])
-def test_step_static_matches_step(which):
+def test_step_static_matches_step(which, steps):
     torch = pytest.importorskip("torch")
     # embryo disk: more than 32 massive bodies, so the kick splits its sources
     # over blocks and keeps per-chunk partial sums in the static scratch;
@@ -46,11 +47,12 @@ def test_step_static_matches_step(which):
     flags = torch.zeros(n, dtype=torch.int32, device=dev)
     torch.cuda.synchronize()
     L = merc.lib()
+    # with several steps per call the call alternates its two r_crit tables
     for call in range(2):
-        g.step(1)
+        g.step(steps)
         ref = g.state()
         st = L.merc_step_static(0, C.byref(params), n, nm, C.c_void_p(pos.data_ptr()), C.c_void_p(vel.data_ptr()),
-                                C.c_void_p(mass.data_ptr()), C.c_void_p(flags.data_ptr()), 1, None)
+                                C.c_void_p(mass.data_ptr()), C.c_void_p(flags.data_ptr()), steps, None)
         assert st == merc.MERC_OK, f"call {call}: status {st}"
         got_pos = pos.cpu().numpy()
         got_vel = vel.cpu().numpy()
@@ -74,3 +76,26 @@ def test_step_static_rejects_oversize():
     # the element drift is not served by this entry point
     p2 = merc.default_params(drift=merc.DRIFT_ELEMENTS)
     assert L.merc_step_static(0, C.byref(p2), 4, 1, ptr, ptr, ptr, None, 1, None) == merc.MERC_ERR_CONFIG
+
+
+def test_step_static_refuses_stream_capture():
+    """The call copies small tables from its own stack and waits for its
+    stream, so it must not be recorded into a graph: on a capturing stream it
+    returns MERC_ERR_STATE and queues nothing."""
+    torch = pytest.importorskip("torch")
+    sysm = systems.outer_solar_system()
+    n, nm = sysm.n_total, int(sysm.n_massive[0])
+    params = merc.default_params(dt=sysm.dt, hill_factor=sysm.hill_factor, drift=merc.DRIFT_UNIVERSAL)
+    dev = torch.device("cuda:0")
+    buf = torch.ones(3 * n, dtype=torch.float64, device=dev)
+    mass = torch.from_numpy(np.ascontiguousarray(sysm.mass)).to(dev)
+    L = merc.lib()
+    s = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(graph, stream=s):
+        buf.mul_(1.0)
+        st = L.merc_step_static(0, C.byref(params), n, nm, C.c_void_p(buf.data_ptr()), C.c_void_p(buf.data_ptr()),
+                                C.c_void_p(mass.data_ptr()), None, 1, C.c_void_p(s.cuda_stream))
+    torch.cuda.synchronize()
+    assert st == merc.MERC_ERR_STATE
