@@ -16,13 +16,17 @@ ours:       K timed steps on the GPU through libmerc.so.  One bench step is one
             (512 MB write) between calls; `value` counts integrator body-steps
             over device time (CUDA events), `e2e` is host wall time of the
             public C-ABI call sequence set_state (H2D, pinned) -> step -> get_state
-            (D2H) per bench step.  Also reported: kick-kernel roofline against the
-            measured FP64 FMA peak, the same for the encounter sub-step kernel
-            (timed in three more calls), the CPU oracle on the host cores, and
-            the element-drift (reference-compat) path.
-reference:  the CPU restatement of the reference step (oracle/, OpenMP over all
-            host cores), same workload and metric; the reference itself is CUDA
-            only and ships no CPU path.
+            (D2H, pinned) per bench step, replaying the timed calls from the
+            same start state with the same flush.  Also reported: kick-kernel
+            roofline against the measured FP64 FMA peak, the same for the
+            encounter sub-step kernel (timed in three more calls), the CPU
+            oracle on the host cores (the reference's element step as
+            cpu_baseline, the universal drift beside it; for the sweep and the
+            Planet Nine workload OpenMP over systems), and the element-drift
+            (reference-algorithm) path on the GPU.
+reference:  the CPU restatement of the reference's step (element drift,
+            oracle/, OpenMP over all host cores), same workload and metric; the
+            reference itself is CUDA only and ships no CPU path.
 N > 1 runs N independent replicas (one per GPU, no collective; weak scaling).
 """
 from __future__ import annotations
@@ -137,33 +141,48 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def cpu_baseline(sysm, params_kw, sample_s=12.0):
-    """The oracle on this host's cores, timed on a bounded number of steps."""
+def cpu_rate(sysm, params_kw, sample_s=12.0, warm_steps=0, label=None):
+    """The oracle (OpenMP over bodies for one system, over systems for a
+    batch) on this host's cores: body-steps/s over a bounded number of steps
+    of the full workload, after `warm_steps` untimed steps."""
     from oracle import Oracle
     from oracle import default_params as oparams
 
     O = Oracle()
     p = oparams(**params_kw)
     pos, vel, alag = O.load_elements(p, sysm.body_offset, sysm.n_massive, sysm.mass, sysm.elements)
+    fl = None
+    if warm_steps:
+        pos, vel, alag, fl, _ = O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag,
+                                      steps=warm_steps)
     t0 = time.perf_counter()
-    pos, vel, alag, fl, _ = O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag, steps=1)
+    pos, vel, alag, fl, _ = O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag, flags=fl, steps=1)
     one = time.perf_counter() - t0
     steps = int(max(1, min(5000, sample_s / max(one, 1e-6))))
     t0 = time.perf_counter()
     O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag, flags=fl, steps=steps)
     dt = time.perf_counter() - t0
+    drift = "element drift (the reference's step)" if params_kw.get("drift", 0) == 0 else "universal drift"
     return {"value": sysm.n_total * steps / dt, "unit": UNIT, "cores": O.threads(), "kind": "port",
-            "sample": f"{steps} steps of the full {sysm.n_total}-body workload ({dt:.1f} s)"}
+            "sample": f"{steps} steps of the full {sysm.n_total}-body workload{label or ''}, {drift} ({dt:.1f} s)"}
+
+
+def cpu_baseline(sysm, params_kw, sample_s=12.0):
+    return cpu_rate(sysm, params_kw, sample_s)
 
 
 def run_reference(args, world, rank, dist):
+    """The reference's algorithm on the host cores: the oracle's restatement
+    of the reference step (element drift: elements round trip and 8 fixed
+    Danby iterations, src/sim.cuh:692-713), binary64 with the host's C
+    library, OpenMP over the bodies; the universal-drift figure beside it."""
     if rank != 0:
         return
     from oracle import Oracle
     from oracle import default_params as oparams
 
     sysm = workload()
-    kw = dict(dt=sysm.dt, hill_factor=sysm.hill_factor, drift=1)
+    kw = dict(dt=sysm.dt, hill_factor=sysm.hill_factor, drift=0)
     O = Oracle()
     p = oparams(**kw)
     pos, vel, alag = O.load_elements(p, sysm.body_offset, sysm.n_massive, sysm.mass, sysm.elements)
@@ -174,16 +193,20 @@ def run_reference(args, world, rank, dist):
     O.run(p, sysm.body_offset, sysm.n_massive, sysm.mass, pos, vel, alag, flags=fl, steps=args.steps * S)
     dt = time.perf_counter() - t0
     value = sysm.n_total * S * args.steps / dt
+    universal = cpu_rate(sysm, dict(kw, drift=1), sample_s=8.0, warm_steps=args.warmup * S)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": sysm.label, "bodies": sysm.n_total, "n_massive": int(sysm.n_massive[0]),
-                       "dt": sysm.dt, "drift": "universal", "hill_factor": sysm.hill_factor, "batch": S,
-                       "step": f"{S} integrator steps"},
+                       "dt": sysm.dt, "drift": "elements (the reference's step)", "hill_factor": sysm.hill_factor,
+                       "batch": S, "step": f"{S} integrator steps"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.threads(), "kind": "port",
-                             "sample": f"{args.steps * S} full integrator steps after {args.warmup * S} warm-up steps"},
+                             "sample": f"{args.steps * S} full integrator steps after {args.warmup * S} warm-up "
+                                       f"steps, element drift (the reference's step)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "CPU restatement of the reference step (the reference ships CUDA only)"}
+            "cpu_universal_drift": universal,
+            "note": "CPU restatement of the reference step (src/sim.cuh:679-742, element drift) on all host "
+                    "cores; the reference ships CUDA only"}
     print(json.dumps(line), flush=True)
 
 
@@ -235,6 +258,26 @@ def sweep_section(merc, args, local, dist, world, rank):
             "speedup_vs_one_by_one": batched / one_by_one}
 
 
+def sweep_cpu(gpu):
+    """The 4096-system sweep on the host cores (OpenMP over systems, the
+    reference's ensemble split src/simutils.cuh:288-290 done by threads):
+    the universal drift the GPU runs and the reference's element step."""
+    sysm = systems.sweep()
+    kw = dict(dt=sysm.dt, hill_factor=sysm.hill_factor)
+    uni = cpu_rate(sysm, dict(kw, drift=1), sample_s=6.0)
+    ele = cpu_rate(sysm, dict(kw, drift=0), sample_s=6.0)
+    return {"cpu_universal": uni, "cpu_elements": ele,
+            "gpu_over_cpu_universal": gpu["batched_body_steps_per_s"] / uni["value"]}
+
+
+def p9_cpu():
+    """The Planet Nine sweep on the host cores, both drifts (OpenMP over systems)."""
+    sysm = systems.p9_sweep()
+    kw = dict(dt=sysm.dt, hill_factor=sysm.hill_factor)
+    return {"cpu_universal": cpu_rate(sysm, dict(kw, drift=1), sample_s=4.0),
+            "cpu_elements": cpu_rate(sysm, dict(kw, drift=0), sample_s=4.0)}
+
+
 def p9_section(merc, args, local, dist, world, rank):
     """The reference's own workload: the Planet Nine configuration (Planet
     Nine + 4 giants + 10235 TNOs, p9_config.py) as 32 sweep systems in one
@@ -257,7 +300,7 @@ def p9_section(merc, args, local, dist, world, rank):
     return out
 
 
-def planetesimal_section(merc, args, local, dist, world, rank):
+def planetesimal_section(merc, args, local, dist, world, rank, peak):
     """Workload 4: Sun + 4 giants + 8192 planetesimals + 131072 test particles,
     dt 0.25, one 8-step graph (test-particle half kicks merged across step
     boundaries).  Reports body-steps/s, pair interactions/s and the HBM rate of
@@ -277,7 +320,13 @@ def planetesimal_section(merc, args, local, dist, world, rank):
     return {"workload": sysm.label, "bodies": int(sysm.n_total), "n_massive": nm, "steps": steps,
             "body_steps_per_s": sum_over_ranks(dist, float(sysm.n_total * steps)) / t, "ms_per_step": ms / steps,
             "pairs_per_s": sum_over_ranks(dist, float(2 * (nm * (nm - 1) + nt * nm) * steps)) / t,
-            "test_particle_stream_gbs": sum_over_ranks(dist, 96.0 * nt * steps) / t / 1e9}
+            "test_particle_stream_gbs": sum_over_ranks(dist, 96.0 * nt * steps) / t / 1e9,
+            "fp64_frac_algorithmic": FLOPS_PER_PAIR * 2 * (nm * (nm - 1) + nt * nm) * steps / t / 1e12 / peak,
+            "fp64_frac_note": "27 algorithmic flops per ordered pair and half kick over the measured FP64 FMA "
+                              "peak, whole step; above 1 because the two half kicks around a step boundary are "
+                              "merged into one pass (18 FP64 instructions per test-particle pair serve 54 "
+                              "algorithmic flops) and the symmetric massive pass evaluates each unordered pair "
+                              "once"}
 
 
 def warm_start_section(merc, args, local):
@@ -354,6 +403,9 @@ def run_ours(args, world, rank, local, dist):
     g.time_kicks(True)
     peak = merc.fp64_peak_tflops(local)
     g.step(args.warmup)
+    # the timed region's start state, for the end-to-end replay below
+    start = g.state()
+    start_alag = g.a_lag()
     l0 = g.launch_count()
     clocks = ClockSampler(local)
     clocks.start()
@@ -381,6 +433,35 @@ def run_ours(args, world, rank, local, dist):
     traffic = load_traffic().get("kick_bytes_per_launch")
     st = g.stats()
 
+    # end to end through the C ABI with host buffers: the timed region's K
+    # calls again, from its start state and with the same L2 flush before each
+    # call (untimed); each call uploads the state from pinned host memory
+    # (set_state), steps, and reads the result back into pinned memory
+    # (get_state), so the copies are the only difference from `value`
+    try:
+        import torch
+
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+        pos_h, vel_h, alag_h = pin(start.pos), pin(start.vel), pin(start_alag)
+        flags_h = pin(start.flags)
+        pinned = True
+    except Exception:
+        pos_h, vel_h, alag_h, flags_h = start.pos.copy(), start.vel.copy(), start_alag.copy(), start.flags.copy()
+        pinned = False
+    import merc as _m
+
+    out_h = _m.State(pos_h, vel_h, flags_h)
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        g.flush_l2(512 << 20)
+        t0 = time.perf_counter()
+        g.set_state(pos_h, vel_h, alag_h)
+        g.step(S)
+        g.state(out=out_h)
+        e2e_s += time.perf_counter() - t0
+    e2e_s = max_over_ranks(dist, e2e_s)
+    e2e_value = sum_over_ranks(dist, float(n * S * args.steps)) / e2e_s
+
     # the encounter sub-step (the largest share of the step at this encounter
     # density): a few more timed calls with events around its kernel
     g.time_kicks(False)
@@ -398,27 +479,6 @@ def run_ours(args, world, rank, local, dist):
     enc_achieved = FLOPS_PER_PAIR * enc_pairs / (enc_avg_ms * 1e-3) / 1e12
     g.time_encounter(False)
 
-    # end to end through the C ABI with host buffers (pinned) and copies
-    e2e_steps = max(3, min(args.steps, 20))
-    host = g.state()
-    alag = g.a_lag()
-    try:
-        import torch
-
-        pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
-        pos_h, vel_h, alag_h = pin(host.pos.copy()), pin(host.vel.copy()), pin(alag.copy())
-    except Exception:
-        pos_h, vel_h, alag_h = host.pos.copy(), host.vel.copy(), alag.copy()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        g.set_state(pos_h, vel_h, alag_h)
-        g.step(S)
-        out = g.state()
-        pos_h[:] = out.pos
-        vel_h[:] = out.vel
-    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
-    e2e_value = sum_over_ranks(dist, float(n * S * e2e_steps)) / e2e_s
-
     # element-drift (reference-compat, bitwise-checked) path, same workload
     compat = None
     if not args.skip_compat:
@@ -428,17 +488,35 @@ def run_ours(args, world, rank, local, dist):
         gc.step(2)
         cs = max(2, min(args.steps, 10))
         gc.step(cs)
-        compat = {"value": n * cs / (gc.stats().last_step_ms / 1e3), "steps": cs, "drift": "elements"}
+        compat = {"value": n * cs / (gc.stats().last_step_ms / 1e3), "steps": cs, "drift": "elements",
+                  "note": "the reference's algorithm on the GPU, bit for bit with the oracle; compare with "
+                          "cpu_baseline (the same algorithm on the host cores)"}
         gc.close()
     g.close()
     sweep = None if args.skip_sweep else sweep_section(merc, args, local, dist, world, rank)
     p9 = None if args.skip_p9 else p9_section(merc, args, local, dist, world, rank)
-    planet = None if args.skip_planetesimal else planetesimal_section(merc, args, local, dist, world, rank)
+    planet = None if args.skip_planetesimal else planetesimal_section(merc, args, local, dist, world, rank, peak)
+    if sweep:
+        sweep["kick_fp64_frac_algorithmic"] = FLOPS_PER_PAIR * sweep["batched_pairs_per_s"] / 1e12 / peak
+        sweep["kick_fp64_frac_note"] = ("pair work only (27 flops per pair over the measured FP64 FMA peak); the "
+                                        "drift's Stumpff/Newton work, the larger share of this workload, is not "
+                                        "counted")
     warm = None if args.skip_warm else warm_start_section(merc, args, local)
 
     if rank != 0:
         return
-    cpu = cpu_baseline(sysm, kw) if not args.skip_cpu else None
+    cpu = cpu_ref = None
+    if not args.skip_cpu:
+        # the reference's step (element drift) as the baseline; the universal
+        # drift on the same cores beside it
+        cpu = cpu_rate(sysm, dict(kw, drift=0), sample_s=12.0)
+        cpu_ref = cpu_rate(sysm, kw, sample_s=8.0)
+        if compat:
+            compat["gpu_over_cpu_same_algorithm"] = compat["value"] / cpu["value"]
+        if sweep:
+            sweep.update(sweep_cpu(sweep))
+        if p9:
+            p9.update(p9_cpu())
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -459,8 +537,11 @@ def run_ours(args, world, rank, local, dist):
                                "encounter_bodies_per_step": ce_per_step, "pairs_per_launch": enc_pairs,
                                "flops_per_pair": FLOPS_PER_PAIR},
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 7 * 8 * n,
-                "d2h_bytes_per_step": 6 * 8 * n + 4 * n, "steps": e2e_steps},
+        "cpu_universal_drift": cpu_ref,
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": int(pos_h.nbytes + vel_h.nbytes + alag_h.nbytes),
+                "d2h_bytes_per_step": int(pos_h.nbytes + vel_h.nbytes + flags_h.nbytes), "steps": args.steps,
+                "pinned": pinned, "start": "the timed region's start state, same L2 flush before each call"},
         "pairs_per_s": value * 2 * (nm - 1) if n == nm else None,
         "gpu_launches": int(launches),
         "clocks": ck,

@@ -266,10 +266,19 @@ class Integrator:
     def roundtrip(self):
         self._check(self.L.merc_roundtrip(self.h))
 
-    def state(self) -> State:
-        pos = np.empty(3 * self.n)
-        vel = np.empty(3 * self.n)
-        flags = np.empty(self.n, np.uint32)
+    def state(self, out: State | None = None) -> State:
+        """The state (merc_get_state); `out` gives the host arrays to fill
+        (e.g. pinned buffers), C-contiguous float64 / uint32 of the right sizes."""
+        if out is not None:
+            pos, vel, flags = out.pos, out.vel, out.flags
+            if (pos.dtype != np.float64 or vel.dtype != np.float64 or flags.dtype != np.uint32
+                    or pos.size != 3 * self.n or vel.size != 3 * self.n or flags.size != self.n
+                    or not (pos.flags.c_contiguous and vel.flags.c_contiguous and flags.flags.c_contiguous)):
+                raise ValueError("state(out=...): arrays of the wrong type, size or layout")
+        else:
+            pos = np.empty(3 * self.n)
+            vel = np.empty(3 * self.n)
+            flags = np.empty(self.n, np.uint32)
         self._check(self.L.merc_get_state(self.h, _p(pos, _f64p), _p(vel, _f64p), _p(flags, _u32p)))
         return State(pos, vel, flags)
 
