@@ -1,9 +1,15 @@
-"""Generate tests/golden/energy_outer.json: energy of the outer-solar-system
-workload (5 massive bodies + 100 test particles, dt 0.5 yr, changeover 3 Hill
-radii) after 1e4 steps, from the CPU oracle in long double (the energy-error
-reference) and in binary64 with the reference's element drift (the
-reference algorithm).  Run from the repository root:
-    python tests/golden/make_energy.py
+"""Generate the energy fixtures: energy after 1e4 steps from the CPU oracle in
+long double (the energy-error reference) and in binary64, with the
+reference's element drift (the reference algorithm) and the universal drift.
+
+    python tests/golden/make_energy.py outer    -> energy_outer.json
+        outer-solar-system workload (5 massive bodies + 100 test particles,
+        dt 0.5 yr, changeover 3 Hill radii)
+    python tests/golden/make_energy.py embryo   -> energy_embryo.json
+        the 2002-body embryo disk (dt 0.01 yr, changeover 3 Hill radii, close
+        encounters every step); about an hour on 8 cores
+
+Run from the repository root.
 """
 import json
 import os
@@ -23,10 +29,10 @@ from oracle import default_params as oparams  # noqa: E402
 STEPS = 10000
 
 
-def main():
+def main(which="outer"):
     build()
     O = Oracle()
-    s = systems.outer_solar_system()
+    s = systems.outer_solar_system() if which == "outer" else systems.embryo_disk()
     out = {"workload": s.label, "steps": STEPS, "dt": s.dt, "hill_factor": s.hill_factor}
     for drift, name in ((0, "elements"), (1, "universal")):
         p = oparams(dt=s.dt, hill_factor=s.hill_factor, drift=drift)
@@ -40,9 +46,9 @@ def main():
             res[tag] = {"energy": e1, "rel_error": abs(e1 - e0) / abs(e0)}
         out[name] = {"energy0": e0, **res}
         print(name, res, f"{time.time() - t:.1f}s")
-    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "energy_outer.json"), "w") as f:
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), f"energy_{which}.json"), "w") as f:
         json.dump(out, f, indent=1)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else "outer")
