@@ -58,6 +58,8 @@ extern "C" {
 #define MERC_FLAG_CE_EVER 2u   /* close encounter detected in any step since load */
 #define MERC_FLAG_EJECTED 4u   /* heliocentric distance exceeded eject_r (sticky) */
 #define MERC_FLAG_NONFINITE 8u /* position or velocity became NaN/inf (sticky) */
+#define MERC_FLAG_MERGED 16u   /* absorbed in a physical collision and parked (sticky; merc_set_radii) */
+#define MERC_FLAG_GREW 32u     /* absorbed another body in a physical collision (sticky) */
 
 /* Integration parameters.  Defaults (merc_default_params) are the
  * reference's compile-time constants (src/constants.cuh:4-11) and its
@@ -182,6 +184,49 @@ int merc_energy(merc_ctx* ctx, double* energy);
  * context's heliocentric positions and democratic-heliocentric velocities,
  * which is the system's total).  L: 3 doubles per system, L[3 s + c]. */
 int merc_angular_momentum(merc_ctx* ctx, double* L);
+
+/* ---- physical collisions ----
+ * No counterpart in the reference: its encounter test only chooses the
+ * sub-stepper (src/sim.cuh:589-613, 699-730) and bodies pass through each
+ * other.  merc_set_radii switches detection on for the loaded systems:
+ * radius[j] (AU, n_total values, >= 0; 0 for a point body) for every body;
+ * NULL switches it off (the default; every load switches it off).
+ * Once per step, after the drift and the encounter sub-step, each body in
+ * close encounter that step is tested against the massive bodies of its
+ * system: |x_i - x_j| < R_i + R_j is a collision.  (Only bodies in encounter
+ * are tested, so R_i + R_j must stay below the changeover radius, as it does
+ * for physical radii.)  Colliding pairs (a < b, by index in the system)
+ * merge in ascending order while both are unmerged: the heavier body
+ * survives (the lower index on a tie) and takes the total mass and the
+ * mass-weighted mean position and velocity (momentum and centre of mass are
+ * kept; flag MERC_FLAG_GREW); the other body is flagged MERC_FLAG_MERGED,
+ * keeps a mass of MERC_MERGED_MASS if it was massive (a source must keep a
+ * non-zero critical radius for the reference's changeover formula) and is
+ * parked on a circular orbit at MERC_PARK_R + 64 x its index AU in the
+ * x-y plane, where it interacts with nothing.  A massless body that hits a
+ * massive one is parked the same way and changes nothing else.  The element
+ * and universal paths both support it (small systems then run the per-phase
+ * kernels, not the persistent sweep kernel).  Masses: merc_get_masses. */
+#define MERC_MERGED_MASS 1e-300
+#define MERC_PARK_R 1e6
+int merc_set_radii(merc_ctx* ctx, const double* radius);
+
+/* One resolved collision: step (counted from the load, 1 = the first step),
+ * and the global body indices of the survivor and of the absorbed body. */
+typedef struct merc_collision {
+  int64_t step;
+  int64_t survivor;
+  int64_t absorbed;
+} merc_collision;
+
+/* Collisions resolved since merc_set_radii, in the order they were resolved.
+ * Copies min(total, max) records to out (may be NULL with max 0) and the
+ * total count to *count; records beyond the context's log of 65536 are
+ * counted but not kept. */
+int merc_get_collisions(merc_ctx* ctx, merc_collision* out, int64_t max, int64_t* count);
+
+/* Current masses (n_total doubles): the loaded masses, changed by collisions. */
+int merc_get_masses(merc_ctx* ctx, double* mass);
 
 /* Number of kernel launches issued by this context since creation. */
 int64_t merc_launch_count(const merc_ctx* ctx);

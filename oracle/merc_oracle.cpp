@@ -11,6 +11,7 @@
 #include <omp.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdio>
 #include <memory>
 
@@ -44,6 +45,11 @@ template <class R> struct Sys {
   std::vector<V3<R>> x, v;
   std::vector<R> m, alag;
   std::vector<uint32_t> flags;
+  // physical collisions (empty: off): radii, steps since load, events
+  // (step, survivor, absorbed; indices within the system)
+  std::vector<double> rad;
+  int64_t step = 0;
+  std::vector<int64_t> ev;
 };
 
 // Index of the source a body excludes as "itself": its index in the system,
@@ -104,6 +110,56 @@ static bool close_encounter(const V3<R>& pos, int self, const Src<R>* src, int n
     ce = ce || ((mag < src[i].rc) && (self != i));
   }
   return ce;
+}
+
+// Physical collisions after the drift (no reference counterpart; restates
+// k_collide_find / k_collide_resolve of the GPU library, merc_collide.cuh):
+// every body in encounter this step against the massive bodies of its system,
+// |x_a - x_b| < R_a + R_b on the drift outputs; the pairs (a < b) merge in
+// ascending order while both are unmerged: the heavier survives (the lower
+// index on a tie) with the total mass and the mass-weighted mean position and
+// velocity; the other body keeps MERC_MERGED_MASS if it was massive and is
+// parked on a circular orbit at MERC_PARK_R + 64 x its index.
+template <class R, class M> static void collide(Sys<R>& S, const std::vector<char>& ce, R hill) {
+  S.step++;
+  std::vector<std::pair<int, int>> pairs;
+  for (int j = 0; j < S.n; j++) {
+    if (!ce[j] || (S.flags[j] & MERC_FLAG_MERGED)) continue;
+    for (int i = 0; i < S.nm; i++) {
+      if (i == j || (S.flags[i] & MERC_FLAG_MERGED)) continue;
+      const int a = std::min(i, j), b = std::max(i, j);
+      const R dx = S.x[b].x - S.x[a].x, dy = S.x[b].y - S.x[a].y, dz = S.x[b].z - S.x[a].z;
+      const R d2 = std::fma(dx, dx, std::fma(dy, dy, dz * dz));
+      const R rs = R(S.rad[a]) + R(S.rad[b]);
+      if (d2 < rs * rs) pairs.push_back({a, b});
+    }
+  }
+  std::sort(pairs.begin(), pairs.end());
+  pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
+  for (const auto& pr : pairs) {
+    const int a = pr.first, b = pr.second;
+    if ((S.flags[a] | S.flags[b]) & MERC_FLAG_MERGED) continue;
+    const int s = S.m[b] > S.m[a] ? b : a, o = s == a ? b : a;
+    if (o < S.nm) {
+      const R ms = S.m[s], mo = S.m[o], Mt = ms + mo;
+      S.x[s] = {std::fma(ms, S.x[s].x, mo * S.x[o].x) / Mt, std::fma(ms, S.x[s].y, mo * S.x[o].y) / Mt,
+                std::fma(ms, S.x[s].z, mo * S.x[o].z) / Mt};
+      S.v[s] = {std::fma(ms, S.v[s].x, mo * S.v[o].x) / Mt, std::fma(ms, S.v[s].y, mo * S.v[o].y) / Mt,
+                std::fma(ms, S.v[s].z, mo * S.v[o].z) / Mt};
+      S.m[s] = Mt;
+      S.m[o] = R(MERC_MERGED_MASS);
+    }
+    const R r = R(MERC_PARK_R) + R(64) * R(o);
+    S.x[o] = {r, R(0), R(0)};
+    S.v[o] = {R(0), R(1) / std::sqrt(r), R(0)};
+    S.alag[o] = r;
+    S.flags[s] |= MERC_FLAG_GREW;
+    S.flags[o] |= MERC_FLAG_MERGED;
+    S.ev.push_back(S.step);
+    S.ev.push_back(s);
+    S.ev.push_back(o);
+  }
+  (void)hill;
 }
 
 // One Mercurius step of one system: the loop body of mercurius_solver,
@@ -172,6 +228,7 @@ template <class R, class M> static void step_system(Sys<R>& S, const Params& P, 
   }
   S.x.swap(xn);
   S.v.swap(vn);
+  if (!S.rad.empty()) collide<R, M>(S, ce, hill);
   // second solar jump, sim.cuh:735-737
   p = momentum(S);
   for (int j = 0; j < n; j++) {
@@ -277,20 +334,53 @@ static int check_layout(int n_sys, const int64_t* off, const int32_t* nm) {
   return MERC_OK;
 }
 
+// Collision arguments of run_impl: radii (NULL: off), masses written back,
+// steps since load before the call, and the events (step, survivor, absorbed
+// as global indices) in the order the GPU library logs them: by step, then
+// by the pair (lower, higher index).
+struct CollideIO {
+  const double* radius = nullptr;
+  double* mass_out = nullptr;
+  int64_t step0 = 0;
+  std::vector<int64_t> events;
+};
+
 template <class R, class M>
 static int run_impl(const merc_params* mp, int n_sys, const int64_t* off, const int32_t* nm, const double* mass,
-                    double* pos, double* vel, double* alag, uint32_t* flags, int64_t n_steps, int64_t* stats) {
+                    double* pos, double* vel, double* alag, uint32_t* flags, int64_t n_steps, int64_t* stats,
+                    CollideIO* col = nullptr) {
   Params P = to_params(mp);
   const int64_t ntot = off[n_sys];
   const int nthr = omp_get_max_threads();
   const bool by_system = n_sys >= 2 * nthr;
   std::vector<Counters> cnt(n_sys);
+  std::vector<std::vector<int64_t>> ev(n_sys);
 #pragma omp parallel for schedule(dynamic, 1) if (by_system)
   for (int s = 0; s < n_sys; s++) {
     Sys<R> S;
     gather(S, off[s], off[s + 1] - off[s], nm[s], ntot, mass, pos, vel, alag, flags);
+    if (col && col->radius) {
+      S.rad.assign(col->radius + off[s], col->radius + off[s + 1]);
+      S.step = col->step0;
+    }
     for (int64_t k = 0; k < n_steps; k++) step_system<R, M>(S, P, !by_system, cnt[s]);
     scatter(S, off[s], ntot, pos, vel, alag, flags);
+    if (col && col->radius) {
+      for (int j = 0; j < S.n; j++) col->mass_out[off[s] + j] = double(S.m[j]);
+      for (size_t e = 0; e < S.ev.size(); e += 3)
+        ev[s].insert(ev[s].end(), {S.ev[e], off[s] + S.ev[e + 1], off[s] + S.ev[e + 2]});
+    }
+  }
+  if (col && col->radius) {
+    std::vector<std::array<int64_t, 3>> all;
+    for (int s = 0; s < n_sys; s++)
+      for (size_t e = 0; e < ev[s].size(); e += 3) all.push_back({ev[s][e], ev[s][e + 1], ev[s][e + 2]});
+    std::stable_sort(all.begin(), all.end(), [](const std::array<int64_t, 3>& x, const std::array<int64_t, 3>& y) {
+      const int64_t xa = std::min(x[1], x[2]), ya = std::min(y[1], y[2]);
+      const int64_t xb = std::max(x[1], x[2]), yb = std::max(y[1], y[2]);
+      return x[0] != y[0] ? x[0] < y[0] : (xa != ya ? xa < ya : xb < yb);
+    });
+    for (const auto& e : all) col->events.insert(col->events.end(), e.begin(), e.end());
   }
   if (stats) {
     for (int s = 0; s < n_sys; s++) {
@@ -350,6 +440,36 @@ int oracle_run(const merc_params* mp, int n_sys, const int64_t* off, const int32
   if (precision == 2)
     return run_impl<double, MercMath>(mp, n_sys, off, nm, mass, pos, vel, alag, flags, n_steps, stats);
   return run_impl<double, StdMath>(mp, n_sys, off, nm, mass, pos, vel, alag, flags, n_steps, stats);
+}
+
+// oracle_run with physical collisions: radius[n_total] (AU), mass in/out
+// (merged masses written back), step0 = steps since load before the call.
+// events: room for 3 x max_events int64 (step, survivor, absorbed), *n_events
+// gets the total.
+int oracle_run_collide(const merc_params* mp, int n_sys, const int64_t* off, const int32_t* nm, double* mass,
+                       const double* radius, double* pos, double* vel, double* alag, uint32_t* flags,
+                       int64_t n_steps, int precision, int64_t* stats, int64_t step0, int64_t* events,
+                       int64_t max_events, int64_t* n_events) {
+  int st = check_layout(n_sys, off, nm);
+  if (st) return st;
+  if (!radius || !mass || !flags) return MERC_ERR_CONFIG;
+  const int64_t ntot = off[n_sys];
+  std::vector<double> m_in(mass, mass + ntot);
+  CollideIO io;
+  io.radius = radius;
+  io.mass_out = mass;
+  io.step0 = step0;
+  if (precision == 1)
+    st = run_impl<long double, StdMath>(mp, n_sys, off, nm, m_in.data(), pos, vel, alag, flags, n_steps, stats, &io);
+  else if (precision == 2)
+    st = run_impl<double, MercMath>(mp, n_sys, off, nm, m_in.data(), pos, vel, alag, flags, n_steps, stats, &io);
+  else
+    st = run_impl<double, StdMath>(mp, n_sys, off, nm, m_in.data(), pos, vel, alag, flags, n_steps, stats, &io);
+  const int64_t ne = (int64_t)io.events.size() / 3;
+  if (n_events) *n_events = ne;
+  for (int64_t k = 0; k < std::min(ne, max_events); k++)
+    for (int c = 0; c < 3; c++) events[3 * k + c] = io.events[3 * k + c];
+  return st;
 }
 
 // Batch boundary: reverse DH, elements, cartesian, forward DH (sim.cuh:744-765,

@@ -86,6 +86,8 @@ class Oracle:
                                            _f64p, C.c_int]
         L.oracle_run.argtypes = [C.POINTER(MercParams), C.c_int, _i64p, _i32p, _f64p, _f64p, _f64p, _f64p, _u32p,
                                  C.c_int64, C.c_int, _i64p]
+        L.oracle_run_collide.argtypes = [C.POINTER(MercParams), C.c_int, _i64p, _i32p, _f64p, _f64p, _f64p, _f64p,
+                                         _f64p, _u32p, C.c_int64, C.c_int, _i64p, C.c_int64, _i64p, C.c_int64, _i64p]
         L.oracle_roundtrip.argtypes = [C.POINTER(MercParams), C.c_int, _i64p, _i32p, _f64p, _f64p, _f64p, _f64p,
                                        C.c_int]
         L.oracle_to_elements.argtypes = [C.POINTER(MercParams), C.c_int, _i64p, _i32p, _f64p, _f64p, _f64p, _f64p,
@@ -138,6 +140,32 @@ class Oracle:
         if st:
             raise ValueError(f"oracle_run status {st}")
         return pos, vel, alag, flags, stats
+
+    def run_collide(self, params, offsets, n_massive, mass, radius, pos, vel, alag, flags=None, steps=1,
+                    precision=0, step0=0, max_events=65536):
+        """run() with physical collisions: returns (pos, vel, alag, flags,
+        stats[4], mass, events (k x 3: step, survivor, absorbed))."""
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        nm = np.ascontiguousarray(n_massive, dtype=np.int32)
+        n = int(off[-1])
+        pos = _f64(pos).copy()
+        vel = _f64(vel).copy()
+        alag = _f64(alag).copy()
+        mass = _f64(mass).copy()
+        rad = _f64(radius)
+        flags = np.zeros(n, np.uint32) if flags is None else np.ascontiguousarray(flags, np.uint32).copy()
+        stats = np.zeros(4, np.int64)
+        ev = np.zeros(3 * max_events, np.int64)
+        ne = C.c_int64(0)
+        st = self.L.oracle_run_collide(C.byref(params), len(nm), _ptr(off, _i64p), _ptr(nm, _i32p),
+                                       _ptr(mass, _f64p), _ptr(rad, _f64p), _ptr(pos, _f64p), _ptr(vel, _f64p),
+                                       _ptr(alag, _f64p), _ptr(flags, _u32p), int(steps), int(precision),
+                                       _ptr(stats, _i64p), int(step0), _ptr(ev, _i64p), int(max_events),
+                                       C.byref(ne))
+        if st:
+            raise ValueError(f"oracle_run_collide status {st}")
+        k = min(ne.value, max_events)
+        return pos, vel, alag, flags, stats, mass, ev[:3 * k].reshape(-1, 3)
 
     def roundtrip(self, params, offsets, n_massive, mass, pos, vel, precision=0):
         off = np.ascontiguousarray(offsets, dtype=np.int64)

@@ -27,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <array>
 #include <mutex>
@@ -45,6 +46,7 @@ using namespace merc;
 #include "merc_mlp.cuh"
 #include "merc_kernels.cuh"
 #include "merc_sweep.cuh"
+#include "merc_collide.cuh"
 
 // ---------------------------------------------------------------------------
 // context
@@ -117,6 +119,9 @@ struct merc_ctx {
   unsigned long long* d_log_count = nullptr;
   long long log_cap = 0;
   double last_ms = 0.0;
+  // physical collisions (merc_set_radii): buffers allocated with the state
+  Collide col;
+  bool collide_on = false;
 };
 
 namespace {
@@ -169,6 +174,8 @@ void free_all(merc_ctx* ctx) {
   for (void* a : ctx->allocs) cudaFree(a);
   ctx->allocs.clear();
   ctx->D = Dev();
+  ctx->col = Collide();
+  ctx->collide_on = false;
   ctx->loaded = false;
 }
 
@@ -471,12 +478,17 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     if (bx)
       k_encounter_big_exact<<<ctx->sms, kExactRowThreads * p.bs_rows, 0, s>>>(D, rcB, p.dt, p.compat_block,
                                                                               p.bs_rows, p.softening2);
+    if (ctx->collide_on) {
+      k_collide_find<<<ctx->sms * 4, 256, 0, s>>>(D, ctx->col);
+      k_collide_resolve<<<1, 32, 0, s>>>(D, ctx->col, p.hill_factor);
+      nk += 2;
+    }
     momentum_exact(D.vo);
     k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.xo, D.vo, rcB, hdt);
     if ((st = kick_ev(2))) return st;
     kick_exact_all(rcB, rcA, 1);
     if ((st = kick_ev(3))) return st;
-    nk = 8 + 6 * bx;
+    nk += 8 + 6 * bx;
   } else {
     // programmatic dependent launches: a kernel may be scheduled while its
     // predecessor finishes; every kernel here waits for it (griddep_wait)
@@ -642,6 +654,11 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       nk++;
     }
     if (fork) CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+    if (ctx->collide_on) {
+      launch(k_collide_find, ctx->sms * 4, 256, D, ctx->col);
+      launch(k_collide_resolve, 1, 32, D, ctx->col, p.hill_factor);
+      nk += 2;
+    }
     momentum(D.vo);
     if (jump_cl)
       launch(k_jump_cluster<false>, njc, kJumpThreads, D, (const double*)D.xo, (const double*)D.vo, rcB, hdt);
@@ -744,8 +761,8 @@ size_t sweep_smem_bytes(const merc_ctx* ctx) {
 // so a few large systems (the reference's Planet Nine sweep: 4 to 32 systems
 // of 10240 bodies) fill the GPU as well as thousands of small ones.
 bool use_persistent(const merc_ctx* ctx) {
-  return ctx->p.drift == MERC_DRIFT_UNIVERSAL && !ctx->has_big && ctx->log_cap == 0 && ctx->nmax_sys > 0 &&
-         sweep_smem_bytes(ctx) <= (size_t)ctx->smem_optin;
+  return ctx->p.drift == MERC_DRIFT_UNIVERSAL && !ctx->has_big && ctx->log_cap == 0 && !ctx->collide_on &&
+         ctx->nmax_sys > 0 && sweep_smem_bytes(ctx) <= (size_t)ctx->smem_optin;
 }
 
 // Work items for blocks of `threads` and a grid of at most `grid` blocks:
@@ -1147,6 +1164,71 @@ int merc_get_a_lag(merc_ctx* ctx, double* a_lag) {
   return MERC_OK;
 }
 
+int merc_set_radii(merc_ctx* ctx, const double* radius) {
+  if (!ctx) return MERC_ERR_CONFIG;
+  if (!ctx->loaded) return fail(ctx, MERC_ERR_STATE, "merc_set_radii before a load");
+  CK(cudaSetDevice(ctx->device));
+  drop_graphs(ctx);  // the step graphs gain or lose the collision kernels
+  if (!radius) {
+    ctx->collide_on = false;
+    return MERC_OK;
+  }
+  const int n = ctx->D.n;
+  for (int j = 0; j < n; j++)
+    if (!(radius[j] >= 0.0) || !std::isfinite(radius[j]))
+      return fail(ctx, MERC_ERR_CONFIG, "radius[%d] must be finite and >= 0", j);
+  Collide& C = ctx->col;
+  int st;
+  if (!C.radius) {
+    double* r = nullptr;
+    if ((st = dalloc(ctx, &r, n)) || (st = dalloc(ctx, &C.n_pairs, 2)) || (st = dalloc(ctx, &C.pairs, kColPairCap)) ||
+        (st = dalloc(ctx, &C.step, 1)) || (st = dalloc(ctx, &C.n_events, 1)) ||
+        (st = dalloc(ctx, &C.events, 3 * (size_t)kColEventCap)))
+      return st;
+    C.radius = r;
+    C.m = ctx->d_m;
+  }
+  const long long step0 = ctx->steps_done, zero = 0;
+  CK(cudaMemcpyAsync((void*)C.radius, radius, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(C.n_pairs, 0, 2 * sizeof(int), ctx->stream));
+  CK(cudaMemcpyAsync(C.step, &step0, sizeof step0, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(C.n_events, &zero, sizeof zero, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->collide_on = true;
+  return MERC_OK;
+}
+
+int merc_get_collisions(merc_ctx* ctx, merc_collision* out, int64_t max, int64_t* count) {
+  if (!ctx || max < 0 || (max > 0 && !out)) return MERC_ERR_CONFIG;
+  if (!ctx->loaded) return fail(ctx, MERC_ERR_STATE, "merc_get_collisions before a load");
+  long long total = 0;
+  int lost = 0;
+  if (ctx->col.n_events) {
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpy(&total, ctx->col.n_events, sizeof total, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&lost, ctx->col.n_pairs + 1, sizeof lost, cudaMemcpyDeviceToHost));
+  }
+  if (count) *count = total;
+  const int64_t k = std::min<int64_t>(std::min<int64_t>(total, kColEventCap), max);
+  if (k > 0) {
+    std::vector<long long> ev(3 * (size_t)k);
+    CK(cudaMemcpy(ev.data(), ctx->col.events, sizeof(long long) * ev.size(), cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < k; i++) out[i] = merc_collision{ev[3 * i], ev[3 * i + 1], ev[3 * i + 2]};
+  }
+  if (lost) return fail(ctx, MERC_ERR_STATE, "more than %d collision candidates in one step: some were dropped",
+                        kColPairCap);
+  return MERC_OK;
+}
+
+int merc_get_masses(merc_ctx* ctx, double* mass) {
+  if (!ctx || !mass) return MERC_ERR_CONFIG;
+  if (!ctx->loaded) return fail(ctx, MERC_ERR_STATE, "merc_get_masses before a load");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpyAsync(mass, ctx->d_m, sizeof(double) * ctx->D.n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return MERC_OK;
+}
+
 int merc_get_elements(merc_ctx* ctx, double* elements) {
   if (!ctx || !elements) return MERC_ERR_CONFIG;
   if (!ctx->loaded) return fail(ctx, MERC_ERR_STATE, "merc_get_elements before a load");
@@ -1273,12 +1355,14 @@ int merc_mlp_append_log(merc_ctx* ctx, const float* samples, int64_t n) {
 }
 
 // ---- checkpoint file ----
-// Little-endian binary: "MERCCKP1", uint32 version (2), uint32 sizeof(merc_params),
+// Little-endian binary: "MERCCKP1", uint32 version (3), uint32 sizeof(merc_params),
 // merc_params, int32 n_systems, int64 n_bodies, int64 steps_done,
 // int64 body_offset[n_systems + 1], int32 n_massive[n_systems], double
 // mass[n], pos[3n], vel[3n], a_lag[n], uint32 flags[n], uint64 counters[5],
-// uint32 has_mlp, float mlp[MERC_MLP_BLOB] (when has_mlp), then the FNV-1a
-// 64-bit hash of every byte before it.
+// uint32 has_mlp, float mlp[MERC_MLP_BLOB] (when has_mlp), uint32 has_radii and,
+// when set, double radius[n], int64 collision step counter, int64 events,
+// int64 event log[3 min(events, 65536)], then the FNV-1a 64-bit hash of every
+// byte before it.  Version 2 files (no collision block) are read too.
 struct CkptWriter {
   std::FILE* f;
   uint64_t h = 1469598103934665603ull;
@@ -1326,10 +1410,23 @@ int merc_save_checkpoint(merc_ctx* ctx, const char* path) {
     mlp.resize(kBlob);
     if ((st = merc_mlp_get_weights(ctx, mlp.data()))) return st;
   }
+  const uint32_t has_radii = ctx->collide_on ? 1u : 0u;
+  std::vector<double> radii;
+  long long col_step = 0, col_events = 0;
+  std::vector<long long> events;
+  if (has_radii) {
+    radii.resize(n);
+    CK(cudaMemcpy(radii.data(), ctx->col.radius, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&col_step, ctx->col.step, sizeof col_step, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&col_events, ctx->col.n_events, sizeof col_events, cudaMemcpyDeviceToHost));
+    events.resize(3 * (size_t)std::min<long long>(col_events, kColEventCap));
+    if (!events.empty())
+      CK(cudaMemcpy(events.data(), ctx->col.events, sizeof(long long) * events.size(), cudaMemcpyDeviceToHost));
+  }
   std::FILE* f = std::fopen(path, "wb");
   if (!f) return fail(ctx, MERC_ERR_CONFIG, "cannot open %s for writing", path);
   CkptWriter w{f};
-  const uint32_t version = 2, psize = sizeof(merc_params), has_mlp = ctx->mlp_ready ? 1u : 0u;
+  const uint32_t version = 3, psize = sizeof(merc_params), has_mlp = ctx->mlp_ready ? 1u : 0u;
   const int64_t steps = ctx->steps_done;
   w.put("MERCCKP1", 8);
   w.put(&version, 4);
@@ -1348,6 +1445,13 @@ int merc_save_checkpoint(merc_ctx* ctx, const char* path) {
   w.put(counters, sizeof counters);
   w.put(&has_mlp, 4);
   if (has_mlp) w.put(mlp.data(), 4 * mlp.size());
+  w.put(&has_radii, 4);
+  if (has_radii) {
+    w.put(radii.data(), 8 * radii.size());
+    w.put(&col_step, 8);
+    w.put(&col_events, 8);
+    w.put(events.data(), 8 * events.size());
+  }
   const uint64_t hash = w.h;
   w.put(&hash, 8);
   const bool ok = w.ok && std::fclose(f) == 0;
@@ -1380,7 +1484,7 @@ int merc_load_checkpoint(merc_ctx* ctx, const char* path) {
   r.get(magic, 8);
   r.get(&version, 4);
   r.get(&psize, 4);
-  if (version != 2 || psize != sizeof(merc_params))
+  if ((version != 2 && version != 3) || psize != sizeof(merc_params))
     return fail(ctx, MERC_ERR_CONFIG, "%s: checkpoint version %u not supported", path, version);
   r.get(&p, sizeof p);
   r.get(&nsys, 4);
@@ -1407,6 +1511,22 @@ int merc_load_checkpoint(merc_ctx* ctx, const char* path) {
     mlp.resize(kBlob);
     r.get(mlp.data(), 4 * mlp.size());
   }
+  uint32_t has_radii = 0;
+  std::vector<double> radii;
+  long long col_step = 0, col_events = 0;
+  std::vector<long long> events;
+  if (version >= 3) {
+    r.get(&has_radii, 4);
+    if (has_radii) {
+      radii.resize(n);
+      r.get(radii.data(), 8 * radii.size());
+      r.get(&col_step, 8);
+      r.get(&col_events, 8);
+      if (!r.ok || col_events < 0) return fail(ctx, MERC_ERR_CONFIG, "%s: bad collision block", path);
+      events.resize(3 * (size_t)std::min<long long>(col_events, kColEventCap));
+      r.get(events.data(), 8 * events.size());
+    }
+  }
   if (!r.ok || r.pos + 8 != buf.size()) return fail(ctx, MERC_ERR_CONFIG, "%s: truncated", path);
   int st;
   if ((st = merc_set_params(ctx, &p)) ||
@@ -1418,6 +1538,13 @@ int merc_load_checkpoint(merc_ctx* ctx, const char* path) {
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->steps_done = steps;
   if (has_mlp && (st = merc_mlp_set_weights(ctx, mlp.data()))) return st;
+  if (has_radii) {
+    if ((st = merc_set_radii(ctx, radii.data()))) return st;
+    CK(cudaMemcpy(ctx->col.step, &col_step, sizeof col_step, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->col.n_events, &col_events, sizeof col_events, cudaMemcpyHostToDevice));
+    if (!events.empty())
+      CK(cudaMemcpy(ctx->col.events, events.data(), sizeof(long long) * events.size(), cudaMemcpyHostToDevice));
+  }
   return MERC_OK;
 }
 

@@ -33,6 +33,10 @@ FLAG_CE_LAST = 1
 FLAG_CE_EVER = 2
 FLAG_EJECTED = 4
 FLAG_NONFINITE = 8
+FLAG_MERGED = 16
+FLAG_GREW = 32
+MERGED_MASS = 1e-300
+PARK_R = 1e6
 
 _i64p = C.POINTER(C.c_int64)
 _i32p = C.POINTER(C.c_int32)
@@ -81,6 +85,12 @@ class MercError(RuntimeError):
 _LIB = None
 
 
+class Collision(C.Structure):
+    """Mirror of ``merc_collision`` in include/merc.h."""
+
+    _fields_ = [("step", C.c_int64), ("survivor", C.c_int64), ("absorbed", C.c_int64)]
+
+
 def lib() -> C.CDLL:
     """Load libmerc.so (once).  Raises if it has not been built."""
     global _LIB
@@ -114,6 +124,9 @@ def lib() -> C.CDLL:
     L.merc_load_systems.argtypes = [vp, C.POINTER(SystemDesc), C.c_int32]
     L.merc_launch_count.argtypes = [vp]
     L.merc_launch_count.restype = C.c_int64
+    L.merc_set_radii.argtypes = [vp, _f64p]
+    L.merc_get_collisions.argtypes = [vp, C.POINTER(Collision), C.c_int64, C.POINTER(C.c_int64)]
+    L.merc_get_masses.argtypes = [vp, _f64p]
     L.merc_step_static.argtypes = [C.c_int, C.POINTER(MercParams), C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
     _f32p = C.POINTER(C.c_float)
@@ -281,6 +294,28 @@ class Integrator:
             flags = np.empty(self.n, np.uint32)
         self._check(self.L.merc_get_state(self.h, _p(pos, _f64p), _p(vel, _f64p), _p(flags, _u32p)))
         return State(pos, vel, flags)
+
+    def set_radii(self, radius=None):
+        """Physical collisions (merc_set_radii): radii in AU for every body, or
+        None to switch detection off."""
+        r = _f64(radius) if radius is not None else None
+        if r is not None and r.size != self.n:
+            raise ValueError("one radius per body")
+        self._check(self.L.merc_set_radii(self.h, _p(r, _f64p)))
+
+    def collisions(self) -> np.ndarray:
+        """Resolved collisions: int64 array of rows (step, survivor, absorbed)."""
+        cnt = C.c_int64(0)
+        self._check(self.L.merc_get_collisions(self.h, None, 0, C.byref(cnt)))
+        k = min(cnt.value, 65536)
+        buf = (Collision * max(k, 1))()
+        self._check(self.L.merc_get_collisions(self.h, buf, k, C.byref(cnt)))
+        return np.array([(c.step, c.survivor, c.absorbed) for c in buf[:k]], dtype=np.int64).reshape(-1, 3)
+
+    def masses(self) -> np.ndarray:
+        m = np.empty(self.n)
+        self._check(self.L.merc_get_masses(self.h, _p(m, _f64p)))
+        return m
 
     def a_lag(self) -> np.ndarray:
         a = np.empty(self.n)

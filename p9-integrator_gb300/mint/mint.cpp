@@ -90,6 +90,7 @@ struct Body {
   std::string name;
   double mass;
   double el[6];
+  double radius;  // optional "radius" key (AU); collisions are detected when any body has one
 };
 
 struct Config {
@@ -106,6 +107,7 @@ Body read_body(const mintjson::Value& v) {
   b.name = v.string_or("name", "");
   b.mass = v.number("mass");
   for (int k = 0; k < 6; k++) b.el[k] = v.number(kElementKeys[k]);
+  b.radius = v.number_or("radius", -1.0);
   return b;
 }
 
@@ -186,12 +188,15 @@ int main(int argc, char** argv) {
     const int64_t ntot = (int64_t)nb * nsys;
     std::vector<int64_t> off(nsys + 1);
     std::vector<int32_t> nmv(nsys, nm);
-    std::vector<double> mass(ntot), el(6 * ntot);
+    std::vector<double> mass(ntot), el(6 * ntot), radius(ntot);
+    bool radii = false;
+    for (auto& b : c.bodies) radii = radii || b.radius >= 0.0;
     for (int s = 0; s < nsys; s++) {
       off[s + 1] = off[s] + nb;
       for (int j = 0; j < nb; j++) {
         int64_t g = off[s] + j;
         mass[g] = c.bodies[j].mass;
+        radius[g] = std::max(0.0, c.bodies[j].radius);
         for (int k = 0; k < 6; k++) el[k * ntot + g] = c.bodies[j].el[k];
       }
       if (!sweep_of.empty()) {  // body 0 takes the sweep's elements, M = 0, mass unchanged
@@ -216,6 +221,7 @@ int main(int argc, char** argv) {
     long long first_batch = 0;
     if (a.resume.empty()) {
       check(merc_load_elements(ctx, nsys, off.data(), nmv.data(), mass.data(), el.data()), ctx, "load");
+      if (radii) check(merc_set_radii(ctx, radius.data()), ctx, "radii");
     } else {
       check(merc_load_checkpoint(ctx, a.resume.c_str()), ctx, "resume");
       merc_stats rs;
@@ -288,6 +294,11 @@ int main(int argc, char** argv) {
       check(merc_roundtrip(ctx), ctx, "roundtrip");
       if (!a.checkpoint.empty() && (checkpoint || batch == iters - 1))
         check(merc_save_checkpoint(ctx, a.checkpoint.c_str()), ctx, "checkpoint");
+    }
+    if (radii && a.info) {
+      int64_t ncol = 0;
+      check(merc_get_collisions(ctx, nullptr, 0, &ncol), ctx, "collisions");
+      std::cout << "Collisions: " << ncol << std::endl;
     }
     merc_destroy(ctx);
     return 0;
