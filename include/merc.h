@@ -50,7 +50,7 @@ extern "C" {
 
 /* warm start of the universal-variable solve */
 #define MERC_WARM_PLAIN 0  /* s0 = dt / r0 */
-#define MERC_WARM_MLP 1    /* FP32 MLP guess, then the same FP64 Newton */
+#define MERC_WARM_MLP 1    /* FP32 MLP guess for long drifts (dt / r0^1.5 >= 0.03), else the series guess; same FP64 Newton */
 #define MERC_WARM_SERIES 2 /* the Kepler equation inverted to third order in dt (default) */
 
 /* per-body flags (uint32) */

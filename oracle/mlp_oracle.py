@@ -4,7 +4,9 @@ and of the GPU inference.
 
 Blob layout (MERC_MLP_BLOB = 1267 floats): W1[32][4], b1[32], W2[32][32],
 b2[32], W3[32], b3, in_mean[4], in_scale[4], out_mean, out_scale,
-box_lo[4], box_hi[4].  Samples: 5 floats (x1, x2, x3, x4, target).
+box_lo[4], box_hi[4].  Samples: 5 floats (ln x1, x2, x3, x4, target y); the
+guess is s = (dt / r0) exp(z), z = -x1 x3 / (2 (1 + x1^2)) + y x1^2 / (1 + x1^2)
+(p9-integrator_gb300/csrc/merc_mlp.cuh).
 """
 import numpy as np
 
@@ -60,7 +62,8 @@ def loss_and_grad(blob, samples):
 
 
 def guess(blob, pos, vel, dt):
-    """Warm-start guess of the universal anomaly for drift inputs (3 x n)."""
+    """Warm-start guess of the universal anomaly for drift inputs (3 x n); NaN
+    where the network is not consulted (outside its box, or x1 < 0.03)."""
     b = np.asarray(blob, np.float64)
     x = np.asarray(pos).reshape(3, -1)
     v = np.asarray(vel).reshape(3, -1)
@@ -70,10 +73,13 @@ def guess(blob, pos, vel, dt):
     s0 = dt / r0
     f = np.stack([dt / r0 ** 1.5, r0 * v2, eta / np.sqrt(r0), np.where(2 - r0 * v2 < 0, 1.0, -1.0)], 1)
     f = f.astype(np.float32).astype(np.float64)
-    inside = np.all((f >= b[BOX_LO:BOX_LO + 4]) & (f <= b[BOX_HI:BOX_HI + 4]), axis=1) & (f[:, 0] >= 1e-5)
+    u = f.copy()
+    u[:, 0] = np.log(f[:, 0])
+    inside = np.all((u >= b[BOX_LO:BOX_LO + 4]) & (u <= b[BOX_HI:BOX_HI + 4]), axis=1) & (f[:, 0] >= np.float32(0.03))
     w1, b1, w2, b2, w3, b3 = unpack(b)
-    xn = (f - b[IN_MEAN:IN_MEAN + 4]) * b[IN_SCALE:IN_SCALE + 4]
+    xn = (u - b[IN_MEAN:IN_MEAN + 4]) * b[IN_SCALE:IN_SCALE + 4]
     yn = silu(silu(xn @ w1.T + b1) @ w2.T + b2) @ w3 + b3
     y = yn / b[OUT_SCALE] + b[OUT_MEAN]
-    delta = f[:, 0] * (f[:, 0] * y - 0.5 * f[:, 2])
-    return np.where(inside, s0 * (1 + delta), s0)
+    q = f[:, 0] ** 2
+    z = (y * q - 0.5 * f[:, 0] * f[:, 2]) / (1 + q)
+    return np.where(inside, s0 * np.exp(z), np.nan)

@@ -568,7 +568,7 @@ __device__ __forceinline__ double f64_of_f32(float x) {
 // r0; kGuessSeries: the universal Kepler equation t = r0 s + eta s^2/2 + zeta
 // s^3/6 + O(s^4) inverted to third order, s = s0 (1 - (eta / 2 r0) s0 + ((3
 // eta^2 - r0 zeta) / 6 r0^2) s0^2) with s0 = dt / r0, kept when within a factor
-// 2 of s0; kGuessRel: s0 (1 + rel), kept under the same condition): Newton on
+// 2 of s0; kGuessRel: s0 (1 + rel), kept within a factor 16): Newton on
 // r0 s + eta G2 + zeta G3 = dt; after each update the
 // Newton error estimate |f''/(2 f')| ds^2 of the new s is compared with tol |s|
 // (trusted once |ds| <= 1e-3 |s|), in FP32 on truncated copies (the decision
@@ -592,8 +592,9 @@ __device__ __forceinline__ UD universal_drift(const FU& U, const d3& x0, const d
       const double q = fmul(U, p0, fma(p0, fma(p0, a2, -a1), 1.0));
       if (q > 0.5 * p0 && q < 2.0 * p0) g = q;
     } else if (s0 == kGuessRel) {
+      // the learned guess covers long drifts, where s/s0 spans ~0.1..4
       const double q = fma(p0, f64_of_f32(rel), p0);
-      if (q > 0.5 * p0 && q < 2.0 * p0) g = q;
+      if (q > 0.0625 * p0 && q < 16.0 * p0) g = q;
     }
     s0 = g;
   }

@@ -403,7 +403,9 @@ int dh_convert(merc_ctx* ctx, bool reverse) {
 
 // initial guess of the universal drift for the parameters (the network's
 // fallback outside its box is the plain guess)
-double guess_of(const merc_params& p) { return p.warm_start == MERC_WARM_SERIES ? kGuessSeries : kGuessPlain; }
+// the guess of a solve the network does not serve (MERC_WARM_MLP outside its
+// feature box) is the series guess
+double guess_of(const merc_params& p) { return p.warm_start == MERC_WARM_PLAIN ? kGuessPlain : kGuessSeries; }
 
 // Launch on the step stream.  With pdl (programmatic dependent launch) the
 // kernel may be scheduled while its predecessor is still running; every kernel
@@ -749,9 +751,7 @@ int sweep_nh(const merc_ctx* ctx) {
 }
 
 size_t sweep_smem_bytes(const merc_ctx* ctx) {
-  size_t b = 2 * 8 * hist_step_doubles(sweep_nh(ctx)) * kSweepChunk;  // two history buffers
-  if (ctx->p.warm_start == MERC_WARM_MLP && ctx->mlp_ready) b += 4 * (size_t)kBlob;
-  return b;
+  return 2 * 8 * hist_step_doubles(sweep_nh(ctx)) * kSweepChunk;  // two history buffers
 }
 
 // The persistent kernel keeps only the massive bodies and their history in
@@ -1771,8 +1771,8 @@ __global__ void k_mlp_probe(int n, const double* pos, const double* vel, double 
   float rel = 0.0f;
   if (blob) {
     float f[4];
-    warm_features_f32(x, v, f32_trunc(dt), f);
-    if (f[0] >= kWarmMinX1) {
+    if (warm_long(x, f32_trunc(dt))) {
+      warm_features_f32(x, v, f32_trunc(dt), f);
       const float d = warm_delta(blob, f);
       if (d == d) {
         s0 = kGuessRel;

@@ -1268,7 +1268,8 @@ __global__ void __launch_bounds__(kMomThreads) k_momentum_big(Dev D, const int* 
 // guess: kGuessPlain or kGuessSeries (universal_drift); mlp != nullptr:
 // learned warm start of the solve (merc_mlp.cuh).  log_data
 // != nullptr: every solve with x1 >= kWarmMinX1 appends its features and
-// training target (5 floats) while the log has room.
+// training target (5 floats) while the log has room; the network is
+// consulted for drifts with x1 >= kWarmNetX1 (warm_long, merc_mlp.cuh).
 constexpr float kWarmMinX1 = 1e-5f;
 #ifndef MERC_DRIFT_THREADS
 #define MERC_DRIFT_THREADS 128
@@ -1313,8 +1314,8 @@ __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, doubl
       if (log_data) w = warm_features(pos, vel, dt);  // the logged features in FP64
       if (mlp) {
         float f[4];
-        warm_features_f32(pos, vel, f32_trunc(dt), f);
-        if (f[0] >= kWarmMinX1) {
+        if (warm_long(pos, f32_trunc(dt))) {
+          warm_features_f32(pos, vel, f32_trunc(dt), f);
           const float d = warm_delta(blob, f);
           if (d == d) {
             s0 = kGuessRel;
@@ -1330,7 +1331,7 @@ __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, doubl
       solved = 1;
       if (log_data && u.converged && w.f[0] >= kWarmMinX1) {
         logit = true;
-        rec[0] = w.f[0];
+        rec[0] = warm_input0(w);
         rec[1] = w.f[1];
         rec[2] = w.f[2];
         rec[3] = w.f[3];

@@ -2,16 +2,21 @@
 //
 // A 4 -> 32 -> 32 -> 1 SiLU network in FP32 predicts the universal anomaly s
 // of a drift.  With mu = 1, r0 = |x0|, eta = x0.v0, alpha = 2/r0 - v0^2, the
-// plain guess is s0 = dt / r0 and the solution is s = s0 (1 + delta) with
-//   delta = -x1 x3 / 2 + x1^2 y,
+// plain guess is s0 = dt / r0, and the drift is fixed by the dimensionless
 //   x1 = dt / r0^1.5,  x2 = r0 v0^2,  x3 = eta / sqrt(r0),  x4 = sign of the energy.
-// The network predicts y (the part of delta beyond its first-order term),
-// from the features normalised by the training set's mean and spread.  At
-// inference the features and delta are computed in FP32 (warm_features_f32,
-// warm_delta) and the drift forms s0 (1 + delta) from its own FP64 s0.  The
-// FP64 Newton solve that follows is unchanged; the guess only moves its
-// starting point.  Outside the feature box seen in training the plain guess
-// is used.
+// The solution is written s = s0 exp(z) with
+//   z = -x1 x3 / (2 (1 + x1^2)) + y x1^2 / (1 + x1^2):
+// for short drifts (x1 << 1) z tends to its series -x1 x3 / 2 + O(x1^2) and
+// the network's error in y enters scaled by x1^2; for long ones (pericentre
+// passages, hyperbolic flybys, x1 up to ~10) s/s0 ranges over a factor ~30
+// and the error in y enters unscaled.  The network sees ln x1, x2, x3, x4
+// (the logged samples store ln x1), normalised by the training set's mean and
+// spread, and predicts y.  At inference the features and exp(z) - 1 are
+// computed in FP32 (warm_features_f32, warm_delta) and the drift forms
+// s0 (1 + delta) from its own FP64 s0.  The FP64 Newton solve that follows is
+// unchanged; the guess only moves its starting point.  Outside the feature box
+// seen in training, and for short drifts (x1 < kWarmNetX1, where the series
+// guess needs one iteration), the series guess is used.
 //
 // Parameter blob (floats): W1[32][4], b1[32], W2[32][32], b2[32], W3[32], b3,
 // then in_mean[4], in_scale[4], out_mean, out_scale, box_lo[4], box_hi[4].
@@ -61,6 +66,19 @@ __device__ __forceinline__ void warm_features_f32(const d3& x0, const d3& v0, fl
   f[3] = (2.0f - r0 * v2) < 0.0f ? 1.0f : -1.0f;
 }
 
+// The network is consulted only for drifts with x1 >= kWarmNetX1: below it the
+// series guess already converges in one Newton iteration (the embryo disk,
+// x1 ~ 0.01, the sweep and the planetesimal disk) and the network's ~1200 FP32
+// multiply-adds per body would cost more than they save.  warm_long decides
+// it from FP32 truncations without a root: x1^4 = dt^4 / r0^6 >= kWarmNetX1^4.
+constexpr float kWarmNetX1 = 0.03f;
+__device__ __forceinline__ bool warm_long(const d3& x0, float dtf) {
+  const float x = f32_trunc(x0.x), y = f32_trunc(x0.y), z = f32_trunc(x0.z);
+  const float r2 = fmaf(x, x, fmaf(y, y, z * z));
+  const float d2 = dtf * dtf, g2 = kWarmNetX1 * kWarmNetX1;
+  return d2 * d2 >= (g2 * g2) * (r2 * r2 * r2);
+}
+
 __device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
 
 // forward pass on normalised inputs; p points at the blob (shared or global)
@@ -85,22 +103,27 @@ __device__ __forceinline__ float mlp_forward(const float* __restrict__ p, const 
 }
 
 // Relative correction of the plain guess, s = (dt / r0) (1 + delta), from
-// FP32 features; NaN outside the trained feature box.
+// FP32 features x1..x4; NaN outside the trained feature box.
 __device__ __forceinline__ float warm_delta(const float* __restrict__ p, const float f[4]) {
+  const float u[4] = {__logf(f[0]), f[1], f[2], f[3]};
   float xn[4];
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    if (!(f[k] >= p[kBoxLo + k] && f[k] <= p[kBoxHi + k])) return __int_as_float(0x7fc00000);
-    xn[k] = (f[k] - p[kInMean + k]) * p[kInScale + k];
+    if (!(u[k] >= p[kBoxLo + k] && u[k] <= p[kBoxHi + k])) return __int_as_float(0x7fc00000);
+    xn[k] = (u[k] - p[kInMean + k]) * p[kInScale + k];
   }
   const float y = mlp_forward(p, xn) / p[kOutScale] + p[kOutMean];
-  return f[0] * fmaf(f[0], y, -0.5f * f[2]);
+  const float q = f[0] * f[0], iq = 1.0f / (1.0f + q);
+  return expm1f(iq * fmaf(y, q, -0.5f * f[0] * f[2]));
 }
 
-// training target y of a solved drift: (s/s0 - 1 + x1 x3 / 2) / x1^2
+// logged network input 0 of a drift: ln x1
+__device__ __forceinline__ float warm_input0(const WarmIn& w) { return (float)log((double)w.f[0]); }
+
+// training target y of a solved drift: (ln(s/s0) + x1 x3 / (2 (1 + x1^2))) (1 + x1^2) / x1^2
 __device__ __forceinline__ float warm_target(const WarmIn& w, double s) {
-  double x1 = (double)w.f[0], x3 = (double)w.f[2];
-  return (float)((s / w.s0 - 1.0 + 0.5 * x1 * x3) / (x1 * x1));
+  const double x1 = (double)w.f[0], x3 = (double)w.f[2], q = x1 * x1;
+  return (float)((log(s / w.s0) + 0.5 * x1 * x3 / (1.0 + q)) * (1.0 + q) / q);
 }
 
 // ---------------------------------------------------------------------------
@@ -112,7 +135,7 @@ __device__ __forceinline__ float warm_target(const WarmIn& w, double s) {
 constexpr int kMlpThreads = 128;
 
 // Loss 0.5 (f(xn) - t)^2 per sample.  Samples come from `data` (5 floats per
-// sample: raw x1..x4, target y), drawn by index hash from [0, n_data);
+// sample: ln x1, x2, x3, x4, target y), drawn by index hash from [0, n_data);
 // normalisation from the blob.  grad_part: [gridDim.x][kNet + 1] (last = loss).
 __global__ void __launch_bounds__(kMlpThreads) k_mlp_grad(const float* __restrict__ blob,
                                                           const float* __restrict__ data, long long n_data,

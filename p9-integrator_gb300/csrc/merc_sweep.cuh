@@ -133,8 +133,11 @@ struct SmemVelTotal {  // encounter sub-step velocity update, sources in shared 
 __global__ void __launch_bounds__(256, 2) k_sweep_persistent(SweepArgs A) {
   extern __shared__ double sm[];
   const int nh = A.nh, C = A.chunk;
-  double* hist = sm;                                           // 2 x C steps of history (double-buffered)
-  float* blob = (float*)(sm + 2 * hist_step_doubles(nh) * C);  // kBlob floats when warm start is on
+  double* hist = sm;  // 2 x C steps of history (double-buffered)
+  // the network's weights stay in global memory (read through L1): the gate
+  // keeps them off the sweep's short drifts, and 5 KB more shared memory per
+  // block would cost the small blocks occupancy
+  const float* __restrict__ blob = A.mlp;
   auto hist_buf = [&](int b) { return hist + (size_t)b * hist_step_doubles(nh) * C; };
   __shared__ double M[kSweepMaxNm], HC[kSweepMaxNm];           // masses, cbrt(m / 3) * hill
   __shared__ double XM[3 * kSweepMaxNm], VM[3 * kSweepMaxNm];  // massive state
@@ -143,11 +146,8 @@ __global__ void __launch_bounds__(256, 2) k_sweep_persistent(SweepArgs A) {
   __shared__ unsigned long long tally[kNumCounters];  // as Dev::counters
 
   const Dev& D = A.D;
-  const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const double hdt = 0.5 * A.dt;
-  if (A.mlp) {
-    for (int k = tid; k < kBlob; k += T) blob[k] = A.mlp[k];
-  }
   unsigned long long my_ce = 0, my_it = 0, my_sol = 0, my_nc = 0, my_simt = 0;
   // Kepler drift or encounter sub-step of one body whose sources are (Xs, Ts)
   auto drift = [&](d3& pos, d3& vel, int self, const Hist& h, int nm, bool& ce) {
@@ -165,8 +165,8 @@ __global__ void __launch_bounds__(256, 2) k_sweep_persistent(SweepArgs A) {
       float rel = 0.0f;
       if (A.mlp) {
         float f[4];
-        warm_features_f32(pos, vel, f32_trunc(A.dt), f);
-        if (f[0] >= kWarmMinX1) {
+        if (warm_long(pos, f32_trunc(A.dt))) {
+          warm_features_f32(pos, vel, f32_trunc(A.dt), f);
           const float d = warm_delta(blob, f);
           if (d == d) {
             s0 = kGuessRel;

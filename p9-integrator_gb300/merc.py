@@ -224,8 +224,12 @@ class Integrator:
         self.n, self.nsys = int(off[-1]), len(nm)
 
     def load_systems(self, sysm):
-        """Load a systems.Systems batch from its elements."""
-        self.load_elements(sysm.body_offset, sysm.n_massive, sysm.mass, sysm.elements)
+        """Load a systems.Systems batch from its elements (or from its cartesian
+        state, for batches that carry one in extra["pos"] / extra["vel"])."""
+        if "pos" in sysm.extra:
+            self.load_state(sysm.body_offset, sysm.n_massive, sysm.mass, sysm.extra["pos"], sysm.extra["vel"])
+        else:
+            self.load_elements(sysm.body_offset, sysm.n_massive, sysm.mass, sysm.elements)
 
     def load_system_list(self, descs):
         """Load systems given one dict each: n_massive, mass and either

@@ -203,6 +203,53 @@ def planetesimal_disk(seed: int = 20261207, n_planetesimals: int = 8192, n_test:
     return _pack([(m, el, 4 + n)], 0.25, 3.0, 1000, f"planetesimal-disk: {4 + n} massive + {n_test} tp")
 
 
+def hard_drifts(seed: int = 20261211, n: int = 3 * 65536, dt: float = 0.1) -> Systems:
+    """Kepler drifts the benchmark workloads rarely make, for the learned warm
+    start: massless test particles around the Sun alone (every step a pure
+    two-body drift), one third each on bound orbits with e U[0,0.99] anywhere
+    on the orbit (perihelion q log-U[0.2,5] AU), on bound orbits with e
+    U[0.5,0.99] within 1.5 rad of true anomaly from perihelion (q log-U[0.05,1]),
+    and on hyperbolic orbits with e U[1.02,4] within 0.9 of the asymptotic true
+    anomaly (q log-U[0.05,2]); random orientations; dt 0.1 yr (G = 1: a circular
+    orbit at 1 AU takes 2 pi yr).  The state is cartesian (extra["pos"],
+    extra["vel"]; there is no massive body, so democratic-heliocentric equals
+    heliocentric velocity); `elements` is left empty."""
+    rng = np.random.default_rng(seed)
+    k = n // 3
+    parts = []
+    for cls, m in (("any", k), ("peri", k), ("hyp", n - 2 * k)):
+        if cls == "any":
+            e = rng.uniform(0.0, 0.99, m)
+            q = np.exp(rng.uniform(np.log(0.2), np.log(5.0), m))
+            f = rng.uniform(-np.pi, np.pi, m)
+        elif cls == "peri":
+            e = rng.uniform(0.5, 0.99, m)
+            q = np.exp(rng.uniform(np.log(0.05), np.log(1.0), m))
+            f = rng.uniform(-1.5, 1.5, m)
+        else:
+            e = rng.uniform(1.02, 4.0, m)
+            q = np.exp(rng.uniform(np.log(0.05), np.log(2.0), m))
+            f = rng.uniform(-0.9, 0.9, m) * np.arccos(-1.0 / e)
+        p = q * (1.0 + e)
+        r = p / (1.0 + e * np.cos(f))
+        x = np.stack([r * np.cos(f), r * np.sin(f), np.zeros(m)])
+        v = np.stack([-np.sin(f), e + np.cos(f), np.zeros(m)]) / np.sqrt(p)
+        inc = np.arccos(rng.uniform(-1.0, 1.0, m))
+        node, peri = _uangle(rng, m), _uangle(rng, m)
+        cw, sw, co, so, ci, si = np.cos(peri), np.sin(peri), np.cos(node), np.sin(node), np.cos(inc), np.sin(inc)
+        rot = np.array([[co * cw - so * sw * ci, -co * sw - so * cw * ci],
+                        [so * cw + co * sw * ci, -so * sw + co * cw * ci],
+                        [sw * si, cw * si]])  # columns: perihelion direction, its normal in the plane
+        parts.append((np.einsum("ijm,jm->im", rot, x[:2]), np.einsum("ijm,jm->im", rot, v[:2])))
+    pos = np.concatenate([a for a, _ in parts], axis=1)
+    vel = np.concatenate([b for _, b in parts], axis=1)
+    out = Systems(np.array([0, n], np.int64), np.array([0], np.int32), np.zeros(n), np.zeros(0), dt, 3.0, 100,
+                  None, f"hard drifts: {n} test particles (e up to 0.99 near perihelion, hyperbolic), dt {dt}")
+    out.extra["pos"] = pos.reshape(-1).copy()
+    out.extra["vel"] = vel.reshape(-1).copy()
+    return out
+
+
 WORKLOADS = {0: outer_solar_system, 1: embryo_disk, 2: sweep, 4: planetesimal_disk}
 
 

@@ -16,12 +16,13 @@ pytestmark = pytest.mark.gpu
 def random_blob(rng):
     b = np.zeros(mlp_oracle.BLOB, np.float32)
     b[:mlp_oracle.NET] = rng.normal(0, 0.3, mlp_oracle.NET)
-    b[mlp_oracle.IN_MEAN:mlp_oracle.IN_MEAN + 4] = [0.01, 1.0, 0.0, 0.0]
-    b[mlp_oracle.IN_SCALE:mlp_oracle.IN_SCALE + 4] = [50.0, 2.0, 3.0, 1.0]
+    # network input 0 is ln x1
+    b[mlp_oracle.IN_MEAN:mlp_oracle.IN_MEAN + 4] = [-4.6, 1.0, 0.0, 0.0]
+    b[mlp_oracle.IN_SCALE:mlp_oracle.IN_SCALE + 4] = [0.5, 2.0, 3.0, 1.0]
     b[mlp_oracle.OUT_MEAN] = 0.1
     b[mlp_oracle.OUT_SCALE] = 4.0
-    b[mlp_oracle.BOX_LO:mlp_oracle.BOX_LO + 4] = [1e-5, 0.0, -2.0, -1.0]
-    b[mlp_oracle.BOX_HI:mlp_oracle.BOX_HI + 4] = [0.1, 2.5, 2.0, 1.0]
+    b[mlp_oracle.BOX_LO:mlp_oracle.BOX_LO + 4] = [np.log(1e-5), 0.0, -5.0, -1.0]
+    b[mlp_oracle.BOX_HI:mlp_oracle.BOX_HI + 4] = [np.log(20.0), 10.0, 5.0, 1.0]
     return b
 
 
@@ -29,7 +30,7 @@ def test_gradient_matches_cpu():
     rng = np.random.default_rng(5)
     blob = random_blob(rng)
     n = 300
-    S = np.stack([rng.uniform(1e-4, 0.05, n), rng.uniform(0.5, 1.5, n), rng.uniform(-0.5, 0.5, n),
+    S = np.stack([np.log(rng.uniform(1e-4, 0.05, n)), rng.uniform(0.5, 1.5, n), rng.uniform(-0.5, 0.5, n),
                   rng.choice([-1.0, 1.0], n), rng.normal(0.1, 0.3, n)], 1).astype(np.float32)
     loss, g = merc.mlp_grad(S, blob)
     loss_ref, g_ref = mlp_oracle.loss_and_grad(blob, S)
@@ -41,14 +42,18 @@ def test_gradient_matches_cpu():
 def test_inference_matches_cpu():
     rng = np.random.default_rng(6)
     blob = random_blob(rng)
-    s = systems.embryo_disk(n_embryos=126)
-    g = merc.Integrator(merc.default_params(dt=s.dt, hill_factor=3.0, drift=merc.DRIFT_UNIVERSAL))
-    g.load_systems(s)
-    st = g.state()
-    g.close()
-    guess, solved, its = merc.warm_start_probe(st.pos, st.vel, s.dt, blob)
-    ref = mlp_oracle.guess(blob, st.pos, st.vel, s.dt)
-    assert np.max(np.abs(guess - ref) / np.abs(ref)) < 1e-6
+    # long drifts, where the network is consulted (x1 >= 0.03)
+    s = systems.hard_drifts(n=4096, seed=6)
+    pos, vel = s.extra["pos"], s.extra["vel"]
+    guess, solved, its = merc.warm_start_probe(pos, vel, s.dt, blob)
+    ref = mlp_oracle.guess(blob, pos, vel, s.dt)
+    # (the drift keeps a learned guess within a factor 16 of dt / r0)
+    p0 = s.dt / np.linalg.norm(pos.reshape(3, -1), axis=0)
+    inside = np.isfinite(ref) & (ref > p0 / 16) & (ref < 16 * p0)
+    assert inside.sum() > 0.3 * inside.size
+    # FP32 inference against float64: the correction exp(z) - 1 carries the
+    # FP32 rounding of z (|z| up to ~1 on long drifts)
+    assert np.max(np.abs(guess[inside] - ref[inside]) / np.abs(ref[inside])) < 1e-5
 
 
 def run(sysm, steps, warm, weights=None, log=0):
@@ -63,7 +68,12 @@ def run(sysm, steps, warm, weights=None, log=0):
     return g
 
 
-def test_trained_warm_start_cuts_iterations_and_keeps_results():
+def test_learned_mode_on_short_drifts_keeps_results():
+    """The embryo disk's drifts are short (x1 = dt / r0^1.5 ~ 0.01, below the
+    network's gate of 0.03): the learned mode takes the series guess there and
+    needs one Newton iteration per solve, against 1.4 for the plain guess, with
+    the same results to 1e-12.  (The network itself is exercised on long
+    drifts below.)"""
     train_sys = systems.embryo_disk(n_embryos=510, seed=21)
     g = run(train_sys, 40, merc.WARM_PLAIN, log=200_000)
     assert g.mlp_log_count() > 10_000
@@ -82,5 +92,41 @@ def test_trained_warm_start_cuts_iterations_and_keeps_results():
     print(f"mean Newton iterations: plain {it_plain:.3f}, learned {it_learned:.3f}, max rel pos diff {rel.max():.2e}")
     assert rel.max() <= 1e-12
     assert np.array_equal(a.flags, b.flags)
-    assert it_learned < 0.8 * it_plain
+    assert it_learned <= 1.001 and it_plain >= 1.3
     assert sl.kepler_nonconverged == 0
+
+
+def test_learned_guess_cuts_iterations_on_hard_drifts():
+    """Drifts the plain and series guesses handle badly (e up to 0.99 near
+    perihelion, hyperbolic flybys, x1 = dt / r0^1.5 up to ~10): a network
+    trained on logged drifts of one such set cuts the Newton iterations on
+    another (different seed).  Measured on a GB300 (mean / executed per warp):
+    plain 3.06 / 4.74, series 2.36 / 4.40, learned 2.07 / 3.31; the plain and
+    series guesses leave a few solves at the iteration cap, the learned none.
+    One iteration is the floor of the a-posteriori stop, and a guess within
+    ~1e-4 of the root still needs two, which bounds the cut of the mean here."""
+    train = systems.hard_drifts(seed=31, n=3 * 65536)
+    g = run(train, 4, merc.WARM_PLAIN, log=2_000_000)
+    assert g.mlp_log_count() > 500_000
+    g.mlp_train(epochs=30, batch=8192, lr=3e-3, seed=5)
+    w = g.mlp_weights()
+    g.close()
+    test_sys = systems.hard_drifts(seed=32, n=65536)
+    res = {}
+    for name, warm in (("plain", merc.WARM_PLAIN), ("series", merc.WARM_SERIES), ("learned", merc.WARM_MLP)):
+        h = run(test_sys, 4, warm, weights=w if warm == merc.WARM_MLP else None)
+        st = h.stats()
+        res[name] = (st.kepler_iterations / st.kepler_solves, st.kepler_simt_iterations / st.kepler_solves,
+                     st.kepler_nonconverged, h.state().pos)
+        h.close()
+    print({k: v[:3] for k, v in res.items()})
+    # the same drifts to the Newton tolerance (a few solves of the plain guess
+    # stop at the iteration cap)
+    a, b = res["plain"][3].reshape(3, -1), res["learned"][3].reshape(3, -1)
+    ok = np.isfinite(a).all(0) & np.isfinite(b).all(0)
+    rel = np.abs(a[:, ok] - b[:, ok]).max(0) / np.linalg.norm(a[:, ok], axis=0)
+    assert np.quantile(rel, 0.99) <= 1e-12 and np.median(rel) <= 1e-14
+    assert res["learned"][2] == 0
+    assert res["learned"][0] <= res["plain"][0] / 1.3
+    assert res["learned"][1] <= res["plain"][1] / 1.25
+    assert res["learned"][1] <= res["series"][1] / 1.15
