@@ -543,12 +543,20 @@ def run_ours(args, world, rank, local, dist):
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "measured FP64 FMA loop on this GPU (merc_diag_fp64_peak)",
                      "kick_ms": kick_avg_ms, "kick_launches": kick_n, "pairs_per_launch": pairs_per_kick,
-                     "flops_per_pair": FLOPS_PER_PAIR},
+                     "flops_per_pair": FLOPS_PER_PAIR,
+                     # utilisation beside the algorithmic figure: the kernel
+                     # evaluates each unordered pair once in 22 FP64
+                     # instructions (both directions), against the measured
+                     # FP64 instruction rate (peak / 2: an FMA is 2 flops)
+                     "fp64_instructions_per_unordered_pair": 22,
+                     "issue_frac": 22 * (nm * (nm - 1) / 2) / (kick_avg_ms * 1e-3) / (peak * 1e12 / 2)},
         "roofline_encounter": {"bound": "fp64", "kernel": "k_encounter_tasks (encounter sub-step)",
                                "achieved": enc_achieved, "peak": peak, "unit": "TFLOP/s",
                                "frac": enc_achieved / peak, "encounter_ms": enc_avg_ms, "launches": enc_n,
                                "encounter_bodies_per_step": ce_per_step, "pairs_per_launch": enc_pairs,
-                               "flops_per_pair": FLOPS_PER_PAIR},
+                               "flops_per_pair": FLOPS_PER_PAIR,
+                               "fp64_instructions_per_pair": 18,
+                               "issue_frac": 18 * enc_pairs / (enc_avg_ms * 1e-3) / (peak * 1e12 / 2)},
         "cpu_baseline": cpu,
         "cpu_universal_drift": cpu_ref,
         "e2e": {"value": e2e_value, "unit": UNIT,
