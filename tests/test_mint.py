@@ -59,3 +59,25 @@ def test_mint_run_matches_oracle(tmp_path, oracle):
     # the 6-digit positions file has the reference layout
     txt = open(tmp_path / "pos.txt").read().splitlines()
     assert txt[0] == "#" and txt[1] == "$" and len(txt[2].split()) == 3
+
+
+@pytest.mark.gpu
+def test_mint_radius_key_turns_collisions_on(tmp_path):
+    """A per-body "radius" key in the config switches physical collisions on
+    (merc_set_radii): the accretion case of test_collisions.py, run through
+    mint, reports its one collision."""
+    from test_collisions import accretion_case
+
+    s, rad = accretion_case()
+    cfg = tmp_path / "c.json"
+    systems.to_json(s, str(cfg), dt=s.dt, batch_size=5, changeover_hill_factor=3.0)
+    import json
+
+    doc = json.load(open(cfg))
+    for b, r in zip(doc["bodies"], rad):
+        b["radius"] = float(r)
+    json.dump(doc, open(cfg, "w"))
+    out = subprocess.run([MINT, "-c", str(cfg), "-t", "2", "-i", "-o", str(tmp_path / "pos.txt")],
+                         capture_output=True, text=True, cwd=tmp_path)
+    assert out.returncode == 0, out.stderr
+    assert "Collisions: 1" in out.stdout
