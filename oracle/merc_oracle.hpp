@@ -376,13 +376,16 @@ template <class R> struct UDrift { PV<R> out; int iters; bool converged; R s; };
 
 // Universal-variable Kepler drift with mu = 1: solve
 //   r0 s + eta G2(s) + zeta G3(s) = dt,  G_k = s^k c_k(alpha s^2),
-// alpha = 2/r0 - v0^2, eta = x0.v0, zeta = 1 - alpha r0, by Newton from s0.
+// alpha = 2/r0 - v0^2, eta = x0.v0, zeta = 1 - alpha r0, by Newton from s0
+// (Laguerre-Conway steps with n = 5 after 8 Newton steps without convergence:
+// Newton can oscillate on drifts long against the pericentre passage).
 // Stopping rule: after the update s += ds, the Newton error estimate of the
 // new s is |f''/(2 f')| ds^2; stop when it is <= tol |s| (and |ds| <= 1e-3 |s|,
 // so the estimate is only trusted in the quadratic regime).  The f and g
 // functions are then evaluated at the final s.
 template <class R>
 UDrift<R> universal_drift(const V3<R>& x0, const V3<R>& v0, R dt, R s0, R tol, int max_iter) {
+  constexpr int kNewtonIters = 8;
   R r0 = std::sqrt(mag2(x0));
   R ir0 = R(1) / r0;
   R eta = std::fma(x0.x, v0.x, std::fma(x0.y, v0.y, x0.z * v0.z));
@@ -400,7 +403,13 @@ UDrift<R> universal_drift(const V3<R>& x0, const V3<R>& v0, R dt, R s0, R tol, i
     R f = std::fma(r0, s, std::fma(eta, G2, std::fma(zeta, G3, -dt)));
     R fp = std::fma(eta, G1, std::fma(zeta, G2, r0));
     R fpp = std::fma(eta, c0, zeta * G1);
-    R ds = -f / fp;
+    R ds;
+    if (it < kNewtonIters) {
+      ds = -f / fp;
+    } else {  // Laguerre-Conway step (n = 5) after kNewtonIters Newton steps
+      const R h = std::fabs(std::fma(R(16) * fp, fp, -R(20) * f * fpp));
+      ds = -R(5) * f / (fp + std::sqrt(h));
+    }
     s = s + ds;
     it++;
     R as = std::fabs(s);

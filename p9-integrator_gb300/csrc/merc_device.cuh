@@ -569,10 +569,12 @@ __device__ __forceinline__ double f64_of_f32(float x) {
 // s^3/6 + O(s^4) inverted to third order, s = s0 (1 - (eta / 2 r0) s0 + ((3
 // eta^2 - r0 zeta) / 6 r0^2) s0^2) with s0 = dt / r0, kept when within a factor
 // 2 of s0; kGuessRel: s0 (1 + rel), kept within a factor 16): Newton on
-// r0 s + eta G2 + zeta G3 = dt; after each update the
+// r0 s + eta G2 + zeta G3 = dt (Laguerre-Conway steps, n = 5, after
+// kNewtonIters Newton steps without convergence); after each update the
 // Newton error estimate |f''/(2 f')| ds^2 of the new s is compared with tol |s|
 // (trusted once |ds| <= 1e-3 |s|), in FP32 on truncated copies (the decision
 // needs no more than a factor of 2); f and g at the final s.
+constexpr int kNewtonIters = 8;  // Newton steps before the Laguerre-Conway fallback
 __device__ __forceinline__ UD universal_drift(const FU& U, const d3& x0, const d3& v0, double dt, double s0,
                                               double tol, int max_iter, float rel = 0.0f) {
   const double rr = fma(x0.x, x0.x, fma(x0.y, x0.y, fmul(U, x0.z, x0.z)));
@@ -610,7 +612,15 @@ __device__ __forceinline__ UD universal_drift(const FU& U, const d3& x0, const d
     double f = fma(r0, s, fma(eta, G2, fma(zeta, G3, -dt)));
     double fp = fma(eta, G1, fma(zeta, G2, r0));
     double fpp = fma(eta, c0, fmul(U, zeta, G1));
-    double ds = fmul(U, -f, rcp_fast(fp));
+    double ds;
+    if (it < kNewtonIters) {
+      ds = fmul(U, -f, rcp_fast(fp));
+    } else {
+      // Laguerre-Conway step (n = 5): converges where Newton oscillates on
+      // long drifts (x1 = dt / r0^1.5 >> 1 near perihelion)
+      const double h = fabs(fma(fmul(U, 16.0, fp), fp, -fmul(U, fmul(U, 20.0, f), fpp)));
+      ds = fmul(U, fmul(U, -5.0, f), rcp_fast(fadd(U, fp, sqrt(h))));
+    }
     s = fadd(U, s, ds);
     it++;
     const float dsf = abs_f32_trunc(ds), sf = abs_f32_trunc(s);

@@ -101,10 +101,9 @@ def test_learned_guess_cuts_iterations_on_hard_drifts():
     perihelion, hyperbolic flybys, x1 = dt / r0^1.5 up to ~10): a network
     trained on logged drifts of one such set cuts the Newton iterations on
     another (different seed).  Measured on a GB300 (mean / executed per warp):
-    plain 3.06 / 4.74, series 2.36 / 4.40, learned 2.07 / 3.31; the plain and
-    series guesses leave a few solves at the iteration cap, the learned none.
-    One iteration is the floor of the a-posteriori stop, and a guess within
-    ~1e-4 of the root still needs two, which bounds the cut of the mean here."""
+    plain 3.06 / 4.66, series 2.35 / 4.30, learned 2.06 / 3.31.  One
+    iteration is the floor of the a-posteriori stop, and a guess within ~1e-4
+    of the root still needs two, which bounds the cut of the mean here."""
     train = systems.hard_drifts(seed=31, n=3 * 65536)
     g = run(train, 4, merc.WARM_PLAIN, log=2_000_000)
     assert g.mlp_log_count() > 500_000
@@ -120,8 +119,7 @@ def test_learned_guess_cuts_iterations_on_hard_drifts():
                      st.kepler_nonconverged, h.state().pos)
         h.close()
     print({k: v[:3] for k, v in res.items()})
-    # the same drifts to the Newton tolerance (a few solves of the plain guess
-    # stop at the iteration cap)
+    # the same drifts to the Newton tolerance
     a, b = res["plain"][3].reshape(3, -1), res["learned"][3].reshape(3, -1)
     ok = np.isfinite(a).all(0) & np.isfinite(b).all(0)
     rel = np.abs(a[:, ok] - b[:, ok]).max(0) / np.linalg.norm(a[:, ok], axis=0)
