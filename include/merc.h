@@ -222,7 +222,9 @@ typedef struct merc_collision {
 /* Collisions resolved since merc_set_radii, in the order they were resolved.
  * Copies min(total, max) records to out (may be NULL with max 0) and the
  * total count to *count; records beyond the context's log of 65536 are
- * counted but not kept. */
+ * counted but not kept.  Returns MERC_ERR_STATE (after copying) if some step
+ * found more than 4096 colliding pairs, more than one step can resolve: pairs
+ * beyond that were not merged. */
 int merc_get_collisions(merc_ctx* ctx, merc_collision* out, int64_t max, int64_t* count);
 
 /* Current masses (n_total doubles): the loaded masses, changed by collisions. */

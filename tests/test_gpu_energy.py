@@ -75,3 +75,35 @@ def test_angular_momentum_diagnostic():
     L1 = g.angular_momentum()[0]
     assert np.linalg.norm(L1 - L0) <= 1e-12 * np.linalg.norm(L0)
     g.close()
+
+
+EMBRYO_GOLD = os.path.join(os.path.dirname(__file__), "golden", "energy_embryo.json")
+
+
+@pytest.mark.skipif(not os.path.exists(EMBRYO_GOLD), reason="energy_embryo.json not generated")
+def test_embryo_disk_energy_error_within_twice_the_reference():
+    """1e4 steps of the 2002-body embryo disk (close encounters every step):
+    the GPU universal drift's relative energy error is within 2x of the
+    reference algorithm's (the element drift, binary64 oracle, from
+    tests/golden/energy_embryo.json), and after the first 300 steps it sits at
+    the long-double oracle's value of its own algorithm (the host's
+    long-double arithmetic is too slow for 1e4 steps of this disk)."""
+    gold = json.load(open(EMBRYO_GOLD))
+    s = systems.embryo_disk()
+    g = merc.Integrator(merc.default_params(dt=s.dt, hill_factor=s.hill_factor, drift=merc.DRIFT_UNIVERSAL))
+    g.load_systems(s)
+    e0 = g.energy()[0]
+    assert abs(e0 - gold["universal"]["energy0"]) <= 1e-14 * abs(e0)
+    g.step(gold["short_steps"])
+    e_short = g.energy()[0]
+    g.step(gold["steps"] - gold["short_steps"])
+    e1 = g.energy()[0]
+    g.close()
+    err_short = abs(e_short - e0) / abs(e0)
+    err = abs(e1 - e0) / abs(e0)
+    ld_short = gold["universal"]["long_double"]["rel_error_short"]
+    ref = gold["elements"]["binary64"]["rel_error"]
+    print(f"energy error: GPU {err_short:.3e} after {gold['short_steps']} steps (long double {ld_short:.3e}), "
+          f"{err:.3e} after {gold['steps']} (reference algorithm {ref:.3e})")
+    assert abs(err_short - ld_short) <= 0.1 * ld_short
+    assert err <= 2.0 * ref
