@@ -226,3 +226,25 @@ def test_stumpff_short_series_for_small_arguments(oracle):
         term3 = -term3 * zl / ((2 * k + 4) * (2 * k + 5))
     assert np.all(np.abs(c[2] - c2.astype(np.float64)) <= 2 * np.spacing(0.5))
     assert np.all(np.abs(c[3] - c3.astype(np.float64)) <= 2 * np.spacing(1.0 / 6.0))
+
+
+def test_laguerre_fallback_on_long_drifts(oracle):
+    """Drifts long against the pericentre passage (bound orbits of the hard
+    drift set with dt = 0.2 yr, x1 = dt / r0^1.5 up to ~14): where 8 Newton
+    steps from the plain guess do not converge the solve continues with
+    Laguerre-Conway steps, and the result agrees with Kepler's equation in
+    40-digit mpmath."""
+    s = systems.hard_drifts(n=3 * 2048, seed=8)
+    x, v = s.extra["pos"].reshape(3, -1), s.extra["vel"].reshape(3, -1)
+    dt = 0.2
+    _, _, its = oracle.universal(x.reshape(-1), v.reshape(-1), dt, max_iter=60)
+    alpha = 2 / np.linalg.norm(x, axis=0) - (v * v).sum(0)
+    long_ones = np.where((its > 8) & (alpha > 0.05))[0]
+    assert len(long_ones) >= 10
+    for j in long_ones[:12]:
+        pos, vel = x[:, j].copy(), v[:, j].copy()
+        rp, rv = kepler_reference(pos, vel, dt)
+        po, vo, it = oracle.universal(pos, vel, dt, max_iter=60)
+        assert it[0] < 60
+        assert np.max(np.abs(po - rp)) <= 1e-11 * np.linalg.norm(rp), (j, it)
+        assert np.max(np.abs(vo - rv)) <= 1e-11 * np.linalg.norm(rv), (j, it)
