@@ -239,7 +239,7 @@ def sweep_section(merc, args, local, dist, world, rank):
     pairs = sysm.pairs_per_step()
     g.close()
     # one by one: a sample of the systems, each loaded and stepped alone,
-    # with the plain guess dt / r0 (the comparator the benchmark spec names)
+    # with the plain guess dt / r0
     sample = sysm.subset(np.linspace(0, sysm.n_systems - 1, 48).astype(int))
     g1 = merc.Integrator(merc.default_params(warm_start=merc.WARM_PLAIN, **kw), device=local)
     t_ms, bodies = 0.0, 0
