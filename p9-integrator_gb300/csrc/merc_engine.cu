@@ -70,6 +70,8 @@ struct merc_ctx {
   SymTask* d_sym = nullptr;   // massive block pairs of the big systems
   long long* d_sym_base = nullptr;
   int* d_big_ids = nullptr;
+  int2* d_exact_groups = nullptr;  // element path: (first body, count) of each grouped exact kick warp
+  int n_exact_groups = 0;
   int n_work = 0, n_work_tp = 0, n_sym = 0, n_big = 0, max_big_nm = 0;
   bool has_small = false, has_big = false, any_multi = false;
   std::vector<void*> allocs;
@@ -368,6 +370,27 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
     CK(cudaMemcpyAsync(ctx->d_work, work.data(), sizeof(Work) * ctx->n_work, cudaMemcpyHostToDevice, s));
   if (ctx->n_big)
     CK(cudaMemcpyAsync(ctx->d_big_ids, big_ids.data(), sizeof(int) * ctx->n_big, cudaMemcpyHostToDevice, s));
+  {
+    // the element path's grouped exact kick: G bodies of one big system per
+    // warp, G chosen so that there are about MERC_EXACT_COVER warps per SM
+    int64_t nbig = 0;
+    for (int sb : big_ids) nbig += off[sb + 1] - off[sb];
+#ifndef MERC_EXACT_COVER
+#define MERC_EXACT_COVER 7  // measured, 2002-body disk: G = 2 1.752 ms per step, 3: 1.767, 4: 1.855, 1: 1.972, 7: 2.374
+#endif
+    const int64_t cover = (int64_t)MERC_EXACT_COVER * dev_sms;
+    const int G = (int)std::max<int64_t>(1, std::min<int64_t>(kExactGroupMax, (nbig + cover - 1) / cover));
+    std::vector<int2> groups;
+    for (int sb : big_ids)
+      for (int64_t j0 = off[sb]; j0 < off[sb + 1]; j0 += G)
+        groups.push_back(make_int2((int)j0, (int)std::min<int64_t>(G, off[sb + 1] - j0)));
+    ctx->n_exact_groups = (int)groups.size();
+    if ((st = dalloc(ctx, &ctx->d_exact_groups, std::max<size_t>(1, groups.size())))) return st;
+    if (!groups.empty())
+      CK(cudaMemcpyAsync(ctx->d_exact_groups, groups.data(), sizeof(int2) * groups.size(), cudaMemcpyHostToDevice,
+                         s));
+    CK(cudaStreamSynchronize(s));  // `groups` is a temporary
+  }
   if (ctx->n_work_tp)
     CK(cudaMemcpyAsync(ctx->d_work_tp, work_tp.data(), sizeof(Work) * ctx->n_work_tp, cudaMemcpyHostToDevice, s));
   if (ctx->n_sym) CK(cudaMemcpyAsync(ctx->d_sym, sym.data(), sizeof(SymTask) * ctx->n_sym, cudaMemcpyHostToDevice, s));
@@ -458,8 +481,9 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       k_kick<<<nb, kThreads, 0, s>>>(D, rc_in, rc_out, hdt, p.softening2, p.compat_block, p.hill_factor, ej2, last,
                                      bx);
       if (bx)
-        k_kick_big_exact<<<nbx, 32 * kExactWarps, 0, s>>>(D, rc_in, rc_out, hdt, p.softening2, p.compat_block,
-                                                          p.hill_factor, ej2, last);
+        k_kick_big_exact_grouped<<<(unsigned)std::max(1, ctx->n_exact_groups), 32, 0, s>>>(
+            D, ctx->d_exact_groups, ctx->n_exact_groups, rc_in, rc_out, hdt, p.softening2, p.compat_block,
+            p.hill_factor, ej2, last);
     };
     if ((st = kick_ev(0))) return st;
     kick_exact_all(rcA, nullptr, 0);
