@@ -330,7 +330,17 @@ __global__ void __launch_bounds__(32 * kExactWarps) k_ce_big_exact(Dev D, const 
     if (!D.big[s]) continue;
     const int b0 = D.off[s], nm = D.nm[s];
     SrcView S = src_view(D, rc_in, b0);
-    const bool ce = warp_close_encounter(load3(D.x, n, j), self_index(j - b0, compat_block), S, nm);
+    // close_encounter_p by the warp, behind the FP32 prefilter: a pair that
+    // ce_maybe clears is certainly outside r_crit (its proven bound) and
+    // needs no FP64 work; every other pair takes the reference's test, so the
+    // flag is warp_close_encounter's
+    const d3 pos = load3(D.x, n, j);
+    const F4 pf = load_f4(D, j);
+    const int self = self_index(j - b0, compat_block);
+    bool ce = false;
+    for (int i = lane; i < nm; i += 32)
+      if (ce_maybe(pf, load_f4(D, b0 + i), f32_trunc(S.rc[4 * (size_t)i]))) ce = ce || ce_pair(pos, self, S, i);
+    ce = __any_sync(0xffffffffu, ce);
     if (lane == 0) D.ce[j] = ce;
   }
 }
