@@ -70,7 +70,7 @@ struct merc_ctx {
   SymTask* d_sym = nullptr;   // massive block pairs of the big systems
   long long* d_sym_base = nullptr;
   int* d_big_ids = nullptr;
-  int2* d_exact_groups = nullptr;  // element path: (first body, count) of each grouped exact kick warp
+  int2* d_exact_groups = nullptr;  // element path: (first body, count) of each block of the exact kick
   int n_exact_groups = 0;
   int n_work = 0, n_work_tp = 0, n_sym = 0, n_big = 0, max_big_nm = 0;
   bool has_small = false, has_big = false, any_multi = false;
@@ -371,15 +371,15 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
   if (ctx->n_big)
     CK(cudaMemcpyAsync(ctx->d_big_ids, big_ids.data(), sizeof(int) * ctx->n_big, cudaMemcpyHostToDevice, s));
   {
-    // the element path's grouped exact kick: G bodies of one big system per
-    // warp, G chosen so that there are about MERC_EXACT_COVER warps per SM
+    // the element path's pipelined exact kick: G bodies of one big system per
+    // block, G chosen so that there are about two blocks per SM
     int64_t nbig = 0;
     for (int sb : big_ids) nbig += off[sb + 1] - off[sb];
-#ifndef MERC_EXACT_COVER
-#define MERC_EXACT_COVER 7  // measured, 2002-body disk: G = 2 1.752 ms per step, 3: 1.767, 4: 1.855, 1: 1.972, 7: 2.374
-#endif
-    const int64_t cover = (int64_t)MERC_EXACT_COVER * dev_sms;
-    const int G = (int)std::max<int64_t>(1, std::min<int64_t>(kExactGroupMax, (nbig + cover - 1) / cover));
+    // measured on the 2002-body disk (ms per step): G = 7 (286 blocks) 1.561,
+    // 5 1.571, 9 1.685, 4 1.638; one body per one-warp block without the
+    // pipeline 1.972, two 1.638
+    const int64_t cover = 2 * (int64_t)dev_sms;
+    const int G = (int)std::max<int64_t>(1, std::min<int64_t>(kPipeGroupMax, (nbig + cover - 1) / cover));
     std::vector<int2> groups;
     for (int sb : big_ids)
       for (int64_t j0 = off[sb]; j0 < off[sb + 1]; j0 += G)
@@ -481,7 +481,7 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       k_kick<<<nb, kThreads, 0, s>>>(D, rc_in, rc_out, hdt, p.softening2, p.compat_block, p.hill_factor, ej2, last,
                                      bx);
       if (bx)
-        k_kick_big_exact_grouped<<<(unsigned)std::max(1, ctx->n_exact_groups), 32, 0, s>>>(
+        k_kick_big_exact_pipe<<<(unsigned)std::max(1, ctx->n_exact_groups), 32 * (1 + kPipeTermWarps), 0, s>>>(
             D, ctx->d_exact_groups, ctx->n_exact_groups, rc_in, rc_out, hdt, p.softening2, p.compat_block,
             p.hill_factor, ej2, last);
     };

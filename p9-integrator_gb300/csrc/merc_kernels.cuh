@@ -238,7 +238,7 @@ __global__ void k_rc(Dev D, double* rc_out, double hill) {
 // exact path (element drift): reference operation order
 // ---------------------------------------------------------------------------
 // Half kick of every body (sim.cuh:683-685, 739-741); skip_big leaves the
-// bodies of big systems to k_kick_big_exact_grouped.
+// bodies of big systems to k_kick_big_exact_pipe.
 __global__ void k_kick(Dev D, const double* __restrict__ rc_in, double* __restrict__ rc_out, double hdt,
                        double soft2, int compat_block, double hill, double eject_r2, int last, int skip_big) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -257,64 +257,65 @@ __global__ void k_kick(Dev D, const double* __restrict__ rc_in, double* __restri
 // arithmetic and order, with the source terms computed 32 at a time.
 constexpr int kExactWarps = 4;  // warps per block
 
-// The kick of the big systems' bodies, G bodies of one system per warp (G <=
-// kExactGroupMax, chosen so that there are a few warps per SM).  The reference's order
-// ends every source term in a sequential fma chain per body and component;
-// run by lanes 0-2 of a warp for one body, each chain step is a warp
-// instruction on the FP64 pipe for 3 busy lanes, as costly as a source term
-// for all 32 (measured: ~72 FP64 instructions per directed pair, of which ~32
-// are the chain).  Here lane 3b + c runs body b's component-c chain, so one
-// chain step serves G bodies: the terms of 32 sources for the G bodies are
-// computed on the 32 lanes (the same exact_term arithmetic), staged in shared
-// memory, then chained in source order.  Same bits as warp_kick_exact.
-constexpr int kExactGroupMax = 10;
-__global__ void __launch_bounds__(32) k_kick_big_exact_grouped(Dev D, const int2* __restrict__ groups, int ngroups,
-                                                                const double* __restrict__ rc_in,
-                                                                double* __restrict__ rc_out, double hdt, double soft2,
-                                                                int compat_block, double hill, double eject_r2,
-                                                                int last) {
-  __shared__ double stage[kExactGroupMax][4][32];
-  const int lane = (int)(threadIdx.x & 31);
+// The kick of the big systems' bodies as a pipeline: one block per group of
+// G <= kPipeGroupMax bodies of one system, warp 0 runs the 3G fma chains
+// (lane 3b + c: body b, component c) while kPipeTermWarps warps compute the
+// next 32 sources' terms for the G bodies (exact_term), double-buffered in
+// shared memory.  The reference's order ends every source term in a
+// sequential fma chain per body and component; a chain step is a warp
+// instruction on the FP64 pipe however few lanes run it (one body per warp,
+// lanes 0-2: ~32 of ~72 FP64 instructions per directed pair), so one step
+// here serves G bodies, and the term warps do not wait for the chain's
+// ~90-cycle dependent steps.  Same bits as warp_kick_exact.
+constexpr int kPipeTermWarps = 3;
+constexpr int kPipeGroupMax = 9;
+__global__ void __launch_bounds__(32 * (1 + kPipeTermWarps))
+    k_kick_big_exact_pipe(Dev D, const int2* __restrict__ groups, int ngroups, const double* __restrict__ rc_in,
+                          double* __restrict__ rc_out, double hdt, double soft2, int compat_block, double hill,
+                          double eject_r2, int last) {
+  __shared__ double stage[2][kPipeGroupMax][4][32];
+  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
   for (int g = blockIdx.x; g < ngroups; g += gridDim.x) {
     const int j0 = groups[g].x, cnt = groups[g].y;
     const int n = D.n, s = D.sys[j0], b0 = D.off[s], nm = D.nm[s];
     SrcView S = src_view(D, rc_in, b0);
-    d3 pos[kExactGroupMax];
-    int self[kExactGroupMax];
-#pragma unroll
-    for (int b = 0; b < kExactGroupMax; b++) {
-      pos[b] = b < cnt ? load3(D.x, n, j0 + b) : d3{0.0, 0.0, 0.0};
-      self[b] = self_index(j0 + b - b0, compat_block);
-    }
-    const int cb = lane / 3, cc = lane - 3 * cb;  // the chain this lane runs (lane < 3 cnt)
+    const int nchunks = (nm + 31) / 32;
     double acc = 0.0;
-    for (int base = 0; base < nm; base += 32) {
-      const int i = base + lane;
-#pragma unroll
-      for (int b = 0; b < kExactGroupMax; b++) {
-        if (b < cnt) {
+    for (int c = 0; c <= nchunks; c++) {
+      if (warp > 0 && c < nchunks) {
+        const int i = 32 * c + lane;
+        for (int b = warp - 1; b < cnt; b += kPipeTermWarps) {
+          const d3 pos = load3(D.x, n, j0 + b);
           d3 d = {0.0, 0.0, 0.0};
-          const double wa = i < nm ? exact_term<false>(pos[b], self[b], S, i, soft2, d) : 0.0;
-          stage[b][0][lane] = wa;
-          stage[b][1][lane] = d.x;
-          stage[b][2][lane] = d.y;
-          stage[b][3][lane] = d.z;
+          const double wa = i < nm ? exact_term<false>(pos, self_index(j0 + b - b0, compat_block), S, i, soft2, d)
+                                   : 0.0;
+          double* st = stage[c & 1][b][0];
+          st[lane] = wa;
+          st[32 + lane] = d.x;
+          st[64 + lane] = d.y;
+          st[96 + lane] = d.z;
         }
       }
-      __syncwarp();
-      if (lane < 3 * cnt) acc = chain_fma<32>(stage[cb][0], stage[cb][1 + cc], min(32, nm - base), acc);
-      __syncwarp();
+      if (warp == 0 && c >= 1 && lane < 3 * cnt) {
+        const int cb = lane / 3, cc = lane - 3 * cb;
+        acc = chain_fma<32>(stage[(c - 1) & 1][cb][0], stage[(c - 1) & 1][cb][1 + cc], min(32, nm - 32 * (c - 1)),
+                            acc);
+      }
+      __syncthreads();
     }
-    for (int b = 0; b < cnt; b++) {
-      const double ax = __shfl_sync(0xffffffffu, acc, 3 * b), ay = __shfl_sync(0xffffffffu, acc, 3 * b + 1),
-                   az = __shfl_sync(0xffffffffu, acc, 3 * b + 2);
-      if (lane == b) {
-        const int j = j0 + b;
-        d3 vel = load3(D.v, n, j);
-        vel.x = fma(ax, hdt, vel.x);
-        vel.y = fma(ay, hdt, vel.y);
-        vel.z = fma(az, hdt, vel.z);
-        kick_epilogue(D, j, j - b0, nm, pos[b], vel, rc_out, hill, eject_r2, last);
+    if (warp == 0) {
+      for (int b = 0; b < cnt; b++) {
+        const double ax = __shfl_sync(0xffffffffu, acc, 3 * b), ay = __shfl_sync(0xffffffffu, acc, 3 * b + 1),
+                     az = __shfl_sync(0xffffffffu, acc, 3 * b + 2);
+        if (lane == b) {
+          const int j = j0 + b;
+          const d3 pos = load3(D.x, n, j);
+          d3 vel = load3(D.v, n, j);
+          vel.x = fma(ax, hdt, vel.x);
+          vel.y = fma(ay, hdt, vel.y);
+          vel.z = fma(az, hdt, vel.z);
+          kick_epilogue(D, j, j - b0, nm, pos, vel, rc_out, hill, eject_r2, last);
+        }
       }
     }
   }
