@@ -502,8 +502,8 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     k_encounter_elements<<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2,
                                                          bx);
     if (bx)
-      k_encounter_big_exact<<<ctx->sms, kExactRowThreads * p.bs_rows, 0, s>>>(D, rcB, p.dt, p.compat_block,
-                                                                              p.bs_rows, p.softening2);
+      k_encounter_big_pipe<<<ctx->sms, 32 + kExactRowThreads * p.bs_rows, 0, s>>>(D, rcB, p.dt, p.compat_block,
+                                                                                 p.bs_rows, p.softening2);
     if (ctx->collide_on) {
       k_collide_find<<<ctx->sms * 4, 256, 0, s>>>(D, ctx->col);
       k_collide_resolve<<<1, 32, 0, s>>>(D, ctx->col, p.hill_factor);

@@ -688,7 +688,7 @@ __global__ void k_drift_elements(Dev D, const double* __restrict__ rc_in, double
 // Encounter sub-step (Richardson extrapolation of modified-midpoint steps
 // against sources frozen at the start of the drift, sim.cuh:701-702) in the
 // reference order; one thread per listed body, grid-stride.  skip_big leaves
-// the bodies of big systems to k_encounter_big_exact.
+// the bodies of big systems to k_encounter_big_pipe.
 __device__ __forceinline__ void encounter_elements_store(const Dev& D, int j, PV bs) {
   const int n = D.n;
   d3 kp = load3(D.xo, n, j), kv = load3(D.vo, n, j);
@@ -710,29 +710,104 @@ __global__ void k_encounter_elements(Dev D, const double* __restrict__ rc_in, do
     encounter_elements_store(D, j, richardson(c, vt, dt, rows));
   }
 }
-// The same for the listed bodies of big systems, one block per body and one
-// group of kExactRowThreads threads per Richardson row, the rows side by side
-// (each group runs its row's modified midpoint; group_kick_exact sums the
-// sources with the group's named barrier); thread 0 combines the rows as
-// richardson() does.  Launched with kExactRowThreads x rows threads.
+// The big systems' listed bodies: one group of kExactRowThreads threads per
+// Richardson row computes the terms of its row's evaluations.
 constexpr int kExactRowThreads = 128;
-__global__ void __launch_bounds__(4 * kExactRowThreads)
-    k_encounter_big_exact(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, int rows,
-                          double soft2) {
-  __shared__ double stage[4][8 * kExactRowThreads + 3];
+
+// The encounter sub-step of the big systems' listed bodies, the rows side by
+// side in lock step with one warp for all their fma chains: one block per
+// encounter body, warp 0 runs the 3 x rows chains (lane
+// 3r + c: row r, component c) while the rows' 128-thread groups compute the
+// next 128 sources' terms (exact_term with the encounter weighting),
+// double-buffered in shared memory.  Round k evaluates the velocity update
+// of every row whose modified midpoint has more than k sub-steps (row r has
+// 2^r), at the row's position of that sub-step; between rounds each group
+// advances its row's state exactly as mod_midpoint does.  Each evaluation is
+// bound by its chain (one dependent fma per source); a chain step costs the
+// FP64 pipe one warp instruction for all rows, and the term groups do not
+// wait for it.  Same bits as richardson() with ExactVelTotal (thread 0
+// combines the rows as richardson() does).  Launched with
+// 32 + kExactRowThreads x rows threads.
+__global__ void __launch_bounds__(32 + 4 * kExactRowThreads)
+    k_encounter_big_pipe(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, int rows,
+                         double soft2) {
+  constexpr int NT = kExactRowThreads;
+  __shared__ double stage[2][4][4][NT];
+  __shared__ double accs[4][3];
   __shared__ PV res[4];
-  const int g = (int)threadIdx.x / kExactRowThreads, tid = (int)threadIdx.x % kExactRowThreads;
+  const bool chainw = threadIdx.x < 32;
+  const int lane = (int)(threadIdx.x & 31);
+  const int g = chainw ? 0 : ((int)threadIdx.x - 32) / NT, tid = chainw ? 0 : ((int)threadIdx.x - 32) % NT;
   const int count = D.ce_count[0];
   for (int k = blockIdx.x; k < count; k += gridDim.x) {
     const int j = D.ce_list[k];
     const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
     if (!D.big[s]) continue;
     SrcView S = src_view(D, rc_in, b0);
-    ExactVelTotal<kExactRowThreads> vt{&S, nm, self_index(j - b0, compat_block), soft2, stage[g], tid, 1 + g};
-    PV c = {load3(D.x, n, j), load3(D.v, n, j)};
-    const PV r = mod_midpoint(c, vt, dt, 1 << g);
-    if (tid == 0) res[g] = r;
-    __syncthreads();
+    const int self = self_index(j - b0, compat_block);
+    const PV c0 = {load3(D.x, n, j), load3(D.v, n, j)};
+    // row g's modified midpoint (mod_midpoint) state, kept by its group
+    const int N = 1 << g;
+    const double h = dt * inv_pow2(N), h2 = 2.0 * h;
+    d3 z0 = c0.pos, z1 = c0.pos;
+    z1.x = fma(c0.vel.x, h, z1.x);
+    z1.y = fma(c0.vel.y, h, z1.y);
+    z1.z = fma(c0.vel.z, h, z1.z);
+    PV c = {z1, c0.vel};
+    const int nchunks = (nm + NT - 1) / NT;
+    const int rounds = 1 << (rows - 1);
+    for (int round = 0; round < rounds; round++) {
+      const bool active = !chainw && round < N;
+      if (active && round > 0) {
+        const d3 t = {fma(h2, c.vel.x, z0.x), fma(h2, c.vel.y, z0.y), fma(h2, c.vel.z, z0.z)};
+        z0 = z1;
+        z1 = t;
+        c.pos = z1;
+      }
+      // rows still running this round: r < rows with 2^r > round
+      int nact = 0;
+      while (nact < rows && (1 << nact) <= round) nact++;
+      const int r_lo = nact, nrun = rows - r_lo;
+      double acc = 0.0;  // chain warp, lane 3 q + cc: row r_lo + q
+      for (int ch = 0; ch <= nchunks; ch++) {
+        if (active && ch < nchunks) {
+          const int i = ch * NT + tid;
+          d3 d = {0.0, 0.0, 0.0};
+          const double wa = i < nm ? exact_term<true>(c.pos, self, S, i, soft2, d) : 0.0;
+          double* st = stage[ch & 1][g][0];
+          st[tid] = wa;
+          st[NT + tid] = d.x;
+          st[2 * NT + tid] = d.y;
+          st[3 * NT + tid] = d.z;
+        }
+        if (chainw && ch >= 1 && lane < 3 * nrun) {
+          const int q = lane / 3, cc = lane - 3 * q;
+          const double* st = stage[(ch - 1) & 1][r_lo + q][0];
+          acc = chain_fma<NT>(st, st + NT * (cc + 1), min(NT, nm - (ch - 1) * NT), acc);
+        }
+        __syncthreads();
+      }
+      if (chainw && lane < 3 * nrun) accs[r_lo + lane / 3][lane % 3] = acc;
+      __syncthreads();
+      if (active) {
+        // ExactVelTotal: the kick's sum, then the Sun
+        d3 nv = {fma(accs[g][0], h, c.vel.x), fma(accs[g][1], h, c.vel.y), fma(accs[g][2], h, c.vel.z)};
+        double r_sq = mag2(c.pos);
+        const double r = stable_sqrt(r_sq);
+        r_sq += soft2;
+        const double denom = r_sq * r;
+        const d3 rv = {c.pos.x / denom, c.pos.y / denom, c.pos.z / denom};
+        nv.x = fma(-rv.x, h, nv.x);
+        nv.y = fma(-rv.y, h, nv.y);
+        nv.z = fma(-rv.z, h, nv.z);
+        c.vel = nv;
+        if (round == N - 1 && tid == 0)
+          res[g] = PV{{0.5 * (z1.x + fma(c.vel.x, h, z0.x)), 0.5 * (z1.y + fma(c.vel.y, h, z0.y)),
+                       0.5 * (z1.z + fma(c.vel.z, h, z0.z))},
+                      c.vel};
+      }
+      __syncthreads();  // accs is rewritten next round
+    }
     if (threadIdx.x == 0) encounter_elements_store(D, j, richardson_of_rows(res, rows));
     __syncthreads();  // res is rewritten for the next body
   }
