@@ -2156,7 +2156,7 @@ int merc_diag_encounter_wait(merc_ctx* ctx, int32_t* gave_up) {
     }
   // one listed body; tasks start at the second unit (the first unit, row 2's
   // evaluation 0 of every listed body, is skipped)
-  const int one = 1, head[2] = {enc_parts(kEncOrder & 3), 0};
+  const int one = 1, head[2] = {enc_unit_parts(0), 0};
   CK(cudaMemcpy(D.ce_list_big, &body, sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(D.ce_count + 1, &one, sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(D.enc_head, head, sizeof head, cudaMemcpyHostToDevice));

@@ -72,7 +72,7 @@ struct Dev {
   unsigned long long* counters = nullptr;  // kNumCounters: CE body-steps, Kepler iterations, solves,
                                            // non-converged, iterations executed per warp (SIMT)
   // encounter task kernel, per entry of the big-system encounter list:
-  double* enc_q = nullptr;    // kEncQ: part sums of the 7 evaluations (enc_parts(row) x 3 each)
+  double* enc_q = nullptr;    // kEncQ: part sums of the 7 evaluations (enc_parts(row, e) x 3 each)
   double* enc_st = nullptr;   // 27: per row z0, z1, vel after its last published evaluation
   double* enc_res = nullptr;  // 18: per row the sub-step result (position, velocity)
   int* enc_cnt = nullptr;     // 11: parts done per evaluation (7), evaluations published per row (3),
@@ -1605,15 +1605,39 @@ __device__ __forceinline__ bool bs_fast_term(const Dev& D, const double* __restr
   return !far;
 }
 
+// Totals of (x, y, z) over the 32 lanes of a warp by a reduce-scatter: at the
+// first level lanes 0-15 keep x and y and lanes 16-31 keep z (and an empty
+// fourth sum), at the second each group of eight lanes keeps one component,
+// and three more levels finish it; six FP64 additions in all, against fifteen
+// for three butterflies (the FP64 pipe is the bound of the sub-step).  A fixed
+// tree: every lane ends with the same totals, whatever the schedule.
+__device__ __forceinline__ d3 warp_sum3(const FU& U, const d3& a) {
+  const unsigned full = 0xffffffffu;
+  const int lane = (int)(threadIdx.x & 31);
+  const bool up = (lane & 16) != 0, b3 = (lane & 8) != 0;
+  double k0 = up ? a.z : a.x, k1 = up ? 0.0 : a.y;
+  const double s0 = up ? a.x : a.z, s1 = up ? a.y : 0.0;
+  k0 = fadd(U, k0, __shfl_xor_sync(full, s0, 16));
+  k1 = fadd(U, k1, __shfl_xor_sync(full, s1, 16));
+  double k = b3 ? k1 : k0;
+  k = fadd(U, k, __shfl_xor_sync(full, b3 ? k0 : k1, 8));
+  k = fadd(U, k, __shfl_xor_sync(full, k, 4));
+  k = fadd(U, k, __shfl_xor_sync(full, k, 2));
+  k = fadd(U, k, __shfl_xor_sync(full, k, 1));
+  return {__shfl_sync(full, k, 0), __shfl_sync(full, k, 8), __shfl_sync(full, k, 16)};
+}
+
 // Sum over sources c0..c1 - 1 of the encounter body's pull, by one warp:
 // sources c0 + lane + 32 k, even k into a0, odd k into a1 (two independent
 // FP64 chains in flight), pairs that need the reference formula marked and
-// added to ae after each chunk of 64 k; then a fixed butterfly, so every lane
-// ends with the same total.
+// added to ae after each chunk of 64 k (skipped when no lane of the warp has
+// one: adding zero changes nothing); then warp_sum3, so every lane ends with
+// the same total.
 __device__ __forceinline__ d3 warp_source_sum(const Dev& D, const double* __restrict__ rc, int b0, int c0, int c1,
                                               int self, const d3& pos, double soft2) {
   const int lane = (int)(threadIdx.x & 31);
   d3 a0 = {0.0, 0.0, 0.0}, a1 = {0.0, 0.0, 0.0}, ae = {0.0, 0.0, 0.0};
+  bool any_slow = false;
   for (int base = c0; base < c1; base += 64 * 32) {
     const int end = min(c1, base + 64 * 32);
     unsigned long long slow = 0ull;
@@ -1623,6 +1647,7 @@ __device__ __forceinline__ d3 warp_source_sum(const Dev& D, const double* __rest
       if (bs_fast_term(D, rc, b0, self, i + 32, pos, soft2, a1)) slow |= 1ull << (k + 1);
     }
     if (i < end && bs_fast_term(D, rc, b0, self, i, pos, soft2, a0)) slow |= 1ull << k;
+    any_slow |= slow != 0ull;
     while (slow) {
       const int q = __ffsll((long long)slow) - 1;
       slow &= slow - 1ull;
@@ -1633,13 +1658,10 @@ __device__ __forceinline__ d3 warp_source_sum(const Dev& D, const double* __rest
         pair_exact<true>(pos, self, src, load_src(D, rc, b0 + src), soft2, ae);
     }
   }
-  d3 acc = {(a0.x + a1.x) + ae.x, (a0.y + a1.y) + ae.y, (a0.z + a1.z) + ae.z};
-  for (int o = 16; o > 0; o >>= 1) {
-    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
-    acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
-  }
-  return acc;
+  d3 acc = {fadd(D.u, a0.x, a1.x), fadd(D.u, a0.y, a1.y), fadd(D.u, a0.z, a1.z)};
+  if (__any_sync(0xffffffffu, any_slow))
+    acc = {fadd(D.u, acc.x, ae.x), fadd(D.u, acc.y, ae.y), fadd(D.u, acc.z, ae.z)};
+  return warp_sum3(D.u, acc);
 }
 
 // Velocity update of an encounter sub-step split over the blocks of a
@@ -1754,10 +1776,10 @@ struct MidRow {
 
 
 // Encounter sub-step of the big systems (three Richardson rows, N = 1, 2, 4)
-// as a persistent task kernel.  The work of an encounter body is 29 part
-// sums: evaluations 0-3 of row 2 (N = 4 sub-steps), 0-1 of row 1 (N = 2) and
-// 0 of row 0 (N = 1), each over enc_parts(row) contiguous parts of the
-// sources (warp_source_sum).  The rows are independent until the final
+// as a persistent task kernel.  The work of an encounter body is
+// enc_tasks_per_body() part sums: evaluations 0-3 of row 2 (N = 4
+// sub-steps), 0-1 of row 1 (N = 2) and 0 of row 0 (N = 1), each over
+// enc_parts(row, e) contiguous parts of the sources (warp_source_sum).  The rows are independent until the final
 // extrapolation, so the critical path is row 2's four evaluations.  Warps take
 // tasks from one atomic counter in units of one (row, evaluation) for every
 // body, in the order kEncOrder, where every unit follows the one it depends
@@ -1781,27 +1803,41 @@ constexpr int kEncTaskWarps = 4;       // warps per block
 constexpr unsigned kEncSleepMax = 256;  // longest sleep between polls, ns (2 us: waiters woke later)
 constexpr int kEncSpin = 1 << 22;      // polls of a dependency wait in a step (about two seconds)
 constexpr int kEncBlocksPerSM = 2;     // more warps lengthen every task on the shared FP64 unit
-// parts of the sources per evaluation of rows 0, 1 and 2, one task each.
+// Evaluation slots of an encounter body: 0-3 row 2's evaluations, 4-5 row 1's,
+// 6 row 0's.
+__host__ __device__ constexpr int enc_slot(int row, int e) { return row == 2 ? e : (row == 1 ? 4 + e : 6); }
+// parts of the sources per evaluation slot, one task each, 4 bits per slot.
 // Measured on the 2002-body disk (ms per step at ~150 / ~190 encounter
-// bodies): 3, 3, 5 parts 0.2695 / 0.2836; 4, 4, 4 0.2757 / 0.2880; 4, 4, 8
-// 0.2821 / 0.2998; 2, 2, 2 0.331 / 0.347.  Shorter tasks on the critical
-// row, longer ones (fewer per-task costs) on the filler rows.
-constexpr int kEncP0 = 3, kEncP1 = 3, kEncP2 = 5;
-__host__ __device__ constexpr int enc_parts(int row) { return row == 2 ? kEncP2 : (row == 1 ? kEncP1 : kEncP0); }
+// bodies), by row (0, 1, 2) with every evaluation of a row alike: 3, 3, 5
+// parts 0.2695 / 0.2836; 4, 4, 4 0.2757 / 0.2880; 4, 4, 8 0.2821 / 0.2998;
+// 2, 2, 2 0.331 / 0.347.  Shorter tasks on the critical row, longer ones
+// (fewer per-task costs) on the filler rows.
+constexpr unsigned kEncPartsBySlot = 5u | 5u << 4 | 5u << 8 | 5u << 12 | 3u << 16 | 3u << 20 | 3u << 24;
+__host__ __device__ constexpr int enc_parts_slot(int slot) { return (int)((kEncPartsBySlot >> (4 * slot)) & 15u); }
+__host__ __device__ constexpr int enc_parts(int row, int e) { return enc_parts_slot(enc_slot(row, e)); }
+// tasks per encounter body, and the first part sum of an evaluation slot
+// within a body's kEncQ (3 per part, slots in order)
+__host__ __device__ constexpr int enc_tasks_per_body() {
+  int t = 0;
+  for (int s = 0; s < 7; s++) t += enc_parts_slot(s);
+  return t;
+}
+__host__ __device__ constexpr int enc_qoff(int slot) {
+  int o = 0;
+  for (int s = 0; s < slot; s++) o += 3 * enc_parts_slot(s);
+  return o;
+}
 // part sums per encounter body: 3 per part of the seven evaluations
-constexpr int kEncQ = 3 * (4 * kEncP2 + 2 * kEncP1 + kEncP0);
-// Hand-out order of the seven (row, evaluation) units of enc_parts(row) x count
-// tasks, 4 bits each (row | e << 2), every unit after the unit it depends on: the
-// critical row 2 first, the other rows' units as filler between its
+constexpr int kEncQ = 3 * enc_tasks_per_body();
+// Hand-out order of the seven (row, evaluation) units of enc_parts(row, e) x
+// count tasks, 4 bits each (row | e << 2), every unit after the unit it depends
+// on: the critical row 2 first, the other rows' units as filler between its
 // evaluations.
 constexpr unsigned enc_unit(int row, int e) { return (unsigned)(row | e << 2); }
 constexpr unsigned kEncOrder = enc_unit(2, 0) | enc_unit(1, 0) << 4 | enc_unit(2, 1) << 8 | enc_unit(0, 0) << 12 |
                                enc_unit(2, 2) << 16 | enc_unit(1, 1) << 20 | enc_unit(2, 3) << 24;
-__device__ __forceinline__ int enc_slot(int row, int e) { return row == 2 ? e : (row == 1 ? 4 + e : 6); }
-// first part sum of an evaluation slot within a body's kEncQ
-__device__ __forceinline__ int enc_qoff(int slot) {
-  return slot < 4 ? 3 * kEncP2 * slot
-                  : (slot < 6 ? 3 * (4 * kEncP2 + kEncP1 * (slot - 4)) : 3 * (4 * kEncP2 + 2 * kEncP1));
+__host__ __device__ constexpr int enc_unit_parts(int unit) {
+  return enc_parts((int)((kEncOrder >> (4 * unit)) & 3u), (int)((kEncOrder >> (4 * unit + 2)) & 3u));
 }
 
 // The whole warp polls *flag >= want (one load of the same address; the
@@ -1832,7 +1868,7 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
   griddep_enter();
   const int lane = (int)(threadIdx.x & 31);
   const int count = D.ce_count[1];
-  const int total = (4 * kEncP2 + 2 * kEncP1 + kEncP0) * count;
+  const int total = enc_tasks_per_body() * count;
   const int nm1 = ONE ? D.nm[0] : 0;
   int* err = D.enc_head + 1;
   for (;;) {
@@ -1840,14 +1876,14 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
     if (lane == 0) t = atomicAdd(D.enc_head, 1);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= total || *(volatile const int*)err) break;
-    // seven units of enc_parts(row) x count tasks, (row, evaluation) in hand-out order
+    // seven units of enc_parts(row, e) x count tasks, (row, evaluation) in hand-out order
     int unit = 0, u = t;
-    while (u >= enc_parts((kEncOrder >> (4 * unit)) & 3) * count) {
-      u -= enc_parts((kEncOrder >> (4 * unit)) & 3) * count;
+    while (u >= enc_unit_parts(unit) * count) {
+      u -= enc_unit_parts(unit) * count;
       unit++;
     }
     const int row = (kEncOrder >> (4 * unit)) & 3, e = (kEncOrder >> (4 * unit + 2)) & 3;
-    const int P = enc_parts(row);
+    const int P = enc_parts(row, e);
     const int k = u / P, q = u % P;
     const int j = D.ce_list_big[k];
     const int n = D.n, s = ONE ? 0 : D.sys[j], b0 = ONE ? 0 : D.off[s], nm = ONE ? nm1 : D.nm[s];

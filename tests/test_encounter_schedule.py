@@ -13,8 +13,11 @@ HDR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), 
 
 def _constants():
     src = open(HDR).read()
-    m = re.search(r"constexpr int kEncP0 = (\d+), kEncP1 = (\d+), kEncP2 = (\d+);", src)
-    p = {0: int(m.group(1)), 1: int(m.group(2)), 2: int(m.group(3))}
+    m = re.search(r"constexpr unsigned kEncPartsBySlot = ([^;]+);", src)
+    parts = re.findall(r"(\d+)u(?: << (\d+))?", m.group(1))
+    p = [0] * 7  # parts per evaluation slot
+    for v, shift in parts:
+        p[int(shift or 0) // 4] = int(v)
     m = re.search(r"constexpr unsigned kEncOrder = ([^;]+);", src)
     units = re.findall(r"enc_unit\((\d), (\d)\)(?: << (\d+))?", m.group(1))
     order = [None] * len(units)
@@ -24,11 +27,7 @@ def _constants():
 
 
 def _qoff(p, slot):
-    if slot < 4:
-        return 3 * p[2] * slot
-    if slot < 6:
-        return 3 * (4 * p[2] + p[1] * (slot - 4))
-    return 3 * (4 * p[2] + 2 * p[1])
+    return 3 * sum(p[:slot])
 
 
 def _slot(row, e):
@@ -47,15 +46,15 @@ def test_order_respects_dependencies():
 def test_decode_covers_every_task_once():
     p, order = _constants()
     for count in (1, 2, 7, 190):
-        total = (4 * p[2] + 2 * p[1] + p[0]) * count
+        total = sum(p) * count
         seen = set()
         for t in range(total):
             unit, u = 0, t
-            while u >= p[order[unit][0]] * count:
-                u -= p[order[unit][0]] * count
+            while u >= p[_slot(*order[unit])] * count:
+                u -= p[_slot(*order[unit])] * count
                 unit += 1
             row, e = order[unit]
-            P = p[row]
+            P = p[_slot(row, e)]
             k, q = divmod(u, P)
             assert 0 <= k < count and 0 <= q < P
             seen.add((row, e, k, q))
@@ -68,9 +67,10 @@ def test_part_slots_do_not_overlap():
     for row, evals in ((2, 4), (1, 2), (0, 1)):
         for e in range(evals):
             off = _qoff(p, _slot(row, e))
-            spans.append((off, off + 3 * p[row]))
+            spans.append((off, off + 3 * p[_slot(row, e)]))
     spans.sort()
     for (a0, a1), (b0, b1) in zip(spans, spans[1:]):
         assert a1 <= b0
     assert spans[0][0] == 0
-    assert spans[-1][1] == 3 * (4 * p[2] + 2 * p[1] + p[0])  # kEncQ
+    assert spans[-1][1] == 3 * sum(p)  # kEncQ
+    assert all(1 <= v <= 15 for v in p)
