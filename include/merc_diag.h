@@ -17,7 +17,9 @@ extern "C" {
 #endif
 
 /* Evaluate a merc_math function on the GPU for n inputs: fn 0 sin, 1 cos,
- * 2 atan2(x, y), 3 acos, 4 log, 5 sinh, 6 cosh, 7 cbrt, 8 exp. */
+ * 2 atan2(x, y), 3 acos, 4 log, 5 sinh, 6 cosh, 7 cbrt, 8 exp; and the
+ * quotients of the Richardson combination: 9 x / 3, 11 x / 15, 12 x / 63 by
+ * the known-reciprocal correction, 10 x / y by the division. */
 int merc_diag_math(int device, int fn, int64_t n, const double* x, const double* y, double* out);
 
 /* FP64 FMA throughput of the device in TFLOP/s (2 flops per FMA), best of

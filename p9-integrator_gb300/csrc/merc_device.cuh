@@ -418,10 +418,39 @@ __device__ __forceinline__ PV mod_midpoint(PV c, const VT& vt, double dt, int N)
   return res;
 }
 
+// x / d bit for bit, for a divisor whose reciprocal y = RN(1 / d) lies below
+// 1 / d by at most 2^-54 relative (d = 3, 15, 63: 2^-54, 2^-56, 2^-54).  Then
+// q = RN(x y) is within one ulp of x / d, the remainder r = x - d q is exact in
+// one fma, and RN(q + r y) is the correctly rounded quotient: Markstein's
+// theorem on the FMA correction of a faithful quotient (P. W. Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Develop. 34(1), 1990).  The theorem needs x / d to
+// be a normal number, so |x| outside 2^-1000 .. 2^1000 takes the division;
+// r = 0 keeps q, so a zero quotient keeps the sign of x.  Three FP64
+// instructions instead of the division's software sequence, whose dependent
+// steps made the Richardson combination of an encounter body the longest
+// serial part of the encounter sub-step on this GPU's FP64 units.
+__device__ __forceinline__ double div_known(double x, double d, double y) {
+  const int ex = (__double2hiint(x) >> 20) & 0x7ff;
+  if (ex < 1023 - 1000 || ex > 1023 + 1000) return x / d;
+  const double q = x * y;
+  const double r = fma(-q, d, x);
+  return r == 0.0 ? q : fma(r, y, q);
+}
+
+// RN(1 / den) for the Richardson denominators 4^j - 1 of up to four rows
+// (0 for any other value: the caller divides)
+__device__ __forceinline__ double rich_recip(double den) {
+  return den == 3.0 ? 1.0 / 3.0 : (den == 15.0 ? 1.0 / 15.0 : (den == 63.0 ? 1.0 / 63.0 : 0.0));
+}
+
+// (p4 a - q) / (p4 - 1) per component (sim.cuh:522-544), the quotient by
+// div_known: the same bits as the division
 __device__ __forceinline__ void rich_combine(PV& o, const PV& a, const PV& q, double p4) {
-  double den = p4 - 1.0;
-  o.pos = {fma(p4, a.pos.x, -q.pos.x) / den, fma(p4, a.pos.y, -q.pos.y) / den, fma(p4, a.pos.z, -q.pos.z) / den};
-  o.vel = {fma(p4, a.vel.x, -q.vel.x) / den, fma(p4, a.vel.y, -q.vel.y) / den, fma(p4, a.vel.z, -q.vel.z) / den};
+  const double den = p4 - 1.0, y = rich_recip(den);
+  auto dv = [den, y](double x) { return y != 0.0 ? div_known(x, den, y) : x / den; };
+  o.pos = {dv(fma(p4, a.pos.x, -q.pos.x)), dv(fma(p4, a.pos.y, -q.pos.y)), dv(fma(p4, a.pos.z, -q.pos.z))};
+  o.vel = {dv(fma(p4, a.vel.x, -q.vel.x)), dv(fma(p4, a.vel.y, -q.vel.y)), dv(fma(p4, a.vel.z, -q.vel.z))};
 }
 
 // The Richardson tableau of richardson() from its rows' modified-midpoint

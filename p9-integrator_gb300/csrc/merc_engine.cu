@@ -55,8 +55,6 @@ struct merc_ctx {
   int device = 0;
   merc_params p{};
   cudaStream_t stream = nullptr;
-  cudaStream_t side = nullptr;  // second branch of the step graphs (drift beside the encounter sub-step)
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::string err;
   Dev D;
   int* d_off = nullptr;
@@ -643,20 +641,18 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     const int dthr = (D.n + kDriftThreads - 1) / kDriftThreads < ctx->sms ? 32 : kDriftThreads;
     // Without small systems the drift (bodies not in encounter) and the big
     // systems' encounter sub-step (the list built by the encounter test) are
-    // independent: the drift runs on a second branch beside it.
-    const bool fork = !ctx->has_small && ctx->has_big;
-    if (fork) {
-      CK(cudaEventRecord(ctx->ev_fork, s));
-      CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-      k_drift_universal<<<(unsigned)((D.n + dthr - 1) / dthr), dthr, 0, ctx->side>>>(
-          D, rcB, p.dt, p.compat_block, p.kepler_tol, p.kepler_max_iter, guess_of(p), mlp, ctx->d_log,
-          ctx->d_log_count, ctx->log_cap);
-      CK(cudaGetLastError());
-      CK(cudaEventRecord(ctx->ev_join, ctx->side));
-    } else {
-      launch(k_drift_universal, (unsigned)((D.n + dthr - 1) / dthr), dthr, D, rcB, p.dt, p.compat_block,
-             p.kepler_tol, p.kepler_max_iter, guess_of(p), mlp, ctx->d_log, ctx->d_log_count, ctx->log_cap);
-    }
+    // independent, and they run side by side: the drift lets the next kernel
+    // launch as soon as it starts (its own dependency wait has returned, so
+    // the encounter test is complete), and the encounter task kernel skips
+    // its dependency wait at the start and waits for the drift at its end, so
+    // its completion still implies the drift's.  (Placed on a second graph
+    // branch instead, the drift's blocks were not scheduled until the
+    // encounter kernel's warps began to exit: a %globaltimer timeline showed
+    // it starting 108 us into a 130 us encounter sub-step and ending after it.)
+    const bool overlap = !ctx->has_small && ctx->has_big && ctx->pdl && p.bs_rows == 3;
+    launch(k_drift_universal, (unsigned)((D.n + dthr - 1) / dthr), dthr, D, rcB, p.dt, p.compat_block,
+           p.kepler_tol, p.kepler_max_iter, guess_of(p), mlp, ctx->d_log, ctx->d_log_count, ctx->log_cap,
+           overlap ? 1 : 0);
     nk++;
     if (ctx->has_small) {
       launch(k_encounter_small, ctx->enc_blocks, 64, D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2);
@@ -664,22 +660,22 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     }
     if (ctx->has_big) {
       // (encounter timing: events on the step stream around the launch; the
-      // drift runs on the second branch, outside the interval)
+      // event between the drift and this kernel makes them run one after the
+      // other, so the interval holds the encounter sub-step alone)
       const bool enc_ev = ctx->time_encounter && !ctx->enc_ev.empty();
       if (enc_ev) CK(cudaEventRecordWithFlags(ctx->enc_ev[2 * step_in_graph], s, cudaEventRecordExternal));
       if (p.bs_rows == 3 && D.nsys == 1)
         launch(k_encounter_tasks<true>, ctx->sms * kEncBlocksPerSM, 32 * kEncTaskWarps, D, rcB, p.dt,
-               p.compat_block, p.softening2, kEncSpin);
+               p.compat_block, p.softening2, kEncSpin, overlap ? 1 : 0);
       else if (p.bs_rows == 3)
         launch(k_encounter_tasks<false>, ctx->sms * kEncBlocksPerSM, 32 * kEncTaskWarps, D, rcB, p.dt,
-               p.compat_block, p.softening2, kEncSpin);
+               p.compat_block, p.softening2, kEncSpin, overlap ? 1 : 0);
       else
         launch(k_encounter_cluster, ctx->enc_blocks * 2, 32, D, rcB, p.dt, p.compat_block, p.bs_rows,
                p.softening2);
       if (enc_ev) CK(cudaEventRecordWithFlags(ctx->enc_ev[2 * step_in_graph + 1], s, cudaEventRecordExternal));
       nk++;
     }
-    if (fork) CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
     if (ctx->collide_on) {
       launch(k_collide_find, ctx->sms * 4, 256, D, ctx->col);
       launch(k_collide_resolve, 1, 32, D, ctx->col, p.hill_factor);
@@ -967,9 +963,6 @@ int merc_create(int device, const merc_params* p, merc_ctx** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) {
@@ -993,9 +986,6 @@ int merc_destroy(merc_ctx* ctx) {
   for (cudaEvent_t e : ctx->enc_ev) cudaEventDestroy(e);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
-  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
-  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
-  if (ctx->side) cudaStreamDestroy(ctx->side);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return MERC_OK;
@@ -2032,7 +2022,7 @@ static int step_static(int device, const merc_params* p, int32_t n_bodies, int32
       k_ce_tiled<<<(unsigned)work.size(), kTile, 0, s>>>(D, d_work, rcB, p->compat_block);
     }
     k_drift_universal<<<nb, kThreads, 0, s>>>(D, rcB, p->dt, p->compat_block, p->kepler_tol, p->kepler_max_iter,
-                                              guess_of(*p), nullptr, nullptr, nullptr, 0);
+                                              guess_of(*p), nullptr, nullptr, nullptr, 0, 0);
     if (!big)
       k_encounter_small<<<sms * 4, 64, 0, s>>>(D, rcB, p->dt, p->compat_block, p->bs_rows, p->softening2);
     else
@@ -2156,13 +2146,13 @@ int merc_diag_encounter_wait(merc_ctx* ctx, int32_t* gave_up) {
     }
   // one listed body; tasks start at the second unit (the first unit, row 2's
   // evaluation 0 of every listed body, is skipped)
-  const int one = 1, head[2] = {enc_unit_parts(0), 0};
+  const int one = 1, head[2] = {enc_parts_slot(0), 0};
   CK(cudaMemcpy(D.ce_list_big, &body, sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(D.ce_count + 1, &one, sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(D.enc_head, head, sizeof head, cudaMemcpyHostToDevice));
   CK(cudaMemset(D.enc_cnt, 0, 11 * sizeof(int)));
   k_encounter_tasks<false><<<ctx->sms * kEncBlocksPerSM, 32 * kEncTaskWarps, 0, ctx->stream>>>(
-      D, D.rc[ctx->rc_cur], ctx->p.dt, ctx->p.compat_block, ctx->p.softening2, 4096);
+      D, D.rc[ctx->rc_cur], ctx->p.dt, ctx->p.compat_block, ctx->p.softening2, 4096, 0);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
   int h[2] = {0, 0};

@@ -29,6 +29,11 @@ constexpr int kEncCluster = 4;   // blocks (a thread-block cluster) per encounte
 // was launched without the attribute), then allow the next kernel to be
 // scheduled.  Called first in every kernel of the step graphs.
 __device__ __forceinline__ void griddep_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Let the next kernel of the stream launch before this one completes (it
+// still waits in griddep_enter unless it is written to wait elsewhere).
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+// The dependency wait of griddep_enter, for a kernel that waits at its end.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 struct Work {
   int sys, t0, c0, c1, chunk;
@@ -1412,8 +1417,10 @@ constexpr int kDriftThreads = MERC_DRIFT_THREADS;  // block of the universal dri
 __global__ void k_drift_universal(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, double tol,
                                   int max_iter, double guess, const float* __restrict__ mlp,
                                   float* __restrict__ log_data, unsigned long long* __restrict__ log_count,
-                                  long long log_cap) {
+                                  long long log_cap, int trigger) {
   griddep_enter();
+  // trigger: the encounter task kernel that follows runs beside this one
+  if (trigger) griddep_launch();
   __shared__ float blob[kBlob];
   if (mlp) {
     for (int k = threadIdx.x; k < kBlob; k += blockDim.x) blob[k] = mlp[k];
@@ -1864,8 +1871,11 @@ __device__ __forceinline__ bool enc_wait(const int* flag, int want, int* err, in
 template <bool ONE>
 __global__ void __launch_bounds__(32 * kEncTaskWarps)
     k_encounter_tasks(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, double soft2,
-                      int spin) {
-  griddep_enter();
+                      int spin, int late_wait) {
+  // late_wait: the preceding kernel is the drift, launched after the
+  // encounter test completed and independent of this kernel; wait for it at
+  // the end instead, so that this kernel's completion implies the drift's
+  if (!late_wait) griddep_enter();
   const int lane = (int)(threadIdx.x & 31);
   const int count = D.ce_count[1];
   const int total = enc_tasks_per_body() * count;
@@ -1972,6 +1982,7 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
     }
     if (lane < 11) cnt[lane] = 0;  // every task of this body is done
   }
+  if (late_wait) griddep_wait();
 }
 
 // ---------------------------------------------------------------------------
@@ -2057,6 +2068,10 @@ __global__ void k_mm_eval(int fn, int n, const double* x, const double* y, doubl
     case 5: r = mm::sinh(a); break;
     case 6: r = mm::cosh(a); break;
     case 7: r = mm::cbrt(a); break;
+    case 9: r = div_known(a, 3.0, 1.0 / 3.0); break;
+    case 10: r = a / y[i]; break;
+    case 11: r = div_known(a, 15.0, 1.0 / 15.0); break;
+    case 12: r = div_known(a, 63.0, 1.0 / 63.0); break;
     default: r = mm::exp(a); break;
   }
   out[i] = r;

@@ -458,7 +458,8 @@ def warm_start_probe(pos, vel, dt, blob=None, tol=1e-13, max_iter=30, device: in
     return g, s, it
 
 
-MM_FUNCS = {"sin": 0, "cos": 1, "atan2": 2, "acos": 3, "log": 4, "sinh": 5, "cosh": 6, "cbrt": 7, "exp": 8}
+MM_FUNCS = {"sin": 0, "cos": 1, "atan2": 2, "acos": 3, "log": 4, "sinh": 5, "cosh": 6, "cbrt": 7, "exp": 8,
+            "div3": 9, "div": 10, "div15": 11, "div63": 12}
 
 
 def device_math(fn: str, x, y=None, device: int = 0) -> np.ndarray:

@@ -9,8 +9,14 @@ root):
   signed zeros and subnormals included;
 - exact_term (merc_device.cuh) sets the changeover weight K = 1 without the
   division y = t / b when b >= 2^-1000, t > fl(b (1 + 2^-51)) and
-  t < fl(b 1e300): then fl(t / b) is a finite double > 1.
+  t < fl(b 1e300): then fl(t / b) is a finite double > 1;
+- div_known (merc_device.cuh), the Richardson quotients x / d for d = 3, 15,
+  63: q = fl(x y) with y = fl(1 / d), r = x - d q exact, fl(q + r y) equals
+  the correctly rounded x / d (Markstein's correction), restated here with
+  exact rational arithmetic for the fma steps.
 """
+from fractions import Fraction
+
 import numpy as np
 
 SPECIAL = np.array([0.0, -0.0, 1.0, -1.0, np.inf, -np.inf, np.nan, 5e-324, -5e-324, 2.2250738585072014e-308,
@@ -71,3 +77,42 @@ def test_changeover_division_skip_bound():
             y = t[ok] / b[ok]
             assert np.isfinite(y).all()
             assert (y > 1.0).all()
+
+
+def _div_known(x, d, y):
+    """div_known with exact fma steps (Fraction arithmetic rounds once)."""
+    if not (2.0 ** -1000 <= abs(x) <= 2.0 ** 1000):
+        return x / d
+    q = x * y  # one rounding, as the device's multiply
+    r_exact = Fraction(x) - Fraction(d) * Fraction(q)
+    r = float(r_exact)
+    assert Fraction(r) == r_exact, "the remainder is not exact"
+    if r == 0.0:
+        return q
+    return float(Fraction(q) + Fraction(r) * Fraction(y))  # fma: one rounding
+
+
+def test_known_reciprocal_division_is_correctly_rounded():
+    rng = np.random.default_rng(4)
+    for d in (3.0, 15.0, 63.0):
+        y = 1.0 / d
+        assert Fraction(y) < Fraction(1) / Fraction(d)  # the reciprocal lies below 1 / d
+        mant = rng.uniform(1.0, 2.0, 12_000)
+        expo = rng.integers(-990, 990, mant.size).astype(np.float64)
+        x = list(mant * np.exp2(expo) * rng.choice([-1.0, 1.0], mant.size))
+        # quotients next to powers of two, exact quotients, and the guard's edges
+        for k in (-900, -3, 0, 1, 7, 900):
+            base = d * 2.0 ** k
+            v = base
+            for _ in range(40):
+                x += [v, -v]
+                v = np.nextafter(v, np.inf)
+            v = base
+            for _ in range(40):
+                v = np.nextafter(v, 0.0)
+                x += [v]
+        x += [0.0, -0.0, 2.0 ** -1000, 2.0 ** 1000, 2.0 ** -1001, 2.0 ** 1001, 5e-324, 1e308]
+        for v in x:
+            got = _div_known(float(v), d, y)
+            want = float(v) / d
+            assert np.float64(got).view(np.uint64) == np.float64(want).view(np.uint64), (v, d, got, want)
