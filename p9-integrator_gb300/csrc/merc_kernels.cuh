@@ -1180,6 +1180,7 @@ constexpr int kRedThreads = MERC_RED_THREADS;  // threads per body of k_kick_red
 #define MERC_RED_BATCH 4
 #endif
 constexpr int kRedBatch = MERC_RED_BATCH;  // partials loaded per thread before they are added
+constexpr int kNearList = 32;             // near pairs per body dealt out over its threads
 
 // Kick of every body of a big system whose sums are in partials: massive
 // bodies add their far-field block partials (symmetric kernel, set 1 when
@@ -1281,8 +1282,43 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
       }
     }
   }
+  // Near pairs (reference formula, a chain of ~45 dependent FP64 operations
+  // each): a body's set mask bits usually sit in one or two words, i.e. with
+  // one or two of its threads.  They are listed in shared memory in (thread,
+  // word, bit) order and the list is dealt out over the body's threads, so
+  // the chain is about one pair long; thread sub adds entries sub,
+  // sub + kRedThreads, ... in order (a fixed order, whatever the schedule).  A
+  // body with more than kNearList near pairs keeps them with their threads.
+  __shared__ int near_list[kThreads / kRedThreads][kNearList];
+  int own = 0;
+#pragma unroll
+  for (int u = 0; u < kRedBatch; u++) own += __popc(words[u]);
+  for (int b = sub + kRedBatch * kRedThreads; massive && b < count; b += kRedThreads)
+    own += __popc(mask[(size_t)b * nm + local]);
+  int incl = own;
+  for (int o = 1; o < kRedThreads; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o, kRedThreads);
+    if (sub >= o) incl += v;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, kRedThreads - 1, kRedThreads);
+  const bool dealt = total <= kNearList;
+  int* list = near_list[threadIdx.x / kRedThreads];
+  if (dealt && massive) {
+    int at = incl - own;
+#pragma unroll
+    for (int u = 0; u < kRedBatch; u++)
+      for (uint32_t w = words[u]; w; w &= w - 1u) list[at++] = 32 * (sub + u * kRedThreads) + __ffs(w) - 1;
+    for (int b = sub + kRedBatch * kRedThreads; b < count; b += kRedThreads)
+      for (uint32_t w = mask[(size_t)b * nm + local]; w; w &= w - 1u) list[at++] = 32 * b + __ffs(w) - 1;
+  }
+  __syncwarp();
   d3 near = {0.0, 0.0, 0.0};
-  if (massive) {
+  if (massive && dealt) {
+    for (int q = sub; q < total; q += kRedThreads) {
+      const int src = list[q];
+      pair_exact<false>(pos, local, src, load_src(D, rc, b0 + src), soft2, near);
+    }
+  } else if (massive) {
 #pragma unroll
     for (int u = 0; u < kRedBatch; u++) {
       const int b = sub + u * kRedThreads;
