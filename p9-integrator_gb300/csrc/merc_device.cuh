@@ -444,13 +444,15 @@ __device__ __forceinline__ double rich_recip(double den) {
   return den == 3.0 ? 1.0 / 3.0 : (den == 15.0 ? 1.0 / 15.0 : (den == 63.0 ? 1.0 / 63.0 : 0.0));
 }
 
-// (p4 a - q) / (p4 - 1) per component (sim.cuh:522-544), the quotient by
+// (p4 a - q) / (p4 - 1) for one component (sim.cuh:522-544), the quotient by
 // div_known: the same bits as the division
+__device__ __forceinline__ double rich_q(double a, double q, double p4) {
+  const double den = p4 - 1.0, y = rich_recip(den), x = fma(p4, a, -q);
+  return y != 0.0 ? div_known(x, den, y) : x / den;
+}
 __device__ __forceinline__ void rich_combine(PV& o, const PV& a, const PV& q, double p4) {
-  const double den = p4 - 1.0, y = rich_recip(den);
-  auto dv = [den, y](double x) { return y != 0.0 ? div_known(x, den, y) : x / den; };
-  o.pos = {dv(fma(p4, a.pos.x, -q.pos.x)), dv(fma(p4, a.pos.y, -q.pos.y)), dv(fma(p4, a.pos.z, -q.pos.z))};
-  o.vel = {dv(fma(p4, a.vel.x, -q.vel.x)), dv(fma(p4, a.vel.y, -q.vel.y)), dv(fma(p4, a.vel.z, -q.vel.z))};
+  o.pos = {rich_q(a.pos.x, q.pos.x, p4), rich_q(a.pos.y, q.pos.y, p4), rich_q(a.pos.z, q.pos.z, p4)};
+  o.vel = {rich_q(a.vel.x, q.vel.x, p4), rich_q(a.vel.y, q.vel.y, p4), rich_q(a.vel.z, q.vel.z, p4)};
 }
 
 // The Richardson tableau of richardson() from its rows' modified-midpoint

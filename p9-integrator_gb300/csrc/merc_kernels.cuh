@@ -615,23 +615,37 @@ __global__ void __cluster_dims__(kJumpCluster, 1, 1) __launch_bounds__(kJumpThre
     part[2] = sz;
   }
   cl.sync();
-  double Px = 0.0, Py = 0.0, Pz = 0.0;
+  // the partials of the cluster's blocks: every remote load in flight before
+  // the additions, which run in rank order
+  double q[kJumpCluster][3];
+#pragma unroll
   for (int r = 0; r < kJumpCluster; r++) {
-    const double* q = cl.map_shared_rank(part, r);
-    Px += q[0];
-    Py += q[1];
-    Pz += q[2];
+    const double* p = cl.map_shared_rank(part, r);
+    q[r][0] = p[0];
+    q[r][1] = p[1];
+    q[r][2] = p[2];
   }
-  cl.sync();  // no block leaves while another may still read its partial
-  if (!mine) return;
-  if (CLEAR) D.ce[j] = 0;
-  const d3 x = {fma(Px, hdt, x0.x), fma(Py, hdt, x0.y), fma(Pz, hdt, x0.z)};
-  store3(D.x, n, j, x);
-  D.xf[j] = f32_trunc(x.x);
-  D.xf[n + j] = f32_trunc(x.y);
-  D.xf[2 * n + j] = f32_trunc(x.z);
-  if (vsrc) store3(D.v, n, j, v);
-  if (j < nm) write_rc(rc_out, n, j, x, v, hc_j);
+  double Px = 0.0, Py = 0.0, Pz = 0.0;
+#pragma unroll
+  for (int r = 0; r < kJumpCluster; r++) {
+    Px += q[r][0];
+    Py += q[r][1];
+    Pz += q[r][2];
+  }
+  // no block leaves while another may still read its partial: arrive now,
+  // wait at the end, after this thread's own work
+  auto reads_done = cl.barrier_arrive();
+  if (mine) {
+    if (CLEAR) D.ce[j] = 0;
+    const d3 x = {fma(Px, hdt, x0.x), fma(Py, hdt, x0.y), fma(Pz, hdt, x0.z)};
+    store3(D.x, n, j, x);
+    D.xf[j] = f32_trunc(x.x);
+    D.xf[n + j] = f32_trunc(x.y);
+    D.xf[2 * n + j] = f32_trunc(x.z);
+    if (vsrc) store3(D.v, n, j, v);
+    if (j < nm) write_rc(rc_out, n, j, x, v, hc_j);
+  }
+  cl.barrier_wait(std::move(reads_done));
 }
 
 // Sets body j's encounter flag (one byte of D.ce, by an atomic OR on its
@@ -1854,8 +1868,11 @@ __host__ __device__ constexpr int enc_slot(int row, int e) { return row == 2 ? e
 // bodies), by row (0, 1, 2) with every evaluation of a row alike: 3, 3, 5
 // parts 0.2695 / 0.2836; 4, 4, 4 0.2757 / 0.2880; 4, 4, 8 0.2821 / 0.2998;
 // 2, 2, 2 0.331 / 0.347.  Shorter tasks on the critical row, longer ones
-// (fewer per-task costs) on the filler rows.
-constexpr unsigned kEncPartsBySlot = 5u | 5u << 4 | 5u << 8 | 5u << 12 | 3u << 16 | 3u << 20 | 3u << 24;
+// (fewer per-task costs) on the filler rows.  Six parts on row 2's last
+// evaluation (the last tasks handed out) shorten the kernel's tail: 0.2618
+// -> 0.2603 ms per step at ~188 encounter bodies (eight: 0.2618; 6 or 8
+// parts on earlier evaluations, or 4 on row 1's second, did not pay).
+constexpr unsigned kEncPartsBySlot = 5u | 5u << 4 | 5u << 8 | 6u << 12 | 3u << 16 | 3u << 20 | 3u << 24;
 __host__ __device__ constexpr int enc_parts_slot(int slot) { return (int)((kEncPartsBySlot >> (4 * slot)) & 15u); }
 __host__ __device__ constexpr int enc_parts(int row, int e) { return enc_parts_slot(enc_slot(row, e)); }
 // tasks per encounter body, and the first part sum of an evaluation slot
@@ -2003,18 +2020,26 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
     }
     if (!__shfl_sync(0xffffffffu, fin, 0)) continue;
     __threadfence();
-    if (lane == 0) {
-      PV b[3];
-      for (int r = 0; r < 3; r++) {
-        const double* rs = res + 6 * r;
-        b[r] = {{__ldcg(rs), __ldcg(rs + 1), __ldcg(rs + 2)}, {__ldcg(rs + 3), __ldcg(rs + 4), __ldcg(rs + 5)}};
+    // The Richardson combination (rich_combine's arithmetic per component),
+    // one component per lane: lanes 0-5 combine rows 1 and 0 (b11), lanes
+    // 6-11 rows 2 and 1 (b21), then lanes 0-5 b21 and b11 (b22).  A warp
+    // instruction costs the FP64 unit the same however few lanes run it, so
+    // the eighteen quotients take a few instructions instead of dozens.
+    {
+      const int c = lane < 6 ? lane : lane - 6;  // component: pos x, y, z, vel x, y, z
+      double b = 0.0;
+      if (lane < 12) {
+        const int r = lane < 6 ? 1 : 2;  // the finer row; the coarser is r - 1
+        b = rich_q(__ldcg(res + 6 * r + c), __ldcg(res + 6 * (r - 1) + c), 4.0);
       }
-      PV b11, b21, b22;
-      rich_combine(b11, b[1], b[0], 4.0);
-      rich_combine(b21, b[2], b[1], 4.0);
-      rich_combine(b22, b21, b11, 16.0);
-      store3(D.xo, n, j, b22.pos);
-      store3(D.vo, n, j, b22.vel);
+      const double b21 = __shfl_sync(0xffffffffu, b, (lane + 6) & 31);
+      if (lane < 6) {
+        const double b22 = rich_q(b21, b, 16.0);
+        if (c < 3)
+          D.xo[(size_t)c * n + j] = b22;
+        else
+          D.vo[(size_t)(c - 3) * n + j] = b22;
+      }
     }
     if (lane < 11) cnt[lane] = 0;  // every task of this body is done
   }
