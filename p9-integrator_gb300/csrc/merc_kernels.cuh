@@ -1900,6 +1900,24 @@ __host__ __device__ constexpr int enc_unit_parts(int unit) {
   return enc_parts((int)((kEncOrder >> (4 * unit)) & 3u), (int)((kEncOrder >> (4 * unit + 2)) & 3u));
 }
 
+// Release / acquire forms of the encounter task kernel's publications: the
+// part sums and row states a warp stores are ordered before the counter it
+// updates (release), and a warp that reads the counter orders its later loads
+// after it (acquire), without a full fence on either side.
+__device__ __forceinline__ int atom_add_acq_rel(int* p, int v) {
+  int r;
+  asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(r) : "l"(p), "r"(v) : "memory");
+  return r;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int r;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(r) : "l"(p) : "memory");
+  return r;
+}
+
 // The whole warp polls *flag >= want (one load of the same address; the
 // lanes stay converged, so no lane waits in a warp-synchronous instruction
 // while another polls); bounded, and it stops early when another warp gave
@@ -1908,10 +1926,7 @@ __host__ __device__ constexpr int enc_unit_parts(int unit) {
 __device__ __forceinline__ bool enc_wait(const int* flag, int want, int* err, int spin) {
   unsigned ns = 128;
   for (int it = 0; it < spin; it++) {
-    if (__all_sync(0xffffffffu, *(volatile const int*)flag >= want)) {
-      __threadfence();
-      return true;
-    }
+    if (__all_sync(0xffffffffu, ld_acquire(flag) >= want)) return true;
     if ((it & 63) == 63 && __any_sync(0xffffffffu, *(volatile const int*)err != 0)) return false;
     __nanosleep(ns);
     ns = ns < kEncSleepMax ? 2 * ns : ns;
@@ -1967,7 +1982,10 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
       m.z1 = {__ldcg(st + 3), __ldcg(st + 4), __ldcg(st + 5)};
       m.vel = {__ldcg(st + 6), __ldcg(st + 7), __ldcg(st + 8)};
     }
-    const int c0 = (int)((int64_t)q * nm / P), c1 = (int)((int64_t)(q + 1) * nm / P);
+    // part q: whole groups of 32 sources (only the system's last group is
+    // partial), so no lane idles in a part's last round but the last part's
+    const int G = (nm + 31) / 32;
+    const int c0 = 32 * (int)((int64_t)q * G / P), c1 = min(32 * (int)((int64_t)(q + 1) * G / P), nm);
     const d3 S = warp_source_sum(D, rc_in, b0, c0, c1, self, m.z1, soft2);
     double* qs = D.enc_q + kEncQ * (size_t)k + enc_qoff(slot);
     int last = 0;
@@ -1975,11 +1993,10 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
       qs[3 * q] = S.x;
       qs[3 * q + 1] = S.y;
       qs[3 * q + 2] = S.z;
-      __threadfence();
-      last = atomicAdd(cnt + slot, 1) == P - 1;
+      last = atom_add_acq_rel(cnt + slot, 1) == P - 1;
     }
     if (!__shfl_sync(0xffffffffu, last, 0)) continue;
-    __threadfence();
+    __syncwarp();  // the other lanes' loads below after lane 0's acquire
     // last part: finish evaluation e of the row
     d3 acc = {0.0, 0.0, 0.0};
     for (int r = 0; r < P; r++) {
@@ -1999,8 +2016,7 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
         st[6] = m.vel.x;
         st[7] = m.vel.y;
         st[8] = m.vel.z;
-        __threadfence();
-        atomicExch(cnt + 7 + row, e + 1);
+        st_release(cnt + 7 + row, e + 1);
       }
       continue;
     }
@@ -2015,11 +2031,10 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
       rs[3] = mine.vel.x;
       rs[4] = mine.vel.y;
       rs[5] = mine.vel.z;
-      __threadfence();
-      fin = atomicAdd(cnt + 10, 1) == 2;
+      fin = atom_add_acq_rel(cnt + 10, 1) == 2;
     }
     if (!__shfl_sync(0xffffffffu, fin, 0)) continue;
-    __threadfence();
+    __syncwarp();  // the other lanes' loads below after lane 0's acquire
     // The Richardson combination (rich_combine's arithmetic per component),
     // one component per lane: lanes 0-5 combine rows 1 and 0 (b11), lanes
     // 6-11 rows 2 and 1 (b21), then lanes 0-5 b21 and b11 (b22).  A warp
