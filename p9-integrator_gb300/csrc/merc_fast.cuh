@@ -139,6 +139,16 @@ __device__ __forceinline__ d3 sun_accel(const FU& U, const d3& pos, double soft2
   return {-(pos.x / denom), -(pos.y / denom), -(pos.z / denom)};
 }
 
+// Component c of sun_accel (posc = pos.x, pos.y or pos.z): the same operations.
+__device__ __forceinline__ double sun_accel_c(const FU& U, const d3& pos, double posc, double soft2) {
+  double r2 = fma(pos.x, pos.x, fma(pos.y, pos.y, fmul(U, pos.z, pos.z)));
+  double s = fadd(U, r2, soft2);
+  if (seed_in_range(r2)) return fmul(U, -posc, inv_softened_r3(U, r2, s));
+  double r = stable_sqrt(r2);
+  double denom = s * r;
+  return -(posc / denom);
+}
+
 // x as an FP32 number by integer operations on the high word (sign, exponent
 // rebias, the top 20 mantissa bits; no conversion on the FP64 pipe): within
 // 2^-20 of x relative, 0 below the FP32 normal range (|x| < 2^-126), NaN above

@@ -1997,42 +1997,37 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
     }
     if (!__shfl_sync(0xffffffffu, last, 0)) continue;
     __syncwarp();  // the other lanes' loads below after lane 0's acquire
-    // last part: finish evaluation e of the row
-    d3 acc = {0.0, 0.0, 0.0};
-    for (int r = 0; r < P; r++) {
-      acc.x += __ldcg(qs + 3 * r);
-      acc.y += __ldcg(qs + 3 * r + 1);
-      acc.z += __ldcg(qs + 3 * r + 2);
-    }
-    m.finish_eval(D.u, acc, soft2);
-    if (m.done < N) {
-      if (lane == 0) {
-        st[0] = m.z0.x;
-        st[1] = m.z0.y;
-        st[2] = m.z0.z;
-        st[3] = m.z1.x;
-        st[4] = m.z1.y;
-        st[5] = m.z1.z;
-        st[6] = m.vel.x;
-        st[7] = m.vel.y;
-        st[8] = m.vel.z;
-        st_release(cnt + 7 + row, e + 1);
+    // last part: finish evaluation e of the row (MidRow::finish_eval and
+    // result), one component per lane on lanes 0-2 (the other lanes repeat
+    // lane 0's and store nothing): the part sums in part order, the sun's
+    // pull at z1, the velocity and the next point, each component with the
+    // operations of the d3 form
+    const int c = lane < 3 ? lane : 0;
+    double a = 0.0;
+    for (int r = 0; r < P; r++) a += __ldcg(qs + 3 * r + c);
+    const double z0c = c == 0 ? m.z0.x : (c == 1 ? m.z0.y : m.z0.z);
+    const double z1c = c == 0 ? m.z1.x : (c == 1 ? m.z1.y : m.z1.z);
+    double vc = c == 0 ? m.vel.x : (c == 1 ? m.vel.y : m.vel.z);
+    vc = fma(sun_accel_c(D.u, m.z1, z1c, soft2), m.h, fma(a, m.h, vc));
+    if (e + 1 < N) {
+      if (lane < 3) {
+        st[c] = z1c;                      // z0 of the next evaluation
+        st[3 + c] = fma(m.h2, vc, z0c);   // z1, the next evaluation point
+        st[6 + c] = vc;
       }
+      __syncwarp();  // lanes 1-2's stores before lane 0's release
+      if (lane == 0) st_release(cnt + 7 + row, e + 1);
       continue;
     }
-    const PV mine = m.result();
     double* res = D.enc_res + 18 * (size_t)k;
-    int fin = 0;
-    if (lane == 0) {
+    if (lane < 3) {
       double* rs = res + 6 * row;
-      rs[0] = mine.pos.x;
-      rs[1] = mine.pos.y;
-      rs[2] = mine.pos.z;
-      rs[3] = mine.vel.x;
-      rs[4] = mine.vel.y;
-      rs[5] = mine.vel.z;
-      fin = atom_add_acq_rel(cnt + 10, 1) == 2;
+      rs[c] = 0.5 * (z1c + fma(vc, m.h, z0c));
+      rs[3 + c] = vc;
     }
+    __syncwarp();  // lanes 1-2's stores before lane 0's release
+    int fin = 0;
+    if (lane == 0) fin = atom_add_acq_rel(cnt + 10, 1) == 2;
     if (!__shfl_sync(0xffffffffu, fin, 0)) continue;
     __syncwarp();  // the other lanes' loads below after lane 0's acquire
     // The Richardson combination (rich_combine's arithmetic per component),
