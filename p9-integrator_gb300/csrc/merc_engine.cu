@@ -546,7 +546,7 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     auto far = [&](const double* rc_in, int set, const int* gate, int ev) {
       int st2;
       if (ev >= 0 && (st2 = kick_ev(ev))) return st2;
-      launch(k_sym<true>, (ctx->n_sym + kSymWarps - 1) / kSymWarps, 32 * kSymWarps, D, ctx->d_sym, ctx->n_sym, rc_in,
+      launch(k_sym<true>, ctx->n_sym, 32 * kSymSplit, D, ctx->d_sym, ctx->n_sym, rc_in,
              p.softening2, set, gate);
       nk++;
       return ev >= 0 ? kick_ev(ev + 1) : MERC_OK;

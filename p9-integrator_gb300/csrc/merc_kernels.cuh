@@ -1055,13 +1055,27 @@ __device__ __forceinline__ void rotate(RotSrc& r, d3& acc, uint32_t& bits) {
 #define MERC_SYM_WARPS 1
 #endif
 constexpr int kSymWarps = MERC_SYM_WARPS;  // block-pair tasks (warps) per block of k_sym
+// The far-field pass (KICK) splits each block-pair task over kSymSplit warps
+// of one block, each taking a contiguous share of the rotations; their sums
+// are added in warp order through shared memory (a fixed order).  The FP64
+// unit is per SM sub-partition, and with one warp per task the 2016 tasks of
+// a 2002-body system put three or four warps on a sub-partition (warp end
+// times 66-84 us within one pass); split in two, a sub-partition holds six or
+// seven half tasks.  Measured: about 1 us less per pass (0.2540 -> 0.2530 ms
+// per step), far less than the load difference suggests: the end times were
+// spread evenly rather than in two groups.
+constexpr int kSymSplit = 2;
 template <bool KICK>
-__global__ void __launch_bounds__(32 * kSymWarps) k_sym(Dev D, const SymTask* __restrict__ tasks, int ntasks,
-                                             const double* __restrict__ rc, double soft2, int set,
-                                             const int* __restrict__ gate) {
+__global__ void __launch_bounds__(32 * (KICK ? kSymSplit : kSymWarps))
+    k_sym(Dev D, const SymTask* __restrict__ tasks, int ntasks, const double* __restrict__ rc, double soft2,
+          int set, const int* __restrict__ gate) {
   griddep_enter();
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (warp >= ntasks) return;  // whole warps leave together
+  constexpr int SPLIT = KICK ? kSymSplit : 1;
+  // KICK: one task per block, warp `part` of SPLIT takes its share of the
+  // rotations; otherwise one task per warp
+  const int warp = KICK ? (int)blockIdx.x : (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int part = KICK ? (int)(threadIdx.x >> 5) : 0;
+  if (warp >= ntasks) return;  // whole blocks (KICK) or warps leave together
   if (KICK && gate && *gate == 0) return;
   const int lane = threadIdx.x & 31;
   if (KICK && gate && warp == 0 && lane == 0) atomicAdd(D.far_recomputes, 1ull);
@@ -1079,28 +1093,31 @@ __global__ void __launch_bounds__(32 * kSymWarps) k_sym(Dev D, const SymTask* __
   A.idx = i;
   A.f = (!KICK && iv) ? load_f4(D, b0 + i) : F4{0.f, 0.f, 0.f, 0.f};
   A.rcf = (!KICK && iv) ? f32_trunc(rc[4 * (size_t)(b0 + i)]) : 0.f;
+  // rotation steps of the task (step k pairs lane t with source lane t + k of
+  // block J; the diagonal task takes k = 1..16, lanes 0-15 only at k = 16),
+  // and this warp's share of them
+  const bool diag = T.I == T.J;
+  const int kbeg = diag ? 1 : 0, kend = diag ? 16 : 31;
+  const int span_k = kend - kbeg + 1;
+  const int k0 = kbeg + (part * span_k) / SPLIT, k1 = kbeg + ((part + 1) * span_k) / SPLIT - 1;
+  // the source rotated to step k0 from the start: lane t holds source t + k0
+  const int jb = 32 * T.J + ((lane + k0) & 31);
   const int j0 = 32 * T.J + lane;
-  const bool jv0 = j0 < nm;
-  B.x = (KICK && jv0) ? D.x[b0 + j0] : 0.0;
-  B.y = (KICK && jv0) ? D.x[D.n + b0 + j0] : 0.0;
-  B.z = (KICK && jv0) ? D.x[2 * D.n + b0 + j0] : 0.0;
-  B.m = (KICK && jv0) ? D.m[b0 + j0] : 0.0;
-  B.thr = (KICK && jv0) ? far_thr[b0 + j0] : 0x7fffffff;
-  B.idx = jv0 ? j0 : -1;
-  B.f = (!KICK && jv0) ? load_f4(D, b0 + j0) : F4{0.f, 0.f, 0.f, 0.f};
-  B.rcf = (!KICK && jv0) ? f32_trunc(rc[4 * (size_t)(b0 + j0)]) : 0.f;
+  const bool jv0 = j0 < nm, jvb = jb < nm;
+  B.x = (KICK && jvb) ? D.x[b0 + jb] : 0.0;
+  B.y = (KICK && jvb) ? D.x[D.n + b0 + jb] : 0.0;
+  B.z = (KICK && jvb) ? D.x[2 * D.n + b0 + jb] : 0.0;
+  B.m = (KICK && jvb) ? D.m[b0 + jb] : 0.0;
+  B.thr = (KICK && jvb) ? far_thr[b0 + jb] : 0x7fffffff;
+  B.idx = jvb ? jb : -1;
+  B.f = (!KICK && jvb) ? load_f4(D, b0 + jb) : F4{0.f, 0.f, 0.f, 0.f};
+  B.rcf = (!KICK && jvb) ? f32_trunc(rc[4 * (size_t)(b0 + jb)]) : 0.f;
   d3 accA = {0.0, 0.0, 0.0}, accB = {0.0, 0.0, 0.0};
   // KICK: near-pair bits (bit q: source 32 J + q for A, 32 I + q for B);
   // !KICK: encounter flags
   uint32_t bitsA = 0u, bitsB = 0u;
-  const bool diag = T.I == T.J;
-  const int kbeg = diag ? 1 : 0, kend = diag ? 16 : 31;
-  int rotations = 0;
-  if (diag) {
-    rotate<KICK>(B, accB, bitsB);
-    rotations++;
-  }
-  for (int k = kbeg; k <= kend; k++) {
+  int rotations = k0;
+  for (int k = k0; k <= k1; k++) {
     const bool act = iv && B.idx >= 0 && !(diag && k == 16 && lane >= 16);
     if (act) {
       if (!KICK) {
@@ -1148,6 +1165,35 @@ __global__ void __launch_bounds__(32 * kSymWarps) k_sym(Dev D, const SymTask* __
       accB.z = __shfl_sync(0xffffffffu, accB.z, src);
     }
     bitsB = __shfl_sync(0xffffffffu, bitsB, src);
+  }
+  if (KICK && SPLIT > 1) {
+    // the warps' shares added in warp order, by warp 0
+    __shared__ double xs[KICK ? kSymSplit - 1 : 1][6][32];
+    __shared__ uint32_t xb[KICK ? kSymSplit - 1 : 1][2][32];
+    if (part > 0) {
+      double* p = &xs[part - 1][0][0];
+      p[lane] = accA.x;
+      p[32 + lane] = accA.y;
+      p[64 + lane] = accA.z;
+      p[96 + lane] = accB.x;
+      p[128 + lane] = accB.y;
+      p[160 + lane] = accB.z;
+      xb[part - 1][0][lane] = bitsA;
+      xb[part - 1][1][lane] = bitsB;
+    }
+    __syncthreads();
+    if (part > 0) return;
+    for (int w = 0; w < SPLIT - 1; w++) {
+      const double* p = &xs[w][0][0];
+      accA.x += p[lane];
+      accA.y += p[32 + lane];
+      accA.z += p[64 + lane];
+      accB.x += p[96 + lane];
+      accB.y += p[128 + lane];
+      accB.z += p[160 + lane];
+      bitsA |= xb[w][0][lane];
+      bitsB |= xb[w][1][lane];
+    }
   }
   if (KICK) {
     const size_t stride = 3 * (size_t)nm;
