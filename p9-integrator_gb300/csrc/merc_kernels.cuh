@@ -140,6 +140,41 @@ __device__ __forceinline__ int write_rc(double* rc, int n, int j, const d3& x, c
   return far;
 }
 
+// write_rc for the universal-drift path, where the kernels are checked
+// against the CPU check to 1e-12 rather than bit for bit: the reference's
+// r_crit formula (rcrit_hc) with 1 / |x| from the FP32-seeded reciprocal
+// square root, |x| = |x|^2 (1 / |x|), and the division by 1 - e^2 as a
+// multiplication by the seeded reciprocal (each within about an ulp of the
+// IEEE operation; outside the seed range, or for 1 - e^2 <= 0, the IEEE
+// forms).  The square root and the two divisions of write_rc were the
+// longest part of the solar jump (3.9 of its 8 us, %globaltimer stamps per
+// phase).
+__device__ __forceinline__ int write_rc_fast(const FU& U, double* rc, int n, int j, const d3& x, const d3& v,
+                                             double hc) {
+  const d3 h = {fma(x.y, v.z, -x.z * v.y), fma(x.z, v.x, -x.x * v.z), fma(x.x, v.y, -x.y * v.x)};
+  const double h2 = mag2(h);
+  const double xx = mag2(x);
+  const double ir = rsqrt_fast(U, xx);
+  const double v2 = mag2(v);
+  const double rdv = fma(x.x, v.x, fma(x.y, v.y, x.z * v.z));
+  const double factor = v2 - ir;
+  const d3 ev = {fma(factor, x.x, -rdv * v.x), fma(factor, x.y, -rdv * v.y), fma(factor, x.z, -rdv * v.z)};
+  const double q = 1.0 - mag2(ev);
+  const double a = q > 0.0 ? h2 * rcp_fast(q) : h2 / q;
+  const double r = a * hc;
+  rc[4 * (size_t)j] = r;
+  rc[4 * (size_t)j + 1] = 0.1 * r;
+  rc[4 * (size_t)j + 2] = 0.9 * r;
+  rc[4 * (size_t)j + 3] = thr_pack(rc2_threshold(r));
+  int far = 0x7fffffff;
+  if (r > 0.0 && r < 1e150) {
+    const double R = kFarRadius * hc * (xx * ir);
+    far = rc2_threshold(R > r ? R : r);
+  }
+  rc_far_thr(rc, n)[j] = far;
+  return far;
+}
+
 __device__ __forceinline__ F4 load_f4(const Dev& D, int g) {
   return f4_of(__ldg(D.xf + g), __ldg(D.xf + D.n + g), __ldg(D.xf + 2 * D.n + g));
 }
@@ -533,7 +568,12 @@ __global__ void __launch_bounds__(kJumpThreads) k_jump(Dev D, const double* __re
   } else {
     v = load3(D.v, n, j);
   }
-  if (j - D.off[s] < D.nm[s]) write_rc(rc_out, n, j, x, v, D.hc[j]);
+  if (j - D.off[s] < D.nm[s]) {
+    if (BIG_P)  // big systems, universal drift only
+      write_rc_fast(D.u, rc_out, n, j, x, v, D.hc[j]);
+    else
+      write_rc(rc_out, n, j, x, v, D.hc[j]);
+  }
 }
 
 // Solar jump of a single big system (system 0 holds every body) by clusters
@@ -643,7 +683,7 @@ __global__ void __cluster_dims__(kJumpCluster, 1, 1) __launch_bounds__(kJumpThre
     D.xf[n + j] = f32_trunc(x.y);
     D.xf[2 * n + j] = f32_trunc(x.z);
     if (vsrc) store3(D.v, n, j, v);
-    if (j < nm) write_rc(rc_out, n, j, x, v, hc_j);
+    if (j < nm) write_rc_fast(D.u, rc_out, n, j, x, v, hc_j);
   }
   cl.barrier_wait(std::move(reads_done));
 }
@@ -1418,7 +1458,7 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   // kick_epilogue with the prefetched inputs
   store3(D.v, n, j, vel);
   if (rc_out && massive) {
-    const int far = write_rc(rc_out, n, j, pos, vel, hc_j);
+    const int far = write_rc_fast(D.u, rc_out, n, j, pos, vel, hc_j);
     if (check && far != thr_j) atomicOr(D.gate, 1);
   }
   if (last) {
