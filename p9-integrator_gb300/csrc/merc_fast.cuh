@@ -66,19 +66,39 @@ __device__ __forceinline__ bool seed_in_range(double r2) {
   return h > 0x3DB00000 && h < 0x42600000;
 }
 
-// Exact pair of the reference (sim.cuh:344-374): weight K or the encounter
-// weighting, self exclusion, softening except for "self".
+// The reference's pair formula (sim.cuh:344-374): weight K or the encounter
+// weighting, self exclusion, softening except for "self" -- for the
+// universal-drift kernels, with the square root and the three divisions
+// (r, the changeover argument y, K, and m / ((r^2 + eps^2) r)) by the
+// FP32-seeded reciprocal square root and reciprocal, each within about an ulp
+// of the IEEE operation (seed_range_ok; outside it, and for r^2 = 0, the IEEE
+// forms).  On this GPU an FP64 square root or division costs about 8.5
+// FP64-pipe slots, the seeded reciprocal 4.5 and reciprocal square root 5.8;
+// the pair is on the chains of the kick reduce and inside the encounter
+// sub-step's part sums.  The element drift keeps exact_term's IEEE form.
+__device__ __forceinline__ double div_seeded(double x, double y) {
+  return seed_range_ok(y) ? x * rcp_fast(y) : x / y;
+}
+__device__ __forceinline__ double changeover_K_seeded(double y) {
+  if (y > 1.0 && y < 1.7976931348623157e308) return 1.0;
+  if (y < 0.0 && y > -1.7976931348623157e308) return 0.0;
+  double K = div_seeded(y * y, 2.0 * y * y - 2.0 * y + 1.0);
+  double gtz = (double)(y > 0.0), gto = (double)(y > 1.0), valid = (double)(y <= 1.0 && y >= 0.0);
+  return K * gtz * valid + gto;
+}
 template <bool BS>
 __device__ __forceinline__ void pair_exact(const d3& pos, int self, int i, const FastSrc& S, double soft2, d3& acc) {
+  const FU U1 = {1.0, -0.0};
   d3 d = {S.x - pos.x, S.y - pos.y, S.z - pos.z};
   double r_sq = mag2(d);
-  double r = stable_sqrt(r_sq);
+  double r = seed_range_ok(r_sq) ? r_sq * rsqrt_fast(U1, r_sq) : stable_sqrt(r_sq);
   double notself = (double)(self != i);
-  double K = changeover_K((notself * r - S.rc01) / S.rc09);
+  double K = changeover_K_seeded(div_seeded(notself * r - S.rc01, S.rc09));
   double w = K;
   if (BS) w = (double)(r <= S.rc) * (1.0 - K) + (double)(r > S.rc) * K;
   r_sq += notself * soft2;
-  double wa = w * stable_div(S.m, r_sq * r);
+  const double den = r_sq * r;
+  double wa = w * (den != 0.0 ? div_seeded(S.m, den) : stable_div(S.m, den));
   acc.x = fma(wa, d.x, acc.x);
   acc.y = fma(wa, d.y, acc.y);
   acc.z = fma(wa, d.z, acc.z);
