@@ -2069,7 +2069,7 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
       m.vel = {__ldcg(st + 6), __ldcg(st + 7), __ldcg(st + 8)};
     }
     // part q: whole groups of 32 sources (only the system's last group is
-    // partial), so no lane idles in a part's last round but the last part's
+    // partial), so no lane idles in a part's last iteration but the last part's
     const int G = (nm + 31) / 32;
     const int c0 = 32 * (int)((int64_t)q * G / P), c1 = min(32 * (int)((int64_t)(q + 1) * G / P), nm);
     const d3 S = warp_source_sum(D, rc_in, b0, c0, c1, self, m.z1, soft2);
