@@ -624,7 +624,7 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     nk++;
     if (ctx->has_big) {
       if (use_sym) {
-        launch(k_sym<false>, (ctx->n_sym + kSymWarps - 1) / kSymWarps, 32 * kSymWarps, D, ctx->d_sym, ctx->n_sym,
+        launch(k_sym<false>, ctx->n_sym, 32 * kSymSplit, D, ctx->d_sym, ctx->n_sym,
                rcB, p.softening2, 0, nullptr);
         nk++;
         if (ctx->n_work_tp) {

@@ -1091,13 +1091,10 @@ __device__ __forceinline__ void rotate(RotSrc& r, d3& acc, uint32_t& bits) {
 // KICK: far-field sums and near-pair masks into partial set `set` (thresholds
 // from rc's far-field table); with `gate`, only when *gate is set.
 // !KICK: encounter test flags (rc's fast thresholds).
-#ifndef MERC_SYM_WARPS
-#define MERC_SYM_WARPS 1
-#endif
-constexpr int kSymWarps = MERC_SYM_WARPS;  // block-pair tasks (warps) per block of k_sym
-// The far-field pass (KICK) splits each block-pair task over kSymSplit warps
-// of one block, each taking a contiguous share of the rotations; their sums
-// are added in warp order through shared memory (a fixed order).  The FP64
+// Each block-pair task runs on kSymSplit warps of one block, each taking a
+// contiguous share of the rotations; the far-field pass (KICK) adds their
+// sums in warp order through shared memory (a fixed order), the encounter
+// test ORs their flags.  The FP64
 // unit is per SM sub-partition, and with one warp per task the 2016 tasks of
 // a 2002-body system put three or four warps on a sub-partition (warp end
 // times 66-84 us within one pass); split in two, a sub-partition holds six or
@@ -1106,16 +1103,16 @@ constexpr int kSymWarps = MERC_SYM_WARPS;  // block-pair tasks (warps) per block
 // spread evenly rather than in two groups.
 constexpr int kSymSplit = 2;
 template <bool KICK>
-__global__ void __launch_bounds__(32 * (KICK ? kSymSplit : kSymWarps))
+__global__ void __launch_bounds__(32 * kSymSplit)
     k_sym(Dev D, const SymTask* __restrict__ tasks, int ntasks, const double* __restrict__ rc, double soft2,
           int set, const int* __restrict__ gate) {
   griddep_enter();
-  constexpr int SPLIT = KICK ? kSymSplit : 1;
+  constexpr int SPLIT = kSymSplit;
   // KICK: one task per block, warp `part` of SPLIT takes its share of the
   // rotations; otherwise one task per warp
-  const int warp = KICK ? (int)blockIdx.x : (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int part = KICK ? (int)(threadIdx.x >> 5) : 0;
-  if (warp >= ntasks) return;  // whole blocks (KICK) or warps leave together
+  const int warp = (int)blockIdx.x;
+  const int part = (int)(threadIdx.x >> 5);
+  if (warp >= ntasks) return;  // whole blocks leave together
   if (KICK && gate && *gate == 0) return;
   const int lane = threadIdx.x & 31;
   if (KICK && gate && warp == 0 && lane == 0) atomicAdd(D.far_recomputes, 1ull);
@@ -1206,31 +1203,36 @@ __global__ void __launch_bounds__(32 * (KICK ? kSymSplit : kSymWarps))
     }
     bitsB = __shfl_sync(0xffffffffu, bitsB, src);
   }
-  if (KICK && SPLIT > 1) {
-    // the warps' shares added in warp order, by warp 0
-    __shared__ double xs[KICK ? kSymSplit - 1 : 1][6][32];
-    __shared__ uint32_t xb[KICK ? kSymSplit - 1 : 1][2][32];
+  if (SPLIT > 1) {
+    // the warps' shares added in warp order (KICK) and their flags or
+    // near-pair bits OR-ed, by warp 0
+    __shared__ double xs[KICK ? kSymSplit - 1 : 1][KICK ? 6 : 1][32];
+    __shared__ uint32_t xb[kSymSplit - 1][2][32];
     if (part > 0) {
-      double* p = &xs[part - 1][0][0];
-      p[lane] = accA.x;
-      p[32 + lane] = accA.y;
-      p[64 + lane] = accA.z;
-      p[96 + lane] = accB.x;
-      p[128 + lane] = accB.y;
-      p[160 + lane] = accB.z;
+      if (KICK) {
+        double* p = &xs[part - 1][0][0];
+        p[lane] = accA.x;
+        p[32 + lane] = accA.y;
+        p[64 + lane] = accA.z;
+        p[96 + lane] = accB.x;
+        p[128 + lane] = accB.y;
+        p[160 + lane] = accB.z;
+      }
       xb[part - 1][0][lane] = bitsA;
       xb[part - 1][1][lane] = bitsB;
     }
     __syncthreads();
     if (part > 0) return;
     for (int w = 0; w < SPLIT - 1; w++) {
-      const double* p = &xs[w][0][0];
-      accA.x += p[lane];
-      accA.y += p[32 + lane];
-      accA.z += p[64 + lane];
-      accB.x += p[96 + lane];
-      accB.y += p[128 + lane];
-      accB.z += p[160 + lane];
+      if (KICK) {
+        const double* p = &xs[w][0][0];
+        accA.x += p[lane];
+        accA.y += p[32 + lane];
+        accA.z += p[64 + lane];
+        accB.x += p[96 + lane];
+        accB.y += p[128 + lane];
+        accB.z += p[160 + lane];
+      }
       bitsA |= xb[w][0][lane];
       bitsB |= xb[w][1][lane];
     }
