@@ -475,9 +475,12 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     const int bx = ctx->has_big ? 1 : 0;
     const unsigned nbx =
         (unsigned)std::min<int64_t>((D.n + kExactWarps - 1) / kExactWarps, (int64_t)ctx->sms * 16);
+    // without small systems the small-system kernels have nothing to do
+    const bool small = ctx->has_small || !bx;
     auto kick_exact_all = [&](const double* rc_in, double* rc_out, int last) {
-      k_kick<<<nb, kThreads, 0, s>>>(D, rc_in, rc_out, hdt, p.softening2, p.compat_block, p.hill_factor, ej2, last,
-                                     bx);
+      if (small)
+        k_kick<<<nb, kThreads, 0, s>>>(D, rc_in, rc_out, hdt, p.softening2, p.compat_block, p.hill_factor, ej2,
+                                       last, bx);
       if (bx)
         k_kick_big_exact_pipe<<<(unsigned)std::max(1, ctx->n_exact_groups), 32 * (1 + kPipeTermWarps), 0, s>>>(
             D, ctx->d_exact_groups, ctx->n_exact_groups, rc_in, rc_out, hdt, p.softening2, p.compat_block,
@@ -487,7 +490,7 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     kick_exact_all(rcA, nullptr, 0);
     if ((st = kick_ev(1))) return st;
     auto momentum_exact = [&](const double* vsrc) {
-      k_momentum<<<sb, kThreads, 0, s>>>(D, vsrc, bx);
+      if (small) k_momentum<<<sb, kThreads, 0, s>>>(D, vsrc, bx);
       if (bx)
         k_momentum_big_exact<<<(unsigned)((D.nsys + kExactWarps - 1) / kExactWarps), 32 * kExactWarps, 0, s>>>(
             D, vsrc);
@@ -496,12 +499,21 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt);
     CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
     if (bx) k_ce_big_exact<<<nbx, 32 * kExactWarps, 0, s>>>(D, rcB, p.compat_block);
-    k_drift_elements<<<nb, kThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.kepler_iters, bx);
-    k_encounter_elements<<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2,
-                                                         bx);
-    if (bx)
-      k_encounter_big_pipe<<<ctx->sms, 32 + kExactRowThreads * p.bs_rows, 0, s>>>(D, rcB, p.dt, p.compat_block,
-                                                                                 p.bs_rows, p.softening2);
+    // big systems only: the encounter sub-step runs beside the drift (the
+    // drift lets it launch at once and it waits for the drift before its
+    // stores; the bodies they integrate are disjoint, the stores blend the
+    // drift's result as the reference does)
+    const bool beside = bx && !small && ctx->pdl;
+    k_drift_elements<<<nb, kThreads, 0, s>>>(D, rcB, p.dt, p.compat_block, p.kepler_iters, bx, beside ? 1 : 0);
+    if (small)
+      k_encounter_elements<<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2,
+                                                           bx);
+    if (bx) {
+      cudaError_t le = step_launch(beside, s, k_encounter_big_pipe, dim3((unsigned)ctx->sms),
+                                   dim3((unsigned)(32 + kExactRowThreads * p.bs_rows)), D, (const double*)rcB,
+                                   p.dt, p.compat_block, p.bs_rows, p.softening2, beside ? 1 : 0);
+      if (le != cudaSuccess) return fail(ctx, MERC_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(le));
+    }
     if (ctx->collide_on) {
       k_collide_find<<<ctx->sms * 4, 256, 0, s>>>(D, ctx->col);
       k_collide_resolve<<<1, 32, 0, s>>>(D, ctx->col, p.hill_factor);
@@ -512,7 +524,7 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     if ((st = kick_ev(2))) return st;
     kick_exact_all(rcB, rcA, 1);
     if ((st = kick_ev(3))) return st;
-    nk += 8 + 6 * bx;
+    nk += 3 + (small ? 5 : 0) + 6 * bx;  // jumps and drift; small-system kick, momentum, encounter; big systems
   } else {
     // programmatic dependent launches: a kernel may be scheduled while its
     // predecessor finishes; every kernel here waits for it (griddep_wait)

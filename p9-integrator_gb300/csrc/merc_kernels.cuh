@@ -382,7 +382,13 @@ __global__ void __launch_bounds__(32 * kExactWarps) k_ce_big_exact(Dev D, const 
     for (int i = lane; i < nm; i += 32)
       if (ce_maybe(pf, load_f4(D, b0 + i), f32_trunc(S.rc[4 * (size_t)i]))) ce = ce || ce_pair(pos, self, S, i);
     ce = __any_sync(0xffffffffu, ce);
-    if (lane == 0) D.ce[j] = ce;
+    if (lane == 0) {
+      D.ce[j] = ce;
+      if (ce) {  // the encounter list of the element path (k_drift_elements lists the small systems')
+        D.ce_list[atomicAdd(&D.ce_count[0], 1)] = j;
+        atomicAdd(&D.counters[0], 1ull);
+      }
+    }
   }
 }
 
@@ -715,21 +721,27 @@ __device__ __forceinline__ void append_ce(bool flag, int j, int* list, int* coun
 // (sim.cuh:692-713).  Bodies in encounter are appended to the encounter list;
 // every body writes its Kepler result to xo/vo (for encounter bodies it enters
 // the blend fma(0, kep, bs) of sim.cuh:718-730, completed by k_encounter).
-// ce_big: the flags of big systems' bodies were set by k_ce_big_exact.
+// ce_big: the flags of big systems' bodies were set, and those bodies listed,
+// by k_ce_big_exact (the encounter sub-step of the big systems may then run
+// beside this kernel).
 __global__ void k_drift_elements(Dev D, const double* __restrict__ rc_in, double dt, int compat_block,
-                                 int kep_iters, int ce_big) {
+                                 int kep_iters, int ce_big, int trigger) {
+  // trigger: the big systems' encounter sub-step that follows runs beside
+  // this kernel (it waits for it before its stores)
+  if (trigger) griddep_launch();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
-  bool is_ce = false;
+  bool is_ce = false, listed = false;
   if (j < D.n) {
     const int n = D.n, s = D.sys[j], b0 = D.off[s], nm = D.nm[s];
     const int self = self_index(j - b0, compat_block);
     SrcView S = src_view(D, rc_in, b0);
     d3 pos = load3(D.x, n, j), vel = load3(D.v, n, j);
     if (ce_big && D.big[s]) {
-      is_ce = D.ce[j] != 0;
+      is_ce = D.ce[j] != 0;  // flagged and listed by k_ce_big_exact
     } else {
       is_ce = close_encounter(pos, self, S, nm);
       D.ce[j] = is_ce;
+      listed = is_ce;
     }
     const double tp = 6.283185307179586476925286766559005768394338798750211641949;
     double a = D.alag[j];
@@ -741,7 +753,7 @@ __global__ void k_drift_elements(Dev D, const double* __restrict__ rc_in, double
     store3(D.xo, n, j, kep.pos);
     store3(D.vo, n, j, kep.vel);
   }
-  append_ce(is_ce, j, D.ce_list, &D.ce_count[0], &D.counters[0]);
+  append_ce(listed, j, D.ce_list, &D.ce_count[0], &D.counters[0]);
 }
 
 // Encounter sub-step (Richardson extrapolation of modified-midpoint steps
@@ -789,7 +801,12 @@ constexpr int kExactRowThreads = 128;
 // 32 + kExactRowThreads x rows threads.
 __global__ void __launch_bounds__(32 + 4 * kExactRowThreads)
     k_encounter_big_pipe(Dev D, const double* __restrict__ rc_in, double dt, int compat_block, int rows,
-                         double soft2) {
+                         double soft2, int late_wait) {
+  // late_wait: launched beside the element drift (the kernel before it,
+  // started after the encounter test completed); the drift writes every
+  // body's Kepler result, which encounter_elements_store reads and blends,
+  // so each block waits for the drift before its first store and before it
+  // leaves (this kernel's completion then implies the drift's)
   constexpr int NT = kExactRowThreads;
   __shared__ double stage[2][4][4][NT];
   __shared__ double accs[4][3];
@@ -867,9 +884,13 @@ __global__ void __launch_bounds__(32 + 4 * kExactRowThreads)
       }
       __syncthreads();  // accs is rewritten next round
     }
-    if (threadIdx.x == 0) encounter_elements_store(D, j, richardson_of_rows(res, rows));
+    if (threadIdx.x == 0) {
+      if (late_wait) griddep_wait();
+      encounter_elements_store(D, j, richardson_of_rows(res, rows));
+    }
     __syncthreads();  // res is rewritten for the next body
   }
+  if (late_wait && threadIdx.x == 0) griddep_wait();
 }
 
 // ---------------------------------------------------------------------------
