@@ -509,7 +509,7 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
       k_encounter_elements<<<ctx->enc_blocks, 64, 0, s>>>(D, rcB, p.dt, p.compat_block, p.bs_rows, p.softening2,
                                                            bx);
     if (bx) {
-      cudaError_t le = step_launch(beside, s, k_encounter_big_pipe, dim3((unsigned)ctx->sms),
+      cudaError_t le = step_launch(beside, s, k_encounter_big_pipe, dim3((unsigned)(kExactEncBlocksPerSM * ctx->sms)),
                                    dim3((unsigned)(32 + kExactRowThreads * p.bs_rows)), D, (const double*)rcB,
                                    p.dt, p.compat_block, p.bs_rows, p.softening2, beside ? 1 : 0);
       if (le != cudaSuccess) return fail(ctx, MERC_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(le));

@@ -782,14 +782,22 @@ __global__ void k_encounter_elements(Dev D, const double* __restrict__ rc_in, do
   }
 }
 // The big systems' listed bodies: one group of kExactRowThreads threads per
-// Richardson row computes the terms of its row's evaluations.
-constexpr int kExactRowThreads = 128;
+// Richardson row computes the terms of its row's evaluations, and the grid
+// has kExactEncBlocksPerSM blocks per SM.  Measured on the 2002-body disk
+// (element path, ms per step at ~150 / ~188 encounter bodies): 128 threads,
+// one block per SM 1.640 / 1.833 (more encounter bodies than SMs take a
+// second round); 64 threads, two blocks per SM 1.509 / 1.513 (three: the
+// same); 96 threads, two 1.558 / 1.561; 32 threads, two or four 1.523 /
+// 1.525.  The sums are the same chains in the same order: same bits.
+constexpr int kExactRowThreads = 64;
+constexpr int kExactEncBlocksPerSM = 2;
 
 // The encounter sub-step of the big systems' listed bodies, the rows side by
 // side in lock step with one warp for all their fma chains: one block per
 // encounter body, warp 0 runs the 3 x rows chains (lane
-// 3r + c: row r, component c) while the rows' 128-thread groups compute the
-// next 128 sources' terms (exact_term with the encounter weighting),
+// 3r + c: row r, component c) while the rows' kExactRowThreads-thread groups
+// compute the next kExactRowThreads sources' terms (exact_term with the
+// encounter weighting),
 // double-buffered in shared memory.  Round k evaluates the velocity update
 // of every row whose modified midpoint has more than k sub-steps (row r has
 // 2^r), at the row's position of that sub-step; between rounds each group
