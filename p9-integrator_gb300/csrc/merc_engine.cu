@@ -496,9 +496,23 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
             D, vsrc);
     };
     momentum_exact(D.v);
-    k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt);
+    // the symmetric encounter test of the big systems (each unordered pair
+    // once, the same exact decisions as k_ce_big_exact: 34 -> ~8 us on the
+    // 2002-body disk) sets flags only, so this jump clears them first; with
+    // the reference's local-index self test (compat_block), or with test
+    // particles in big systems (the symmetric test covers massive pairs), the
+    // warp-per-body test stays
+    const bool sym_ce =
+        bx && ctx->n_work_tp == 0 && (p.compat_block == 0 || p.compat_block >= ctx->max_big_nm);
+    if (sym_ce)
+      k_jump<false, true><<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt);
+    else
+      k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt);
     CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
-    if (bx) k_ce_big_exact<<<nbx, 32 * kExactWarps, 0, s>>>(D, rcB, p.compat_block);
+    if (sym_ce)
+      k_sym<false><<<ctx->n_sym, 32 * kSymSplit, 0, s>>>(D, ctx->d_sym, ctx->n_sym, rcB, p.softening2, 1, nullptr);
+    else if (bx)
+      k_ce_big_exact<<<nbx, 32 * kExactWarps, 0, s>>>(D, rcB, p.compat_block);
     // big systems only: the encounter sub-step runs beside the drift (the
     // drift lets it launch at once and it waits for the drift before its
     // stores; the bodies they integrate are disjoint, the stores blend the

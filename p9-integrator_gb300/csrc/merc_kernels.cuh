@@ -1119,7 +1119,9 @@ __device__ __forceinline__ void rotate(RotSrc& r, d3& acc, uint32_t& bits) {
 
 // KICK: far-field sums and near-pair masks into partial set `set` (thresholds
 // from rc's far-field table); with `gate`, only when *gate is set.
-// !KICK: encounter test flags (rc's fast thresholds).
+// !KICK: encounter test flags (rc's fast thresholds; the flags must be clear
+// before the launch), the flagged bodies appended to the big-system list
+// (set 0) or to the element path's list (set 1).
 // Each block-pair task runs on kSymSplit warps of one block, each taking a
 // contiguous share of the rotations; the far-field pass (KICK) adds their
 // sums in warp order through shared memory (a fixed order), the encounter
@@ -1298,8 +1300,12 @@ __global__ void __launch_bounds__(32 * kSymSplit)
     // flags and the big-system encounter list (each body once)
     const bool fa = iv && bitsA && mark_ce(D.ce, b0 + i);
     const bool fb = jv0 && bitsB && mark_ce(D.ce, b0 + j0);
-    append_ce(fa, b0 + i, D.ce_list_big, &D.ce_count[1], &D.counters[0]);
-    append_ce(fb, b0 + j0, D.ce_list_big, &D.ce_count[1], &D.counters[0]);
+    // set 1: the element path's list (k_drift_elements lists the small
+    // systems' encounter bodies beside these)
+    int* list = set ? D.ce_list : D.ce_list_big;
+    int* cnt = set ? &D.ce_count[0] : &D.ce_count[1];
+    append_ce(fa, b0 + i, list, cnt, &D.counters[0]);
+    append_ce(fb, b0 + j0, list, cnt, &D.counters[0]);
   }
 }
 
