@@ -1309,15 +1309,34 @@ __global__ void __launch_bounds__(32 * kSymSplit)
   }
 }
 
-#ifndef MERC_RED_THREADS
-#define MERC_RED_THREADS 16
-#endif
-constexpr int kRedThreads = MERC_RED_THREADS;  // threads per body of k_kick_reduce_sym (a power of two <= 32)
-#ifndef MERC_RED_BATCH
-#define MERC_RED_BATCH 4
-#endif
-constexpr int kRedBatch = MERC_RED_BATCH;  // partials loaded per thread before they are added
-constexpr int kNearList = 32;             // near pairs per body dealt out over its threads
+constexpr int kRedThreads = 16;  // threads per body of k_kick_reduce_sym
+constexpr int kRedBodies = kThreads / kRedThreads;  // bodies per block
+constexpr int kRedBatch = 4;     // partials loaded per thread before they are added
+constexpr int kNearList = 32;    // near pairs per body dealt out over its threads
+static_assert(kRedBodies <= 32 && kThreads % 32 == 0, "one lane per body in the epilogue warp");
+
+// Totals of six values over the 16 threads of a body (lanes 16h .. 16h + 15
+// of a warp) by a reduce-scatter: at each level half of the values go to the
+// partner lane, so 4 + 2 + 1 + 1 FP64 additions instead of 6 x 4 for
+// butterflies (the FP64 unit of a sub-partition takes a warp instruction at
+// the same cost however few of its lanes need the result).  Thread sub ends
+// with the total of value 4 bit3 + 2 bit2 + bit1 of sub (6 and 7 are empty);
+// a fixed tree, so the result does not depend on scheduling.
+__device__ __forceinline__ double red_scatter6(const double (&v)[6], int sub) {
+  const unsigned full = 0xffffffffu;
+  const bool h8 = (sub & 8) != 0, h4 = (sub & 4) != 0, h2 = (sub & 2) != 0;
+  double k[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const double lo = v[i], hi = i < 2 ? v[4 + i] : 0.0;
+    k[i] = (h8 ? hi : lo) + __shfl_xor_sync(full, h8 ? lo : hi, 8);
+  }
+  double m[2];
+#pragma unroll
+  for (int i = 0; i < 2; i++) m[i] = (h4 ? k[2 + i] : k[i]) + __shfl_xor_sync(full, h4 ? k[i] : k[2 + i], 4);
+  double r = (h2 ? m[1] : m[0]) + __shfl_xor_sync(full, h2 ? m[0] : m[1], 2);
+  return r + __shfl_xor_sync(full, r, 1);
+}
 
 // Kick of every body of a big system whose sums are in partials: massive
 // bodies add their far-field block partials (symmetric kernel, set 1 when
@@ -1325,10 +1344,14 @@ constexpr int kNearList = 32;             // near pairs per body dealt out over 
 // rc = the kick's r_crit table); test particles add their chunk partials (when
 // there is more than one chunk; a single chunk was applied by the tiled
 // kernel).  kRedThreads threads per body each take every kRedThreads-th
-// block; their sums are combined by a fixed butterfly, so the result does not
-// depend on scheduling.  check: after writing rc_out, set *D.gate if a massive body's
-// far-field threshold in rc_out differs from the one in rc (the far field of
-// the next kick must then be recomputed).
+// block; their sums are combined by red_scatter6, so the result does not
+// depend on scheduling.  The epilogue (velocity, r_crit, flags) of the block's
+// kRedBodies bodies runs on one warp, one body per lane, with the totals
+// handed over in shared memory: on the body's own lead thread it took each
+// warp the FP64 instructions of two bodies' epilogues on two lanes.  check:
+// after writing rc_out, set *D.gate if a massive body's far-field threshold in
+// rc_out differs from the one in rc (the far field of the next kick must then
+// be recomputed).
 template <bool ONE>
 __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const int* __restrict__ gate,
                                   double* __restrict__ rc_out, double hdt, double soft2, double hill,
@@ -1336,62 +1359,89 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   griddep_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = t / kRedThreads, sub = t % kRedThreads;
-  const bool valid = j < D.n;
   const int n = D.n;
-  // ONE: a single system, big (no per-body system lookups)
-  const int s = ONE ? 0 : (valid ? D.sys[j] : 0);
-  bool work = valid && (ONE || D.big[s]);
-  const int b0 = (ONE || !work) ? 0 : D.off[s], nm = work ? D.nm[s] : 0, local = j - b0;
-  const bool massive = work && local < nm;
-  // the epilogue's inputs, loaded before the sums (they do not depend on them)
-  const bool lead = work && sub == 0;
-  const double hc_j = (lead && rc_out && massive) ? D.hc[j] : 0.0;
-  const uint32_t flags_j = (lead && last) ? D.flags[j] : 0u;
-  const bool ce_j = (lead && last) ? D.ce[j] != 0 : false;
-  const int thr_j = (lead && check && massive) ? rc_far_thr_c(rc, n)[j] : 0;
+  // which bodies have a kick here: massive bodies of big systems, and test
+  // particles of big systems with more than one chunk partial
+  struct Body {
+    int s, b0, nm, local;
+    bool work, massive;
+  };
+  auto classify = [&](int jj) {
+    Body B;
+    const bool valid = jj < n;
+    // ONE: a single system, big (no per-body system lookups)
+    B.s = ONE ? 0 : (valid ? D.sys[jj] : 0);
+    B.work = valid && (ONE || D.big[B.s]);
+    B.b0 = (ONE || !B.work) ? 0 : D.off[B.s];
+    B.nm = B.work ? D.nm[B.s] : 0;
+    B.local = jj - B.b0;
+    B.massive = B.work && B.local < B.nm;
+    if (B.work && !B.massive && !(D.nchunk[B.s] > 1 && !massive_only)) B.work = false;
+    return B;
+  };
+  // far_mode 1: keep the far-field sum of each massive body in D.far_acc;
+  // 2: take it from there when the gate is clear (the far field of the
+  // second kick of a merged pair is then the first's, the same partials in
+  // the same order)
+  const int set = (gate && *gate) ? 1 : 0;
+  const bool reuse_set = far_mode == 2 && set == 0;
+  // the epilogue warp (spread over the sub-partitions by the block index) and
+  // its lanes' bodies; their inputs are loaded before the sums, which they do
+  // not depend on
+  const int lane = (int)(threadIdx.x & 31);
+  const bool epi = (int)(threadIdx.x >> 5) == (int)(blockIdx.x & (kThreads / 32 - 1)) && lane < kRedBodies;
+  const int je = (int)blockIdx.x * kRedBodies + lane;
+  Body E = {0, 0, 0, 0, false, false};
+  d3 pos_e = {0.0, 0.0, 0.0}, vel_e = {0.0, 0.0, 0.0}, far_e = {0.0, 0.0, 0.0};
+  double hc_e = 0.0;
+  uint32_t flags_e = 0u;
+  bool ce_e = false;
+  int thr_e = 0;
+  if (epi) {
+    E = classify(je);
+    if (E.work) {
+      pos_e = load3(D.x, n, je);
+      vel_e = load3(D.v, n, je);
+      if (E.massive && reuse_set) far_e = load3(D.far_acc, n, je);
+      if (rc_out && E.massive) hc_e = D.hc[je];
+      if (last) {
+        flags_e = D.flags[je];
+        ce_e = D.ce[je] != 0;
+      }
+      if (check && E.massive) thr_e = rc_far_thr_c(rc, n)[je];
+    }
+  }
+  const Body B = classify(j);
+  const bool work = B.work, massive = B.massive;
+  const int s = B.s, b0 = B.b0, nm = B.nm, local = B.local;
   int count = 0;
   const double* base = nullptr;
   const uint32_t* mask = nullptr;
   size_t stride = 0;
   int index = 0;
-  // far_mode 1: keep the far-field sum of each massive body in D.far_acc;
-  // 2: take it from there when the gate is clear (the far field of the
-  // second kick of a merged pair is then the first's, the same partials in
-  // the same order)
-  bool reuse = false;
+  const bool reuse = massive && reuse_set;
   if (massive) {
-    const int set = (gate && *gate) ? 1 : 0;
-    reuse = far_mode == 2 && set == 0;
     count = (nm + 31) / 32;
     base = D.part_sym + (size_t)set * D.sym_set + D.sym_base[s];
     mask = D.near_mask + (size_t)set * (D.sym_set / 3) + D.sym_base[s] / 3;
     stride = 3 * (size_t)nm;
     index = local;
   } else if (work) {
-    if (D.nchunk[s] > 1 && !massive_only) {
-      count = D.nchunk[s];
-      base = D.part;
-      stride = 3 * (size_t)n;
-      index = j;
-    } else {
-      work = false;
-    }
+    count = D.nchunk[s];
+    base = D.part;
+    stride = 3 * (size_t)n;
+    index = j;
   }
   const size_t span = stride / 3;
   d3 acc = {0.0, 0.0, 0.0};
-  d3 pos = {0.0, 0.0, 0.0}, vel = {0.0, 0.0, 0.0};
-  if (work) {
-    pos = load3(D.x, n, j);
-    if (sub == 0) vel = load3(D.v, n, j);
-  }
+  d3 pos = {0.0, 0.0, 0.0};
+  if (work) pos = load3(D.x, n, j);
   // kRedBatch partials' loads in flight before they are added (same order of
   // additions as one at a time); the near-pair mask words with them
   uint32_t words[kRedBatch];
 #pragma unroll
   for (int u = 0; u < kRedBatch; u++) words[u] = 0u;
-  d3 far_j = {0.0, 0.0, 0.0};
   if (reuse) {
-    if (sub == 0) far_j = load3(D.far_acc, n, j);
 #pragma unroll
     for (int u = 0; u < kRedBatch; u++) {
       const int b = sub + u * kRedThreads;
@@ -1471,41 +1521,45 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
       }
     }
   }
-  for (int o = 1; o < kRedThreads; o <<= 1) {
-    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
-    acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
-    near.x += __shfl_xor_sync(0xffffffffu, near.x, o);
-    near.y += __shfl_xor_sync(0xffffffffu, near.y, o);
-    near.z += __shfl_xor_sync(0xffffffffu, near.z, o);
+  // the body's totals (far field x, y, z, near pairs x, y, z) to shared
+  // memory, one value per even thread of the body
+  __shared__ double tot[kRedBodies][6];
+  {
+    const double v6[6] = {acc.x, acc.y, acc.z, near.x, near.y, near.z};
+    const double tv = red_scatter6(v6, sub);
+    const int vi = 4 * ((sub >> 3) & 1) + 2 * ((sub >> 2) & 1) + ((sub >> 1) & 1);
+    if ((sub & 1) == 0 && vi < 6) tot[threadIdx.x / kRedThreads][vi] = tv;
   }
-  if (!work || sub != 0) return;
-  if (massive) {
-    if (reuse)
-      acc = far_j;
+  __syncthreads();
+  if (!epi || !E.work) return;
+  // kick_epilogue with the prefetched inputs, one body per lane
+  d3 a = {tot[lane][0], tot[lane][1], tot[lane][2]};
+  if (E.massive) {
+    if (reuse_set)
+      a = far_e;
     else if (far_mode == 1)
-      store3(D.far_acc, n, j, acc);
-    acc.x += near.x;
-    acc.y += near.y;
-    acc.z += near.z;
+      store3(D.far_acc, n, je, a);
+    a.x += tot[lane][3];
+    a.y += tot[lane][4];
+    a.z += tot[lane][5];
   }
-  vel.x = fma(acc.x, hdt, vel.x);
-  vel.y = fma(acc.y, hdt, vel.y);
-  vel.z = fma(acc.z, hdt, vel.z);
-  // kick_epilogue with the prefetched inputs
-  store3(D.v, n, j, vel);
-  if (rc_out && massive) {
-    const int far = write_rc_fast(D.u, rc_out, n, j, pos, vel, hc_j);
-    if (check && far != thr_j) atomicOr(D.gate, 1);
+  d3 vel = vel_e;
+  vel.x = fma(a.x, hdt, vel.x);
+  vel.y = fma(a.y, hdt, vel.y);
+  vel.z = fma(a.z, hdt, vel.z);
+  store3(D.v, n, je, vel);
+  if (rc_out && E.massive) {
+    const int far = write_rc_fast(D.u, rc_out, n, je, pos_e, vel, hc_e);
+    if (check && far != thr_e) atomicOr(D.gate, 1);
   }
   if (last) {
-    uint32_t f = flags_j & ~MERC_FLAG_CE_LAST;
-    if (ce_j) f |= MERC_FLAG_CE_LAST | MERC_FLAG_CE_EVER;
-    if (eject_r2 > 0.0 && mag2(pos) > eject_r2) f |= MERC_FLAG_EJECTED;
-    bool fin = mm::isfinite_(pos.x) && mm::isfinite_(pos.y) && mm::isfinite_(pos.z) && mm::isfinite_(vel.x) &&
-               mm::isfinite_(vel.y) && mm::isfinite_(vel.z);
+    uint32_t f = flags_e & ~MERC_FLAG_CE_LAST;
+    if (ce_e) f |= MERC_FLAG_CE_LAST | MERC_FLAG_CE_EVER;
+    if (eject_r2 > 0.0 && mag2(pos_e) > eject_r2) f |= MERC_FLAG_EJECTED;
+    bool fin = mm::isfinite_(pos_e.x) && mm::isfinite_(pos_e.y) && mm::isfinite_(pos_e.z) &&
+               mm::isfinite_(vel.x) && mm::isfinite_(vel.y) && mm::isfinite_(vel.z);
     if (!fin) f |= MERC_FLAG_NONFINITE;
-    D.flags[j] = f;
+    D.flags[je] = f;
   }
 }
 
