@@ -282,6 +282,7 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
   Dev& D = ctx->D;
   D.n = n;
   D.nsys = n_systems;
+  D.nm0 = n_systems == 1 ? nm[0] : 0;
   const long long sym_set = std::max<long long>(3, sym_total);  // a multiple of 3 (NB * 3 * nm per system)
   int st;
   if ((st = dalloc(ctx, &ctx->d_big, n_systems)) || (st = dalloc(ctx, &ctx->d_nchunk, n_systems)) ||
@@ -509,8 +510,12 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     else
       k_jump<false, false><<<nb, kThreads, 0, s>>>(D, D.x, nullptr, rcB, hdt);
     CK(cudaMemsetAsync(D.ce_count, 0, 2 * sizeof(int), s));
-    if (sym_ce)
-      k_sym<false><<<ctx->n_sym, 32 * kSymSplit, 0, s>>>(D, ctx->d_sym, ctx->n_sym, rcB, p.softening2, 1, nullptr);
+    if (sym_ce && D.nsys == 1)
+      k_sym<false, true><<<ctx->n_sym, 32 * kSymSplit, 0, s>>>(D, ctx->d_sym, ctx->n_sym, rcB, p.softening2, 1,
+                                                               nullptr);
+    else if (sym_ce)
+      k_sym<false, false><<<ctx->n_sym, 32 * kSymSplit, 0, s>>>(D, ctx->d_sym, ctx->n_sym, rcB, p.softening2, 1,
+                                                                nullptr);
     else if (bx)
       k_ce_big_exact<<<nbx, 32 * kExactWarps, 0, s>>>(D, rcB, p.compat_block);
     // big systems only: the encounter sub-step runs beside the drift (the
@@ -572,8 +577,12 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     auto far = [&](const double* rc_in, int set, const int* gate, int ev) {
       int st2;
       if (ev >= 0 && (st2 = kick_ev(ev))) return st2;
-      launch(k_sym<true>, ctx->n_sym, 32 * kSymSplit, D, ctx->d_sym, ctx->n_sym, rc_in,
-             p.softening2, set, gate);
+      if (D.nsys == 1)
+        launch(k_sym<true, true>, ctx->n_sym, 32 * kSymSplit, D, ctx->d_sym, ctx->n_sym, rc_in, p.softening2, set,
+               gate);
+      else
+        launch(k_sym<true, false>, ctx->n_sym, 32 * kSymSplit, D, ctx->d_sym, ctx->n_sym, rc_in, p.softening2, set,
+               gate);
       nk++;
       return ev >= 0 ? kick_ev(ev + 1) : MERC_OK;
     };
@@ -650,8 +659,12 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     nk++;
     if (ctx->has_big) {
       if (use_sym) {
-        launch(k_sym<false>, ctx->n_sym, 32 * kSymSplit, D, ctx->d_sym, ctx->n_sym,
-               rcB, p.softening2, 0, nullptr);
+        if (D.nsys == 1)
+          launch(k_sym<false, true>, ctx->n_sym, 32 * kSymSplit, D, ctx->d_sym, ctx->n_sym, rcB, p.softening2, 0,
+                 nullptr);
+        else
+          launch(k_sym<false, false>, ctx->n_sym, 32 * kSymSplit, D, ctx->d_sym, ctx->n_sym, rcB, p.softening2, 0,
+                 nullptr);
         nk++;
         if (ctx->n_work_tp) {
           launch(k_ce_tiled, ctx->n_work_tp, kTile, D, ctx->d_work_tp, rcB, p.compat_block);
@@ -1990,6 +2003,7 @@ static int step_static(int device, const merc_params* p, int32_t n_bodies, int32
   plan(cv, D, &d_off, &d_nm, &d_big, &d_nchunk, &d_work, &d_ids, &d_flags_scratch);
   D.n = n;
   D.nsys = 1;
+  D.nm0 = nm;
   D.off = d_off;
   D.nm = d_nm;
   D.big = d_big;

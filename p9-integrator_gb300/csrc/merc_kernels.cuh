@@ -45,6 +45,7 @@ struct Dev {
   int nsys = 0;  // systems
   const int* off = nullptr;
   const int* nm = nullptr;
+  int nm0 = 0;  // massive bodies of system 0 when it is the only system (read without a load)
   const int* sys = nullptr;  // system of each body
   const unsigned char* big = nullptr;  // per system: served by the tiled kernels
   const int* nchunk = nullptr;         // per system: source chunks of the tiled kick
@@ -608,7 +609,7 @@ __global__ void __cluster_dims__(kJumpCluster, 1, 1) __launch_bounds__(kJumpThre
     if (CLEAR) D.ce_count[0] = D.ce_count[1] = 0;
     if (CLEAR && D.enc_head) D.enc_head[0] = 0;
   }
-  const int n = D.n, nm = D.nm[0];
+  const int n = D.n, nm = D.nm0;
   const double* vv = vsrc ? vsrc : D.v;
   // this thread's body, loaded before the momentum (it does not depend on it)
   const bool mine = j < n;
@@ -1084,6 +1085,23 @@ struct SymTask {
   int sys, I, J;
 };
 
+// Task t of a single system of NB 32-body blocks, in the host list's order:
+// the off-diagonal pairs I < J row by row, then the diagonal ones (I, I).
+// Row I starts at I (2 NB - I - 1) / 2; the FP32 root estimates the row and
+// integer steps correct it.  Decoded instead of loaded, so the block's first
+// loads are its bodies' (one memory round trip before the pair work rather
+// than three: task, system offsets, bodies).
+__device__ __forceinline__ SymTask sym_decode(int t, int NB) {
+  const long long nb = NB, np = nb * (nb - 1) / 2;
+  if (t >= np) return SymTask{0, (int)(t - np), (int)(t - np)};
+  const float b = 2.0f * (float)NB - 1.0f;
+  long long r = (long long)((b - sqrtf(fmaxf(b * b - 8.0f * (float)t, 0.0f))) * 0.5f);
+  r = r < 0 ? 0 : (r > nb - 2 ? nb - 2 : r);
+  while (r > 0 && r * (2 * nb - r - 1) / 2 > t) r--;
+  while ((r + 1) * (2 * nb - r - 2) / 2 <= t) r++;
+  return SymTask{0, (int)r, (int)(t - r * (2 * nb - r - 1) / 2 + r + 1)};
+}
+
 struct RotSrc {
   double x, y, z, m;
   int thr, idx;
@@ -1133,7 +1151,9 @@ __device__ __forceinline__ void rotate(RotSrc& r, d3& acc, uint32_t& bits) {
 // per step), far less than the load difference suggests: the end times were
 // spread evenly rather than in two groups.
 constexpr int kSymSplit = 2;
-template <bool KICK>
+// ONE: a single system (tasks decoded from the block index, no table or
+// system lookups).
+template <bool KICK, bool ONE>
 __global__ void __launch_bounds__(32 * kSymSplit)
     k_sym(Dev D, const SymTask* __restrict__ tasks, int ntasks, const double* __restrict__ rc, double soft2,
           int set, const int* __restrict__ gate) {
@@ -1147,8 +1167,8 @@ __global__ void __launch_bounds__(32 * kSymSplit)
   if (KICK && gate && *gate == 0) return;
   const int lane = threadIdx.x & 31;
   if (KICK && gate && warp == 0 && lane == 0) atomicAdd(D.far_recomputes, 1ull);
-  const SymTask T = tasks[warp];
-  const int s = T.sys, b0 = D.off[s], nm = D.nm[s];
+  const SymTask T = ONE ? sym_decode(warp, (D.nm0 + 31) / 32) : tasks[warp];
+  const int s = T.sys, b0 = ONE ? 0 : D.off[s], nm = ONE ? D.nm0 : D.nm[s];
   const int* far_thr = rc_far_thr_c(rc, D.n);
   const int i = 32 * T.I + lane;
   const bool iv = i < nm;
@@ -1270,8 +1290,9 @@ __global__ void __launch_bounds__(32 * kSymSplit)
   }
   if (KICK) {
     const size_t stride = 3 * (size_t)nm;
-    double* base = D.part_sym + (size_t)set * D.sym_set + D.sym_base[s];
-    uint32_t* mask = D.near_mask + (size_t)set * (D.sym_set / 3) + D.sym_base[s] / 3;
+    const long long sbase = ONE ? 0 : D.sym_base[s];
+    double* base = D.part_sym + (size_t)set * D.sym_set + sbase;
+    uint32_t* mask = D.near_mask + (size_t)set * (D.sym_set / 3) + sbase / 3;
     if (diag) {
       if (iv) {
         double* p = base + (size_t)T.I * stride;
@@ -1373,7 +1394,7 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
     B.s = ONE ? 0 : (valid ? D.sys[jj] : 0);
     B.work = valid && (ONE || D.big[B.s]);
     B.b0 = (ONE || !B.work) ? 0 : D.off[B.s];
-    B.nm = B.work ? D.nm[B.s] : 0;
+    B.nm = B.work ? (ONE ? D.nm0 : D.nm[B.s]) : 0;
     B.local = jj - B.b0;
     B.massive = B.work && B.local < B.nm;
     if (B.work && !B.massive && !(D.nchunk[B.s] > 1 && !massive_only)) B.work = false;
@@ -1402,7 +1423,7 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
     if (E.work) {
       pos_e = load3(D.x, n, je);
       vel_e = load3(D.v, n, je);
-      if (E.massive && reuse_set) far_e = load3(D.far_acc, n, je);
+      if (E.massive && far_mode == 2) far_e = load3(D.far_acc, n, je);  // used when the gate is clear
       if (rc_out && E.massive) hc_e = D.hc[je];
       if (last) {
         flags_e = D.flags[je];
@@ -1420,10 +1441,12 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   size_t stride = 0;
   int index = 0;
   const bool reuse = massive && reuse_set;
+  // (a single system's partials start at 0)
+  const long long sbase = ONE ? 0 : (massive ? D.sym_base[s] : 0);
   if (massive) {
     count = (nm + 31) / 32;
-    base = D.part_sym + (size_t)set * D.sym_set + D.sym_base[s];
-    mask = D.near_mask + (size_t)set * (D.sym_set / 3) + D.sym_base[s] / 3;
+    base = D.part_sym + (size_t)set * D.sym_set + sbase;
+    mask = D.near_mask + (size_t)set * (D.sym_set / 3) + sbase / 3;
     stride = 3 * (size_t)nm;
     index = local;
   } else if (work) {
@@ -1441,11 +1464,15 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   uint32_t words[kRedBatch];
 #pragma unroll
   for (int u = 0; u < kRedBatch; u++) words[u] = 0u;
-  if (reuse) {
+  // the second kick of a merged pair: the near-pair words of partial set 0,
+  // loaded beside the gate rather than after it (a set gate, which is rare,
+  // reloads them from set 1 with the partials below)
+  if (massive && far_mode == 2) {
+    const uint32_t* mask0 = D.near_mask + sbase / 3;
 #pragma unroll
     for (int u = 0; u < kRedBatch; u++) {
       const int b = sub + u * kRedThreads;
-      words[u] = b < count ? mask[(size_t)b * nm + local] : 0u;
+      words[u] = b < count ? mask0[(size_t)b * nm + local] : 0u;
     }
   }
   for (int b0r = sub, r = 0; !reuse && b0r < count; b0r += kRedBatch * kRedThreads, r++) {
@@ -2124,7 +2151,7 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
   const int lane = (int)(threadIdx.x & 31);
   const int count = D.ce_count[1];
   const int total = enc_tasks_per_body() * count;
-  const int nm1 = ONE ? D.nm[0] : 0;
+  const int nm1 = ONE ? D.nm0 : 0;
   int* err = D.enc_head + 1;
   for (;;) {
     int t = 0;
