@@ -79,10 +79,14 @@ __device__ __forceinline__ bool seed_in_range(double r2) {
 __device__ __forceinline__ double div_seeded(double x, double y) {
   return seed_range_ok(y) ? x * rcp_fast(y) : x / y;
 }
+// (inside [0, 1] the reference's K gtz valid + gto is K itself, and outside
+// the finite range its form is kept; selects rather than products with 0/1
+// factors, whose conversions and multiplications each take an FP64 slot)
 __device__ __forceinline__ double changeover_K_seeded(double y) {
   if (y > 1.0 && y < 1.7976931348623157e308) return 1.0;
   if (y < 0.0 && y > -1.7976931348623157e308) return 0.0;
-  double K = div_seeded(y * y, 2.0 * y * y - 2.0 * y + 1.0);
+  const double K = div_seeded(y * y, 2.0 * y * y - 2.0 * y + 1.0);
+  if (y >= 0.0 && y <= 1.0) return K;
   double gtz = (double)(y > 0.0), gto = (double)(y > 1.0), valid = (double)(y <= 1.0 && y >= 0.0);
   return K * gtz * valid + gto;
 }
@@ -92,11 +96,14 @@ __device__ __forceinline__ void pair_exact(const d3& pos, int self, int i, const
   d3 d = {S.x - pos.x, S.y - pos.y, S.z - pos.z};
   double r_sq = mag2(d);
   double r = seed_range_ok(r_sq) ? r_sq * rsqrt_fast(U1, r_sq) : stable_sqrt(r_sq);
-  double notself = (double)(self != i);
-  double K = changeover_K_seeded(div_seeded(notself * r - S.rc01, S.rc09));
+  // notself * r and notself * soft2 of the reference as selects (the same
+  // values for finite r)
+  const bool other = self != i;
+  double K = changeover_K_seeded(div_seeded((other ? r : 0.0) - S.rc01, S.rc09));
   double w = K;
-  if (BS) w = (double)(r <= S.rc) * (1.0 - K) + (double)(r > S.rc) * K;
-  r_sq += notself * soft2;
+  // (r <= rc) (1 - K) + (r > rc) K: the same value, NaN where either is
+  if (BS) w = r <= S.rc ? 1.0 - K : K;
+  if (other) r_sq += soft2;
   const double den = r_sq * r;
   double wa = w * (den != 0.0 ? div_seeded(S.m, den) : stable_div(S.m, den));
   acc.x = fma(wa, d.x, acc.x);

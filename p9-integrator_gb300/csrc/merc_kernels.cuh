@@ -583,10 +583,32 @@ __global__ void __launch_bounds__(kJumpThreads) k_jump(Dev D, const double* __re
   }
 }
 
+// Totals of (x, y, z) over the 32 lanes of a warp by a reduce-scatter: at the
+// first level lanes 0-15 keep x and y and lanes 16-31 keep z (and an empty
+// fourth sum), at the second each group of eight lanes keeps one component,
+// and three more levels finish it; six FP64 additions in all, against fifteen
+// for three butterflies (the FP64 pipe is the bound of the sub-step).  A fixed
+// tree: every lane ends with the same totals, whatever the schedule.
+__device__ __forceinline__ d3 warp_sum3(const FU& U, const d3& a) {
+  const unsigned full = 0xffffffffu;
+  const int lane = (int)(threadIdx.x & 31);
+  const bool up = (lane & 16) != 0, b3 = (lane & 8) != 0;
+  double k0 = up ? a.z : a.x, k1 = up ? 0.0 : a.y;
+  const double s0 = up ? a.x : a.z, s1 = up ? a.y : 0.0;
+  k0 = fadd(U, k0, __shfl_xor_sync(full, s0, 16));
+  k1 = fadd(U, k1, __shfl_xor_sync(full, s1, 16));
+  double k = b3 ? k1 : k0;
+  k = fadd(U, k, __shfl_xor_sync(full, b3 ? k0 : k1, 8));
+  k = fadd(U, k, __shfl_xor_sync(full, k, 4));
+  k = fadd(U, k, __shfl_xor_sync(full, k, 2));
+  k = fadd(U, k, __shfl_xor_sync(full, k, 1));
+  return {__shfl_sync(full, k, 0), __shfl_sync(full, k, 8), __shfl_sync(full, k, 16)};
+}
+
 // Solar jump of a single big system (system 0 holds every body) by clusters
 // of kJumpCluster blocks: block r of a cluster sums the momentum of massive
-// bodies [r nm / 8, (r + 1) nm / 8) (thread t adds bodies t, t + B, ...; a
-// fixed butterfly per warp; warp sums in warp order), the cluster exchanges
+// bodies [r nm / 8, (r + 1) nm / 8) (thread t adds bodies t, t + B, ...;
+// warp_sum3 per warp; warp sums in warp order), the cluster exchanges
 // the eight partials through distributed shared memory and every block adds
 // them in rank order, so every cluster gets the same bits with one eighth of
 // the momentum work per block.  Then as k_jump: x = xsrc + dt/2 P, v copied
@@ -639,46 +661,35 @@ __global__ void __cluster_dims__(kJumpCluster, 1, 1) __launch_bounds__(kJumpThre
       }
     }
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    px += __shfl_xor_sync(0xffffffffu, px, o);
-    py += __shfl_xor_sync(0xffffffffu, py, o);
-    pz += __shfl_xor_sync(0xffffffffu, pz, o);
-  }
+  // (every FP64 instruction of these sums costs its warp's sub-partition a
+  // full warp slot however few lanes need the result, and each warp of this
+  // kernel is alone on its sub-partition: the sums run one component per
+  // lane where they can)
+  const d3 wt = warp_sum3(D.u, d3{px, py, pz});
   if (lane == 0) {
-    wsum[warp][0] = px;
-    wsum[warp][1] = py;
-    wsum[warp][2] = pz;
+    wsum[warp][0] = wt.x;
+    wsum[warp][1] = wt.y;
+    wsum[warp][2] = wt.z;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double sx = 0.0, sy = 0.0, sz = 0.0;
-    for (int w = 0; w < nw; w++) {
-      sx += wsum[w][0];
-      sy += wsum[w][1];
-      sz += wsum[w][2];
-    }
-    part[0] = sx;
-    part[1] = sy;
-    part[2] = sz;
+  if (threadIdx.x < 3) {
+    double sc = 0.0;
+    for (int w = 0; w < nw; w++) sc += wsum[w][threadIdx.x];
+    part[threadIdx.x] = sc;
   }
   cl.sync();
-  // the partials of the cluster's blocks: every remote load in flight before
-  // the additions, which run in rank order
-  double q[kJumpCluster][3];
+  // the partials of the cluster's blocks, added in rank order by lanes 0-2
+  // of every warp (one component each; the remote loads in flight before the
+  // additions), then handed to the other lanes
+  double q[kJumpCluster];
+  const int c = lane < 3 ? lane : 0;
 #pragma unroll
-  for (int r = 0; r < kJumpCluster; r++) {
-    const double* p = cl.map_shared_rank(part, r);
-    q[r][0] = p[0];
-    q[r][1] = p[1];
-    q[r][2] = p[2];
-  }
-  double Px = 0.0, Py = 0.0, Pz = 0.0;
+  for (int r = 0; r < kJumpCluster; r++) q[r] = cl.map_shared_rank(part, r)[c];
+  double Pc = 0.0;
 #pragma unroll
-  for (int r = 0; r < kJumpCluster; r++) {
-    Px += q[r][0];
-    Py += q[r][1];
-    Pz += q[r][2];
-  }
+  for (int r = 0; r < kJumpCluster; r++) Pc += q[r];
+  const double Px = __shfl_sync(0xffffffffu, Pc, 0), Py = __shfl_sync(0xffffffffu, Pc, 1),
+               Pz = __shfl_sync(0xffffffffu, Pc, 2);
   // no block leaves while another may still read its partial: arrive now,
   // wait at the end, after this thread's own work
   auto reads_done = cl.barrier_arrive();
@@ -1866,27 +1877,6 @@ __device__ __forceinline__ bool bs_fast_term(const Dev& D, const double* __restr
   return !far;
 }
 
-// Totals of (x, y, z) over the 32 lanes of a warp by a reduce-scatter: at the
-// first level lanes 0-15 keep x and y and lanes 16-31 keep z (and an empty
-// fourth sum), at the second each group of eight lanes keeps one component,
-// and three more levels finish it; six FP64 additions in all, against fifteen
-// for three butterflies (the FP64 pipe is the bound of the sub-step).  A fixed
-// tree: every lane ends with the same totals, whatever the schedule.
-__device__ __forceinline__ d3 warp_sum3(const FU& U, const d3& a) {
-  const unsigned full = 0xffffffffu;
-  const int lane = (int)(threadIdx.x & 31);
-  const bool up = (lane & 16) != 0, b3 = (lane & 8) != 0;
-  double k0 = up ? a.z : a.x, k1 = up ? 0.0 : a.y;
-  const double s0 = up ? a.x : a.z, s1 = up ? a.y : 0.0;
-  k0 = fadd(U, k0, __shfl_xor_sync(full, s0, 16));
-  k1 = fadd(U, k1, __shfl_xor_sync(full, s1, 16));
-  double k = b3 ? k1 : k0;
-  k = fadd(U, k, __shfl_xor_sync(full, b3 ? k0 : k1, 8));
-  k = fadd(U, k, __shfl_xor_sync(full, k, 4));
-  k = fadd(U, k, __shfl_xor_sync(full, k, 2));
-  k = fadd(U, k, __shfl_xor_sync(full, k, 1));
-  return {__shfl_sync(full, k, 0), __shfl_sync(full, k, 8), __shfl_sync(full, k, 16)};
-}
 
 // Sum over sources c0..c1 - 1 of the encounter body's pull, by one warp:
 // sources c0 + lane + 32 k, even k into a0, odd k into a1 (two independent
