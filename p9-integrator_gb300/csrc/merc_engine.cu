@@ -577,12 +577,12 @@ int enqueue_step(merc_ctx* ctx, bool record_kick_events, int step_in_graph, int*
     auto far = [&](const double* rc_in, int set, const int* gate, int ev) {
       int st2;
       if (ev >= 0 && (st2 = kick_ev(ev))) return st2;
+      // the gated pass (usually empty) in fewer blocks, each looping over tasks
+      const int nfar = gate ? (ctx->n_sym + kSymGatedDiv - 1) / kSymGatedDiv : ctx->n_sym;
       if (D.nsys == 1)
-        launch(k_sym<true, true>, ctx->n_sym, 32 * kSymSplit, D, ctx->d_sym, ctx->n_sym, rc_in, p.softening2, set,
-               gate);
+        launch(k_sym<true, true>, nfar, 32 * kSymSplit, D, ctx->d_sym, ctx->n_sym, rc_in, p.softening2, set, gate);
       else
-        launch(k_sym<true, false>, ctx->n_sym, 32 * kSymSplit, D, ctx->d_sym, ctx->n_sym, rc_in, p.softening2, set,
-               gate);
+        launch(k_sym<true, false>, nfar, 32 * kSymSplit, D, ctx->d_sym, ctx->n_sym, rc_in, p.softening2, set, gate);
       nk++;
       return ev >= 0 ? kick_ev(ev + 1) : MERC_OK;
     };

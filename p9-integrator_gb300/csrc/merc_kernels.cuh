@@ -1162,22 +1162,23 @@ __device__ __forceinline__ void rotate(RotSrc& r, d3& acc, uint32_t& bits) {
 // per step), far less than the load difference suggests: the end times were
 // spread evenly rather than in two groups.
 constexpr int kSymSplit = 2;
-// ONE: a single system (tasks decoded from the block index, no table or
-// system lookups).
+// Tasks per block of the gated second far-field pass.  It is usually empty
+// (its blocks read the clear gate and leave): 2016 one-task blocks took
+// 3.2 us to do that; a quarter of the blocks, each looping over four tasks
+// when the gate is set, 0.2399 -> 0.2389 ms per step on the 2002-body disk.
+// (The encounter test keeps one task per block and two warps per task: two
+// tasks per block measured +3 us per step, four and eight warps per task
+// +0.9 and +2.9 us.)
+constexpr int kSymGatedDiv = 4;
+// One block-pair task on the kSymSplit warps of a block (k_sym); ONE: a
+// single system (tasks decoded from the index, no table or system lookups).
 template <bool KICK, bool ONE>
-__global__ void __launch_bounds__(32 * kSymSplit)
-    k_sym(Dev D, const SymTask* __restrict__ tasks, int ntasks, const double* __restrict__ rc, double soft2,
-          int set, const int* __restrict__ gate) {
-  griddep_enter();
+__device__ __forceinline__ void sym_task(const Dev& D, const SymTask* __restrict__ tasks, int warp,
+                                         const double* __restrict__ rc, double soft2, int set) {
   constexpr int SPLIT = kSymSplit;
-  // KICK: one task per block, warp `part` of SPLIT takes its share of the
-  // rotations; otherwise one task per warp
-  const int warp = (int)blockIdx.x;
+  // warp `part` of SPLIT takes its share of the task's rotations
   const int part = (int)(threadIdx.x >> 5);
-  if (warp >= ntasks) return;  // whole blocks leave together
-  if (KICK && gate && *gate == 0) return;
   const int lane = threadIdx.x & 31;
-  if (KICK && gate && warp == 0 && lane == 0) atomicAdd(D.far_recomputes, 1ull);
   const SymTask T = ONE ? sym_decode(warp, (D.nm0 + 31) / 32) : tasks[warp];
   const int s = T.sys, b0 = ONE ? 0 : D.off[s], nm = ONE ? D.nm0 : D.nm[s];
   const int* far_thr = rc_far_thr_c(rc, D.n);
@@ -1338,6 +1339,21 @@ __global__ void __launch_bounds__(32 * kSymSplit)
     int* cnt = set ? &D.ce_count[0] : &D.ce_count[1];
     append_ce(fa, b0 + i, list, cnt, &D.counters[0]);
     append_ce(fb, b0 + j0, list, cnt, &D.counters[0]);
+  }
+}
+// Tasks blockIdx.x, blockIdx.x + gridDim.x, ... (whole blocks leave
+// together; a barrier between tasks keeps the next task's shared-memory
+// exchange after this one's reads).
+template <bool KICK, bool ONE>
+__global__ void __launch_bounds__(32 * kSymSplit)
+    k_sym(Dev D, const SymTask* __restrict__ tasks, int ntasks, const double* __restrict__ rc, double soft2,
+          int set, const int* __restrict__ gate) {
+  griddep_enter();
+  if (KICK && gate && *gate == 0) return;
+  if (KICK && gate && blockIdx.x == 0 && (threadIdx.x & 31) == 0) atomicAdd(D.far_recomputes, 1ull);
+  for (int t = (int)blockIdx.x; t < ntasks; t += (int)gridDim.x) {
+    sym_task<KICK, ONE>(D, tasks, t, rc, soft2, set);
+    __syncthreads();
   }
 }
 
