@@ -2215,11 +2215,31 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
     const int c = lane < 3 ? lane : 0;
     double a = 0.0;
     for (int r = 0; r < P; r++) a += __ldcg(qs + 3 * r + c);
+    // The final evaluation of a row: when the other two rows have published
+    // their results already (read beside the part sums), this warp is the
+    // last of the body and combines the rows at once, their results loaded
+    // beside its own finish and its own row's taken from lanes 0-2, without
+    // the counter's round trip and the reload (the same values either way).
+    // Lanes 0-11 hold the pair of rows their Richardson quotient needs: lanes
+    // 0-5 rows 1 and 0 (b11), lanes 6-11 rows 2 and 1 (b21), component cr.
+    const bool final_eval = e + 1 == N;
+    int others = 0;
+    if (final_eval && lane == 0) others = ld_acquire(cnt + 10);
+    const bool last_row = __shfl_sync(0xffffffffu, others, 0) == 2;
+    __syncwarp();  // the other lanes' loads below after lane 0's acquire
+    double* res = D.enc_res + 18 * (size_t)k;
+    const int cr = lane < 6 ? lane : lane - 6;  // component: pos x, y, z, vel x, y, z
+    const int rhi = lane < 6 ? 1 : 2;           // the finer row; the coarser is rhi - 1
+    double o_hi = 0.0, o_lo = 0.0;
+    if (last_row && lane < 12) {
+      if (rhi != row) o_hi = __ldcg(res + 6 * rhi + cr);
+      if (rhi - 1 != row) o_lo = __ldcg(res + 6 * (rhi - 1) + cr);
+    }
     const double z0c = c == 0 ? m.z0.x : (c == 1 ? m.z0.y : m.z0.z);
     const double z1c = c == 0 ? m.z1.x : (c == 1 ? m.z1.y : m.z1.z);
     double vc = c == 0 ? m.vel.x : (c == 1 ? m.vel.y : m.vel.z);
     vc = fma(sun_accel_c(D.u, m.z1, z1c, soft2), m.h, fma(a, m.h, vc));
-    if (e + 1 < N) {
+    if (!final_eval) {
       if (lane < 3) {
         st[c] = z1c;                      // z0 of the next evaluation
         st[3 + c] = fma(m.h2, vc, z0c);   // z1, the next evaluation point
@@ -2229,36 +2249,44 @@ __global__ void __launch_bounds__(32 * kEncTaskWarps)
       if (lane == 0) st_release(cnt + 7 + row, e + 1);
       continue;
     }
-    double* res = D.enc_res + 18 * (size_t)k;
-    if (lane < 3) {
-      double* rs = res + 6 * row;
-      rs[c] = 0.5 * (z1c + fma(vc, m.h, z0c));
-      rs[3 + c] = vc;
+    const double pc = 0.5 * (z1c + fma(vc, m.h, z0c));
+    if (last_row) {
+      const int src = cr < 3 ? cr : cr - 3;
+      const double sp = __shfl_sync(0xffffffffu, pc, src & 31), sv = __shfl_sync(0xffffffffu, vc, src & 31);
+      const double own = cr < 3 ? sp : sv;
+      if (rhi == row) o_hi = own;
+      if (rhi - 1 == row) o_lo = own;
+    } else {
+      if (lane < 3) {
+        double* rs = res + 6 * row;
+        rs[c] = pc;
+        rs[3 + c] = vc;
+      }
+      __syncwarp();  // lanes 1-2's stores before lane 0's release
+      int fin = 0;
+      if (lane == 0) fin = atom_add_acq_rel(cnt + 10, 1) == 2;
+      if (!__shfl_sync(0xffffffffu, fin, 0)) continue;
+      __syncwarp();  // the other lanes' loads below after lane 0's acquire
+      if (lane < 12) {
+        o_hi = __ldcg(res + 6 * rhi + cr);
+        o_lo = __ldcg(res + 6 * (rhi - 1) + cr);
+      }
     }
-    __syncwarp();  // lanes 1-2's stores before lane 0's release
-    int fin = 0;
-    if (lane == 0) fin = atom_add_acq_rel(cnt + 10, 1) == 2;
-    if (!__shfl_sync(0xffffffffu, fin, 0)) continue;
-    __syncwarp();  // the other lanes' loads below after lane 0's acquire
     // The Richardson combination (rich_combine's arithmetic per component),
     // one component per lane: lanes 0-5 combine rows 1 and 0 (b11), lanes
     // 6-11 rows 2 and 1 (b21), then lanes 0-5 b21 and b11 (b22).  A warp
     // instruction costs the FP64 unit the same however few lanes run it, so
     // the eighteen quotients take a few instructions instead of dozens.
     {
-      const int c = lane < 6 ? lane : lane - 6;  // component: pos x, y, z, vel x, y, z
       double b = 0.0;
-      if (lane < 12) {
-        const int r = lane < 6 ? 1 : 2;  // the finer row; the coarser is r - 1
-        b = rich_q(__ldcg(res + 6 * r + c), __ldcg(res + 6 * (r - 1) + c), 4.0);
-      }
+      if (lane < 12) b = rich_q(o_hi, o_lo, 4.0);
       const double b21 = __shfl_sync(0xffffffffu, b, (lane + 6) & 31);
       if (lane < 6) {
         const double b22 = rich_q(b21, b, 16.0);
-        if (c < 3)
-          D.xo[(size_t)c * n + j] = b22;
+        if (cr < 3)
+          D.xo[(size_t)cr * n + j] = b22;
         else
-          D.vo[(size_t)(c - 3) * n + j] = b22;
+          D.vo[(size_t)(cr - 3) * n + j] = b22;
       }
     }
     if (lane < 11) cnt[lane] = 0;  // every task of this body is done
