@@ -69,11 +69,15 @@ __device__ __forceinline__ double rcrit_hc(const d3& r, const d3& v, double hc) 
 
 // Changeover weight K(y), y = (r_ij - 0.1 rc) / (0.9 rc) (sim.cuh:176-183).
 // The common cases y > 1 (K = 1) and y < 0 (K = 0) give the same bits as the
-// branch-free formula; everything else takes the formula.
+// branch-free formula, and so does K itself for y in [0, 1] (K gtz valid +
+// gto with gtz = valid = 1, gto = 0; K = +0 at y = 0); the rest (infinite
+// or NaN y) takes the formula.  (Products with 0/1 factors and their
+// conversions each take an FP64 slot.)
 __device__ __forceinline__ double changeover_K(double y) {
   if (y > 1.0 && y < 1.7976931348623157e308) return 1.0;
   if (y < 0.0 && y > -1.7976931348623157e308) return 0.0;
   double K = y * y / (2.0 * y * y - 2.0 * y + 1.0);
+  if (y >= 0.0 && y <= 1.0) return K;
   double gtz = (double)(y > 0.0), gto = (double)(y > 1.0), valid = (double)(y <= 1.0 && y >= 0.0);
   return K * gtz * valid + gto;
 }
@@ -100,8 +104,10 @@ __device__ __forceinline__ double exact_term(const d3& pos, int self, const SrcV
   double r_sq = mag2(d);
   double r = stable_sqrt(r_sq);
   double rc = S.rc[4 * i], rc01 = S.rc[4 * i + 1], rc09 = S.rc[4 * i + 2];
-  double notself = (double)(self != i);
-  double r_ij = notself * r;  // norm3d of d is the same sqrt of the same fma chain
+  // notself * r and notself * soft2 of the reference as selects: the same
+  // values for finite r (a non-finite r makes the term NaN either way)
+  const bool other = self != i;
+  double r_ij = other ? r : 0.0;  // norm3d of d is the same sqrt of the same fma chain
   // K = changeover_K(y), y = (r_ij - rc01) / rc09.  Without the division
   // where y is certainly in (1, DBL_MAX), i.e. K = 1: with b = rc09 normal
   // and t > fl(b (1 + 2^-51)) >= b (1 + 2^-52), t / b > 1 + 2^-52 rounds to
@@ -113,8 +119,9 @@ __device__ __forceinline__ double exact_term(const d3& pos, int self, const SrcV
   else
     K = changeover_K(t / rc09);
   double w = K;
-  if (BS) w = (double)(r <= rc) * (1.0 - K) + (double)(r > rc) * K;
-  r_sq += notself * soft2;
+  // (r <= rc) (1 - K) + (r > rc) K: the same value (NaN where K is)
+  if (BS) w = r <= rc ? 1.0 - K : K;
+  if (other) r_sq += soft2;
   double denom = r_sq * r;
   return w * stable_div(S.m[i], denom);
 }
