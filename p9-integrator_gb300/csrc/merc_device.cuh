@@ -67,16 +67,19 @@ __device__ __forceinline__ double rcrit_hc(const d3& r, const d3& v, double hc) 
   return a * hc;
 }
 
-// Changeover weight K(y), y = (r_ij - 0.1 rc) / (0.9 rc) (sim.cuh:176-183).
-// The common cases y > 1 (K = 1) and y < 0 (K = 0) give the same bits as the
-// branch-free formula, and so does K itself for y in [0, 1] (K gtz valid +
-// gto with gtz = valid = 1, gto = 0; K = +0 at y = 0); the rest (infinite
-// or NaN y) takes the formula.  (Products with 0/1 factors and their
-// conversions each take an FP64 slot.)
-__device__ __forceinline__ double changeover_K(double y) {
+// Changeover weight K(y), y = (r_ij - 0.1 rc) / (0.9 rc) (sim.cuh:176-183),
+// K = y^2 / ((2 y) y - 2 y + 1) with the reference's roundings, its additions
+// and products as FMAs on the run-time unit constants (each the same single
+// rounding).  The common cases y > 1 (K = 1) and y < 0 (K = 0) give the same
+// bits as the branch-free formula, and so does K itself for y in [0, 1]
+// (K gtz valid + gto with gtz = valid = 1, gto = 0; K = +0 at y = 0); the
+// rest (infinite or NaN y) takes the formula.  (Products with 0/1 factors
+// and their conversions each take an FP64 slot.)
+__device__ __forceinline__ double changeover_K(const FU& U, double y) {
   if (y > 1.0 && y < 1.7976931348623157e308) return 1.0;
   if (y < 0.0 && y > -1.7976931348623157e308) return 0.0;
-  double K = y * y / (2.0 * y * y - 2.0 * y + 1.0);
+  const double y2 = fmul(U, fmul(U, 2.0, y), y), d = fadd(U, fsub(U, y2, fmul(U, 2.0, y)), 1.0);
+  double K = fmul(U, y, y) / d;
   if (y >= 0.0 && y <= 1.0) return K;
   double gtz = (double)(y > 0.0), gto = (double)(y > 1.0), valid = (double)(y <= 1.0 && y >= 0.0);
   return K * gtz * valid + gto;
@@ -90,6 +93,7 @@ struct SrcView {
   const double* z;
   const double* m;
   const double* rc;  // rc, 0.1 rc, 0.9 rc, fast-path threshold: rc[4*i + k]
+  FU u;              // run-time unit constants of the exact term's additions and products
 };
 
 // K-weighted kick of one body over the system's sources in the reference's
@@ -100,8 +104,12 @@ struct SrcView {
 template <bool BS>
 __device__ __forceinline__ double exact_term(const d3& pos, int self, const SrcView& S, int i, double soft2,
                                              d3& d) {
-  d = {S.x[i] - pos.x, S.y[i] - pos.y, S.z[i] - pos.z};
-  double r_sq = mag2(d);
+  // additions and products as FMAs on the run-time unit constants (the same
+  // single roundings, so the same bits; an FMA issues about 19% faster than
+  // DADD and DMUL on this GPU)
+  const FU& U = S.u;
+  d = {fsub(U, S.x[i], pos.x), fsub(U, S.y[i], pos.y), fsub(U, S.z[i], pos.z)};
+  double r_sq = fma(d.x, d.x, fma(d.y, d.y, fmul(U, d.z, d.z)));
   double r = stable_sqrt(r_sq);
   double rc = S.rc[4 * i], rc01 = S.rc[4 * i + 1], rc09 = S.rc[4 * i + 2];
   // notself * r and notself * soft2 of the reference as selects: the same
@@ -112,18 +120,18 @@ __device__ __forceinline__ double exact_term(const d3& pos, int self, const SrcV
   // where y is certainly in (1, DBL_MAX), i.e. K = 1: with b = rc09 normal
   // and t > fl(b (1 + 2^-51)) >= b (1 + 2^-52), t / b > 1 + 2^-52 rounds to
   // a double > 1; t < fl(b 1e300) keeps it finite.
-  const double t = r_ij - rc01;
+  const double t = fsub(U, r_ij, rc01);
   double K;
-  if (rc09 >= 0x1p-1000 && t > rc09 * (1.0 + 0x1p-51) && t < rc09 * 1e300)
+  if (rc09 >= 0x1p-1000 && t > fmul(U, rc09, 1.0 + 0x1p-51) && t < fmul(U, rc09, 1e300))
     K = 1.0;
   else
-    K = changeover_K(t / rc09);
+    K = changeover_K(U, t / rc09);
   double w = K;
   // (r <= rc) (1 - K) + (r > rc) K: the same value (NaN where K is)
-  if (BS) w = r <= rc ? 1.0 - K : K;
-  if (other) r_sq += soft2;
-  double denom = r_sq * r;
-  return w * stable_div(S.m[i], denom);
+  if (BS) w = r <= rc ? fsub(U, 1.0, K) : K;
+  if (other) r_sq = fadd(U, r_sq, soft2);
+  const double denom = fmul(U, r_sq, r);
+  return fmul(U, w, stable_div(S.m[i], denom));
 }
 
 template <bool BS>

@@ -93,6 +93,7 @@ __device__ __forceinline__ SrcView src_view(const Dev& D, const double* rc, int 
   S.z = D.x + 2 * D.n + b0;
   S.m = D.m + b0;
   S.rc = rc + 4 * (size_t)b0;
+  S.u = D.u;
   return S;
 }
 
