@@ -1165,12 +1165,14 @@ __device__ __forceinline__ void rotate(RotSrc& r, d3& acc, uint32_t& bits) {
 constexpr int kSymSplit = 2;
 // Tasks per block of the gated second far-field pass.  It is usually empty
 // (its blocks read the clear gate and leave): 2016 one-task blocks took
-// 3.2 us to do that; a quarter of the blocks, each looping over four tasks
-// when the gate is set, 0.2399 -> 0.2389 ms per step on the 2002-body disk.
-// (The encounter test keeps one task per block and two warps per task: two
-// tasks per block measured +3 us per step, four and eight warps per task
-// +0.9 and +2.9 us.)
-constexpr int kSymGatedDiv = 4;
+// 3.2 us to do that.  On the 2002-body disk, where it never runs, half and a
+// quarter of the blocks (two or four tasks each) saved 0.6 and 1.1 us per
+// step; with 300 embryos at e = 0.6, where it runs at almost every step,
+// they cost 2.6 and 12.4 us per step (0.3023 -> 0.3049 and 0.3147 ms).  Two
+// tasks per block: the smaller loss where the pass runs.  (The encounter test
+// keeps one task per block and two warps per task: two tasks per block
+// measured +3 us per step, four and eight warps per task +0.9 and +2.9 us.)
+constexpr int kSymGatedDiv = 2;
 // One block-pair task on the kSymSplit warps of a block (k_sym); ONE: a
 // single system (tasks decoded from the index, no table or system lookups).
 template <bool KICK, bool ONE>
