@@ -283,6 +283,7 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
   D.n = n;
   D.nsys = n_systems;
   D.nm0 = n_systems == 1 ? nm[0] : 0;
+  D.gate_words = std::max(1, ((D.nm0 + 31) / 32 + 63) / 64);
   const long long sym_set = std::max<long long>(3, sym_total);  // a multiple of 3 (NB * 3 * nm per system)
   int st;
   if ((st = dalloc(ctx, &ctx->d_big, n_systems)) || (st = dalloc(ctx, &ctx->d_nchunk, n_systems)) ||
@@ -294,6 +295,7 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
       (st = dalloc(ctx, &ctx->d_sym_base, n_systems)) ||
       (st = dalloc(ctx, &D.part_sym, 2 * (size_t)sym_set)) || (st = dalloc(ctx, &D.near_mask, 2 * (size_t)(sym_set / 3))) ||
       (st = dalloc(ctx, &D.gate, 1)) || (st = dalloc(ctx, &D.far_recomputes, 1)) ||
+      (st = dalloc(ctx, &D.gate_blocks, (size_t)D.gate_words)) ||
       (st = dalloc(ctx, &D.far_acc, ctx->has_big ? 3 * (size_t)n : 1)))
     return st;
   {
@@ -308,6 +310,7 @@ int alloc_state(merc_ctx* ctx, int32_t n_systems, const int64_t* off, const int3
   }
   D.sym_set = sym_set;
   CK(cudaMemsetAsync(D.gate, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(D.gate_blocks, 0, sizeof(unsigned long long) * (size_t)D.gate_words, ctx->stream));
   CK(cudaMemsetAsync(D.far_recomputes, 0, sizeof(unsigned long long), ctx->stream));
   if ((st = dalloc(ctx, &ctx->d_off, n_systems + 1)) || (st = dalloc(ctx, &ctx->d_nm, n_systems)) ||
       (st = dalloc(ctx, &ctx->d_sys, n)) || (st = dalloc(ctx, &ctx->d_m, n)) || (st = dalloc(ctx, &D.hc, n)) ||

@@ -69,6 +69,10 @@ struct Dev {
   const long long* sym_base = nullptr;  // per system: offset of its block partials in a set (-1: none)
   long long sym_set = 0;             // doubles per partial set (the mask set has sym_set / 3 words)
   int* gate = nullptr;               // set when a merged kick must recompute the far field
+  // a single big system: bit b set when a body of its 32-body block b moved its
+  // far-field threshold (gate_words words; cleared with the gate)
+  unsigned long long* gate_blocks = nullptr;
+  int gate_words = 0;
   double* far_acc = nullptr;         // 3 n: far-field sum of each massive body of a big system, kept by
                                      //     the first reduce of a merged kick for the second
   unsigned long long* far_recomputes = nullptr;  // gated far-field passes that ran
@@ -487,6 +491,7 @@ __global__ void __launch_bounds__(kJumpThreads) k_jump(Dev D, const double* __re
     if (CLEAR) D.ce_count[0] = D.ce_count[1] = 0;
     if (CLEAR && D.enc_head) D.enc_head[0] = 0;
   }
+  if (D.gate_blocks && j < D.gate_words) D.gate_blocks[j] = 0ull;
   const int n = D.n;
   const int j0 = blockIdx.x * blockDim.x, j1 = min(n, j0 + (int)blockDim.x);
   if (j0 >= n) return;  // whole block
@@ -632,6 +637,7 @@ __global__ void __cluster_dims__(kJumpCluster, 1, 1) __launch_bounds__(kJumpThre
     if (CLEAR) D.ce_count[0] = D.ce_count[1] = 0;
     if (CLEAR && D.enc_head) D.enc_head[0] = 0;
   }
+  if (D.gate_blocks && j < D.gate_words) D.gate_blocks[j] = 0ull;
   const int n = D.n, nm = D.nm0;
   const double* vv = vsrc ? vsrc : D.v;
   // this thread's body, loaded before the momentum (it does not depend on it)
@@ -1148,7 +1154,8 @@ __device__ __forceinline__ void rotate(RotSrc& r, d3& acc, uint32_t& bits) {
 }
 
 // KICK: far-field sums and near-pair masks into partial set `set` (thresholds
-// from rc's far-field table); with `gate`, only when *gate is set.
+// from rc's far-field table); with `gate`, only when *gate is set (and for a
+// single system only the block pairs that D.gate_blocks marks).
 // !KICK: encounter test flags (rc's fast thresholds; the flags must be clear
 // before the launch), the flagged bodies appended to the big-system list
 // (set 0) or to the element path's list (set 1).
@@ -1355,6 +1362,13 @@ __global__ void __launch_bounds__(32 * kSymSplit)
   if (KICK && gate && *gate == 0) return;
   if (KICK && gate && blockIdx.x == 0 && (threadIdx.x & 31) == 0) atomicAdd(D.far_recomputes, 1ull);
   for (int t = (int)blockIdx.x; t < ntasks; t += (int)gridDim.x) {
+    // the gated pass of a single system: only the block pairs with a block
+    // whose far-field threshold moved (the others are the same in both sets)
+    if (KICK && ONE && gate) {
+      const SymTask T = sym_decode(t, (D.nm0 + 31) / 32);
+      const unsigned long long* gb = D.gate_blocks;
+      if (!(((gb[T.I >> 6] >> (T.I & 63)) | (gb[T.J >> 6] >> (T.J & 63))) & 1ull)) continue;
+    }
     sym_task<KICK, ONE>(D, tasks, t, rc, soft2, set);
     __syncthreads();
   }
@@ -1473,10 +1487,22 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   const bool reuse = massive && reuse_set;
   // (a single system's partials start at 0)
   const long long sbase = ONE ? 0 : (massive ? D.sym_base[s] : 0);
+  // A single system whose gate is set: the gated pass recomputed only the
+  // block pairs with a block whose far-field threshold moved (into set 1);
+  // the others are the same in both sets (same positions, same thresholds),
+  // so each pair's partial and near-pair word come from the set it was last
+  // computed in: the bits of a full recompute.
+  const bool pick = ONE && massive && set == 1;
+  const int blk = local >> 5;
+  const bool blk_moved = pick && ((D.gate_blocks[blk >> 6] >> (blk & 63)) & 1ull);
+  // set 1 -> set 0 for pair (blk, b) when neither block moved
+  auto back = [&](int b) { return pick && !blk_moved && !((D.gate_blocks[b >> 6] >> (b & 63)) & 1ull); };
+  const uint32_t* mask0 = nullptr;
   if (massive) {
     count = (nm + 31) / 32;
-    base = D.part_sym + (size_t)set * D.sym_set + sbase;
-    mask = D.near_mask + (size_t)set * (D.sym_set / 3) + sbase / 3;
+    mask0 = D.near_mask + sbase / 3;
+    base = D.part_sym + sbase + (size_t)set * D.sym_set;
+    mask = mask0 + (size_t)set * (D.sym_set / 3);
     stride = 3 * (size_t)nm;
     index = local;
   } else if (work) {
@@ -1498,7 +1524,6 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   // loaded beside the gate rather than after it (a set gate, which is rare,
   // reloads them from set 1 with the partials below)
   if (massive && far_mode == 2) {
-    const uint32_t* mask0 = D.near_mask + sbase / 3;
 #pragma unroll
     for (int u = 0; u < kRedBatch; u++) {
       const int b = sub + u * kRedThreads;
@@ -1511,11 +1536,12 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
     for (int u = 0; u < kRedBatch; u++) {
       const int b = b0r + u * kRedThreads;
       const bool ok = b < count;
-      const double* p = base + (size_t)b * stride;
+      const bool bk = back(b);
+      const double* p = base + (size_t)b * stride - (bk ? D.sym_set : 0);
       px[u] = ok ? p[index] : 0.0;
       py[u] = ok ? p[span + index] : 0.0;
       pz[u] = ok ? p[2 * span + index] : 0.0;
-      if (r == 0) words[u] = (ok && massive) ? mask[(size_t)b * nm + local] : 0u;
+      if (r == 0) words[u] = (ok && massive) ? (mask - (bk ? D.sym_set / 3 : 0))[(size_t)b * nm + local] : 0u;
     }
 #pragma unroll
     for (int u = 0; u < kRedBatch; u++) {
@@ -1537,8 +1563,10 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   int own = 0;
 #pragma unroll
   for (int u = 0; u < kRedBatch; u++) own += __popc(words[u]);
+  // near-pair word of source block b from the set its pair was last computed in
+  auto mword = [&](int b) { return (mask - (back(b) ? D.sym_set / 3 : 0))[(size_t)b * nm + local]; };
   for (int b = sub + kRedBatch * kRedThreads; massive && b < count; b += kRedThreads)
-    own += __popc(mask[(size_t)b * nm + local]);
+    own += __popc(mword(b));
   int incl = own;
   for (int o = 1; o < kRedThreads; o <<= 1) {
     const int v = __shfl_up_sync(0xffffffffu, incl, o, kRedThreads);
@@ -1553,7 +1581,7 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
     for (int u = 0; u < kRedBatch; u++)
       for (uint32_t w = words[u]; w; w &= w - 1u) list[at++] = 32 * (sub + u * kRedThreads) + __ffs(w) - 1;
     for (int b = sub + kRedBatch * kRedThreads; b < count; b += kRedThreads)
-      for (uint32_t w = mask[(size_t)b * nm + local]; w; w &= w - 1u) list[at++] = 32 * b + __ffs(w) - 1;
+      for (uint32_t w = mword(b); w; w &= w - 1u) list[at++] = 32 * b + __ffs(w) - 1;
   }
   __syncwarp();
   d3 near = {0.0, 0.0, 0.0};
@@ -1572,7 +1600,7 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
       }
     }
     for (int b = sub + kRedBatch * kRedThreads; b < count; b += kRedThreads) {
-      for (uint32_t w = mask[(size_t)b * nm + local]; w; w &= w - 1u) {
+      for (uint32_t w = mword(b); w; w &= w - 1u) {
         const int src = 32 * b + __ffs(w) - 1;
         pair_exact<false>(pos, local, src, load_src(D, rc, b0 + src), soft2, near);
       }
@@ -1607,7 +1635,10 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
   store3(D.v, n, je, vel);
   if (rc_out && E.massive) {
     const int far = write_rc_fast(D.u, rc_out, n, je, pos_e, vel, hc_e);
-    if (check && far != thr_e) atomicOr(D.gate, 1);
+    if (check && far != thr_e) {
+      atomicOr(D.gate, 1);
+      if (ONE) atomicOr(D.gate_blocks + (E.local >> 11), 1ull << ((E.local >> 5) & 63));
+    }
   }
   if (last) {
     uint32_t f = flags_e & ~MERC_FLAG_CE_LAST;
