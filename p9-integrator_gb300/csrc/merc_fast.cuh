@@ -90,10 +90,13 @@ __device__ __forceinline__ double changeover_K_seeded(double y) {
   double gtz = (double)(y > 0.0), gto = (double)(y > 1.0), valid = (double)(y <= 1.0 && y >= 0.0);
   return K * gtz * valid + gto;
 }
+// The reference formula's factor wa and separation d of one pair
+// (pair_exact adds wa d to its sum with three fmas)
 template <bool BS>
-__device__ __forceinline__ void pair_exact(const d3& pos, int self, int i, const FastSrc& S, double soft2, d3& acc) {
+__device__ __forceinline__ double pair_exact_w(const d3& pos, int self, int i, const FastSrc& S, double soft2,
+                                               d3& d) {
   const FU U1 = {1.0, -0.0};
-  d3 d = {S.x - pos.x, S.y - pos.y, S.z - pos.z};
+  d = {S.x - pos.x, S.y - pos.y, S.z - pos.z};
   double r_sq = mag2(d);
   double r = seed_range_ok(r_sq) ? r_sq * rsqrt_fast(U1, r_sq) : stable_sqrt(r_sq);
   // notself * r and notself * soft2 of the reference as selects (the same
@@ -105,7 +108,12 @@ __device__ __forceinline__ void pair_exact(const d3& pos, int self, int i, const
   if (BS) w = r <= S.rc ? 1.0 - K : K;
   if (other) r_sq += soft2;
   const double den = r_sq * r;
-  double wa = w * (den != 0.0 ? div_seeded(S.m, den) : stable_div(S.m, den));
+  return w * (den != 0.0 ? div_seeded(S.m, den) : stable_div(S.m, den));
+}
+template <bool BS>
+__device__ __forceinline__ void pair_exact(const d3& pos, int self, int i, const FastSrc& S, double soft2, d3& acc) {
+  d3 d;
+  const double wa = pair_exact_w<BS>(pos, self, i, S, soft2, d);
   acc.x = fma(wa, d.x, acc.x);
   acc.y = fma(wa, d.y, acc.y);
   acc.z = fma(wa, d.z, acc.z);
@@ -150,6 +158,25 @@ __device__ __forceinline__ void pair_fast(const FU& U, const d3& pos, int self, 
     // exactly zero: K = 0 and the guarded division returns 0)
     pair_exact<BS>(pos, self, i, S, soft2, acc);
   }
+}
+
+// pair_fast<false> as a term: whether the pair adds w d to the kick's sum
+// (with the same three fmas), and w and d (the same values, so a sum of terms
+// computed on other lanes and added in source order has pair_fast's bits)
+__device__ __forceinline__ bool kick_term(const FU& U, const d3& pos, int self, int i, const FastSrc& S,
+                                          double soft2, double& w, d3& d) {
+  const double dx = fsub(U, S.x, pos.x), dy = fsub(U, S.y, pos.y), dz = fsub(U, S.z, pos.z);
+  const double r2 = fma(dx, dx, fma(dy, dy, fmul(U, dz, dz)));
+  if (hi_word(r2) > S.rc2_hi && i != self && seed_in_range(r2)) {
+    w = fmul(U, S.m, inv_softened_r3(U, r2, fadd(U, r2, soft2)));
+    d = {dx, dy, dz};
+    return true;
+  }
+  if (i != self || r2 != 0.0) {
+    w = pair_exact_w<false>(pos, self, i, S, soft2, d);
+    return true;
+  }
+  return false;
 }
 
 // Sun pull of the encounter sub-stepper: -pos / ((r^2 + eps^2) r)

@@ -242,18 +242,14 @@ __global__ void __launch_bounds__(256, 2) k_sweep_persistent(SweepArgs A) {
           VM[kSweepMaxNm + lane] = v.y;
           VM[2 * kSweepMaxNm + lane] = v.z;
         };
-        // sum_i m_i v_i in source order (as k_momentum), one lane
+        // sum_i m_i v_i in source order (as k_momentum), one component per
+        // lane (an FP64 instruction costs the warp's sub-partition the same
+        // however few lanes run it)
         auto momentum = [&](double* P) {
-          if (lane == 0) {
-            double px = 0.0, py = 0.0, pz = 0.0;
-            for (int i = 0; i < nm; i++) {
-              px = fma(M[i], VM[i], px);
-              py = fma(M[i], VM[kSweepMaxNm + i], py);
-              pz = fma(M[i], VM[2 * kSweepMaxNm + i], pz);
-            }
-            P[0] = px;
-            P[1] = py;
-            P[2] = pz;
+          if (lane < 3) {
+            double p = 0.0;
+            for (int i = 0; i < nm; i++) p = fma(M[i], VM[lane * kSweepMaxNm + i], p);
+            P[lane] = p;
           }
           __syncwarp();
         };
@@ -278,10 +274,34 @@ __global__ void __launch_bounds__(256, 2) k_sweep_persistent(SweepArgs A) {
           }
           __syncwarp();
         };
+        // with nm^2 <= 32 the pair terms of all targets in one round, lane
+        // t nm + j for target t and source j, then each target's lane adds
+        // its terms in source order (kick_term: kick_sum's bits)
         auto kick = [&](const double* Xs, const double* Ts) {
+          d3 a = {0.0, 0.0, 0.0};
+          if (nm * nm <= 32) {
+            const int t = lane / max(nm, 1), j = lane - t * nm;
+            double w = 0.0;
+            d3 d = {0.0, 0.0, 0.0};
+            bool add = false;
+            if (lane < nm * nm) {
+              const d3 xt = {XM[t], XM[kSweepMaxNm + t], XM[2 * kSweepMaxNm + t]};
+              add = kick_term(D.u, xt, self_index(t, A.compat_block), j, smem_src(Xs, M, Ts, nh, j), A.soft2, w, d);
+            }
+            for (int k = 0; k < nm; k++) {
+              const int src = (act ? lane : 0) * nm + k;
+              const double ws = __shfl_sync(0xffffffffu, w, src), dx = __shfl_sync(0xffffffffu, d.x, src),
+                           dy = __shfl_sync(0xffffffffu, d.y, src), dz = __shfl_sync(0xffffffffu, d.z, src);
+              if (__shfl_sync(0xffffffffu, (int)add, src) && act) {
+                a.x = fma(ws, dx, a.x);
+                a.y = fma(ws, dy, a.y);
+                a.z = fma(ws, dz, a.z);
+              }
+            }
+          } else if (act) {
+            a = kick_sum(xm(), self, Xs, Ts, nm);
+          }
           if (act) {
-            const d3 x = xm();
-            const d3 a = kick_sum(x, self, Xs, Ts, nm);
             d3 v = vm();
             v.x = fma(a.x, hdt, v.x);
             v.y = fma(a.y, hdt, v.y);
