@@ -1659,6 +1659,7 @@ __global__ void __launch_bounds__(kTile) k_ce_tiled(Dev D, const Work* __restric
   griddep_enter();
   __shared__ FastSrc tile[kSrcTile];
   __shared__ F4 tilef[kSrcTile];
+  __shared__ float tilerc[kSrcTile];  // the sources' r_crit as FP32 (f32_trunc), once per source
   const Work W = work[blockIdx.x];
   const int n = D.n, s = W.sys, b0 = D.off[s], b1 = D.off[s + 1];
   const int j = W.t0 + threadIdx.x;
@@ -1671,10 +1672,29 @@ __global__ void __launch_bounds__(kTile) k_ce_tiled(Dev D, const Work* __restric
     const int cnt = min(kSrcTile, W.c1 - c);
     __syncthreads();
     stage_sources(D, rc_in, b0, c, cnt, tile);
-    for (int k = threadIdx.x; k < cnt; k += blockDim.x) tilef[k] = load_f4(D, b0 + c + k);
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+      tilef[k] = load_f4(D, b0 + c + k);
+      tilerc[k] = f32_trunc(rc_in[4 * (size_t)(b0 + c + k)]);
+    }
     __syncthreads();
-    if (active)
-      for (int k = 0; k < cnt; k++) ce = ce || pair_ce_f(pos, pf, self, c + k, tile[k], tilef[k]);
+    if (active) {
+      // the FP32 prefilter of four sources at a time without branches; the
+      // exact test (pair_ce, FP64) only where one of them says "maybe" (the
+      // flag is the OR of pair_ce_f over the sources, in any order)
+      int k = 0;
+      for (; k + 4 <= cnt; k += 4) {
+        const bool m0 = ce_maybe(pf, tilef[k], tilerc[k]), m1 = ce_maybe(pf, tilef[k + 1], tilerc[k + 1]),
+                   m2 = ce_maybe(pf, tilef[k + 2], tilerc[k + 2]), m3 = ce_maybe(pf, tilef[k + 3], tilerc[k + 3]);
+        if ((m0 | m1 | m2 | m3) && !ce) {
+          if (m0) ce = pair_ce(pos, self, c + k, tile[k]);
+          if (m1 && !ce) ce = pair_ce(pos, self, c + k + 1, tile[k + 1]);
+          if (m2 && !ce) ce = pair_ce(pos, self, c + k + 2, tile[k + 2]);
+          if (m3 && !ce) ce = pair_ce(pos, self, c + k + 3, tile[k + 3]);
+        }
+      }
+      for (; k < cnt; k++)
+        if (!ce && ce_maybe(pf, tilef[k], tilerc[k])) ce = pair_ce(pos, self, c + k, tile[k]);
+    }
   }
   const bool first = active && ce && mark_ce(D.ce, j);
   append_ce(first, j, D.ce_list_big, &D.ce_count[1], &D.counters[0]);
