@@ -1536,7 +1536,7 @@ __global__ void k_kick_reduce_sym(Dev D, const double* __restrict__ rc, const in
     for (int u = 0; u < kRedBatch; u++) {
       const int b = b0r + u * kRedThreads;
       const bool ok = b < count;
-      const bool bk = back(b);
+      const bool bk = ok && back(b);
       const double* p = base + (size_t)b * stride - (bk ? D.sym_set : 0);
       px[u] = ok ? p[index] : 0.0;
       py[u] = ok ? p[span + index] : 0.0;
