@@ -510,14 +510,24 @@ __device__ __forceinline__ PV richardson(const PV& c, const VT& vt, double dt, i
 // ---- universal-variable drift (new formulation, no reference counterpart) ----
 // Stumpff functions by quartering and doubling, Horner-form Taylor series
 // (three terms when |z| < 5e-5, seven otherwise).
+// |z| > c and |z| < c for a positive normal c as integer compares of the bit
+// patterns (positive doubles order like their bits; NaN is neither, as with
+// the FP64 compares, which each take a slot of the FP64 pipe on this GPU)
+__device__ __forceinline__ bool abs_gt(double z, double c) {
+  const long long a = __double_as_longlong(z) & 0x7fffffffffffffffLL;
+  return a > __double_as_longlong(c) && a <= 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool abs_lt(double z, double c) {
+  return (__double_as_longlong(z) & 0x7fffffffffffffffLL) < __double_as_longlong(c);
+}
 __device__ __forceinline__ void stumpff(double z, double* c0, double* c1, double* c2, double* c3) {
   int k = 0;
-  while (fabs(z) > 0.1 && k < 60) {
+  while (abs_gt(z, 0.1) && k < 60) {
     z = z * 0.25;
     k++;
   }
   double s3, s2;
-  if (fabs(z) < 5e-5) {
+  if (abs_lt(z, 5e-5)) {
     // the z^3 terms are below 1e-17 relative here
     s3 = fma(z, fma(z, 1.0 / 5040.0, -1.0 / 120.0), 1.0 / 6.0);
     s2 = fma(z, fma(z, 1.0 / 720.0, -1.0 / 24.0), 0.5);
