@@ -22,10 +22,17 @@ __device__ __forceinline__ double mag2(const d3& a) { return fma(a.x, a.x, fma(a
 // and sqrt(x (x >= 0)).  Where the guard's factor is 1 and its addend 0 they
 // change nothing (1 x = x and y + 0 = y exactly for y != 0, NaN kept), so
 // those cases skip the two operations; the others keep them.
+// The guards' tests on the bit patterns (integer operations; an FP64 compare
+// takes a slot of the FP64 pipe on this GPU): y != 0 is "not +-0" (NaN
+// included, as in the compare), x >= 0 is "+0..+inf or -0" (NaN excluded).
 __device__ __forceinline__ double stable_div(double x, double y) {  // sim.cuh:81-87
-  return y != 0.0 ? x / y : (0.0 * x) / (y + 1.0);
+  return (__double_as_longlong(y) << 1) != 0 ? x / y : (0.0 * x) / (y + 1.0);
 }
-__device__ __forceinline__ double stable_sqrt(double x) { return sqrt(x >= 0.0 ? x : x * 0.0); }  // :35-40
+__device__ __forceinline__ double stable_sqrt(double x) {  // :35-40
+  const long long b = __double_as_longlong(x);
+  const bool ge0 = (b >= 0 && b <= 0x7ff0000000000000LL) || b == (long long)0x8000000000000000ULL;
+  return sqrt(ge0 ? x : x * 0.0);
+}
 
 // Unit constants read at run time (kernel parameters): fma(one, a, b) and
 // fma(a, b, nz) with one = 1 and nz = -0 give exactly a + b and a * b (the
@@ -117,12 +124,17 @@ __device__ __forceinline__ double exact_term(const d3& pos, int self, const SrcV
   const bool other = self != i;
   double r_ij = other ? r : 0.0;  // norm3d of d is the same sqrt of the same fma chain
   // K = changeover_K(y), y = (r_ij - rc01) / rc09.  Without the division
-  // where y is certainly in (1, DBL_MAX), i.e. K = 1: with b = rc09 normal
-  // and t > fl(b (1 + 2^-51)) >= b (1 + 2^-52), t / b > 1 + 2^-52 rounds to
-  // a double > 1; t < fl(b 1e300) keeps it finite.
+  // where y is certainly in (1, DBL_MAX), i.e. K = 1, decided on the bit
+  // patterns (no FP64 compares): b = rc09 positive, normal and >= 2^-1000; t
+  // more than 4 ulps of b above b, so t >= b (1 + 2^-51) and t / b rounds to
+  // a double >= 1 + 2^-52; t below 2^996 b and finite, so t / b stays finite.
+  // Where the test fails the formula gives K = 1 for such pairs too: the same
+  // bits either way.
   const double t = fsub(U, r_ij, rc01);
   double K;
-  if (rc09 >= 0x1p-1000 && t > fmul(U, rc09, 1.0 + 0x1p-51) && t < fmul(U, rc09, 1e300))
+  const long long tb = __double_as_longlong(t), bb = __double_as_longlong(rc09);
+  if (bb >= 0x0170000000000000LL && bb < 0x7ff0000000000000LL && tb > bb + 4 && tb - bb < (996LL << 52) &&
+      tb < 0x7ff0000000000000LL)
     K = 1.0;
   else
     K = changeover_K(U, t / rc09);
