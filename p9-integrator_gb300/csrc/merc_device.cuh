@@ -652,7 +652,11 @@ __device__ __forceinline__ UD universal_drift(const FU& U, const d3& x0, const d
   double v2 = fma(v0.x, v0.x, fma(v0.y, v0.y, fmul(U, v0.z, v0.z)));
   double alpha = fma(2.0, ir0, -v2);
   double zeta = fma(-alpha, r0, 1.0);
-  if (!(s0 > 0.0)) {
+  // (s0 > 0 and the factor-of-2 window of the series guess tested on the bit
+  // patterns where that is exact: FP64 compares and products take FP64-pipe
+  // slots on this GPU)
+  const long long s0b = __double_as_longlong(s0);
+  if (!(s0b > 0 && s0b <= 0x7ff0000000000000LL)) {
     const double p0 = fmul(U, dt, ir0);
     double g = p0;
     if (s0 == kGuessSeries) {
@@ -660,7 +664,15 @@ __device__ __forceinline__ UD universal_drift(const FU& U, const d3& x0, const d
       const double a2 = fmul(U, fmul(U, fma(fmul(U, 3.0, eta), eta, -fmul(U, r0, zeta)), fmul(U, ir0, ir0)),
                              1.0 / 6.0);
       const double q = fmul(U, p0, fma(p0, fma(p0, a2, -a1), 1.0));
-      if (q > 0.5 * p0 && q < 2.0 * p0) g = q;
+      // 0.5 p0 < q < 2 p0: for p0 in [2^-1020, 2^1022) the halving and the
+      // doubling are exact exponent steps, so the window is pb - 2^52 < qb <
+      // pb + 2^52 on the bits (q of another sign or NaN falls outside)
+      const long long pb = __double_as_longlong(p0), qb = __double_as_longlong(q);
+      if (pb >= 0x0030000000000000LL && pb < 0x7fd0000000000000LL) {
+        if (qb > pb - (1LL << 52) && qb < pb + (1LL << 52)) g = q;
+      } else if (q > 0.5 * p0 && q < 2.0 * p0) {
+        g = q;
+      }
     } else if (s0 == kGuessRel) {
       // the learned guess covers long drifts, where s/s0 spans ~0.1..4
       const double q = fma(p0, f64_of_f32(rel), p0);

@@ -35,8 +35,15 @@ __device__ __forceinline__ double thr_pack(int t) { return __longlong_as_double(
 __device__ __forceinline__ int thr_unpack(double d) { return (int)__double_as_longlong(d); }
 
 // high-word threshold: r^2 hi word above this means r > r_crit with margin
+// 0 < x < 1e150, on the bit pattern (positive doubles order like their bits;
+// NaN, zeros and negatives fail as in the FP64 compares, which each take a
+// slot of the FP64 pipe on this GPU)
+__device__ __forceinline__ bool pos_below_1e150(double x) {
+  const long long b = __double_as_longlong(x);
+  return b > 0 && b < 0x5f138d352e5096afLL;  // the bits of 1e150
+}
 __device__ __forceinline__ int rc2_threshold(double rc) {
-  if (!(rc > 0.0) || !(rc < 1e150)) return 0x7fffffff;
+  if (!pos_below_1e150(rc)) return 0x7fffffff;
   return hi_word(rc * rc) + 1;
 }
 

@@ -128,7 +128,7 @@ __device__ __forceinline__ const int* rc_far_thr_c(const double* rc, int n) {
 // no far pairs for a source without a finite positive r_crit.
 constexpr double kFarRadius = 1.5;
 __device__ __forceinline__ int far_threshold(double rc, const d3& x, double hc) {
-  if (!(rc > 0.0) || !(rc < 1e150)) return 0x7fffffff;
+  if (!pos_below_1e150(rc)) return 0x7fffffff;
   const double R = kFarRadius * hc * sqrt(mag2(x));
   return rc2_threshold(R > rc ? R : rc);
 }
@@ -166,14 +166,16 @@ __device__ __forceinline__ int write_rc_fast(const FU& U, double* rc, int n, int
   const double factor = v2 - ir;
   const d3 ev = {fma(factor, x.x, -rdv * v.x), fma(factor, x.y, -rdv * v.y), fma(factor, x.z, -rdv * v.z)};
   const double q = 1.0 - mag2(ev);
-  const double a = q > 0.0 ? h2 * rcp_fast(q) : h2 / q;
+  // (q > 0 on the bit pattern: positive, not NaN)
+  const long long qb = __double_as_longlong(q);
+  const double a = (qb > 0 && qb <= 0x7ff0000000000000LL) ? h2 * rcp_fast(q) : h2 / q;
   const double r = a * hc;
   rc[4 * (size_t)j] = r;
   rc[4 * (size_t)j + 1] = 0.1 * r;
   rc[4 * (size_t)j + 2] = 0.9 * r;
   rc[4 * (size_t)j + 3] = thr_pack(rc2_threshold(r));
   int far = 0x7fffffff;
-  if (r > 0.0 && r < 1e150) {
+  if (pos_below_1e150(r)) {
     const double R = kFarRadius * hc * (xx * ir);
     far = rc2_threshold(R > r ? R : r);
   }
