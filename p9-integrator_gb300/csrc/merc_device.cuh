@@ -82,12 +82,26 @@ __device__ __forceinline__ double rcrit_hc(const d3& r, const d3& v, double hc) 
 // (K gtz valid + gto with gtz = valid = 1, gto = 0; K = +0 at y = 0); the
 // rest (infinite or NaN y) takes the formula.  (Products with 0/1 factors
 // and their conversions each take an FP64 slot.)
+// The range tests of K(y) on the bit patterns, the same decisions as the
+// compares 1 < y < DBL_MAX, -DBL_MAX < y < 0 and 0 <= y <= 1 (NaN in none)
+__device__ __forceinline__ bool y_above_one(double y) {
+  const long long b = __double_as_longlong(y);
+  return b > 0x3ff0000000000000LL && b < 0x7fefffffffffffffLL;
+}
+__device__ __forceinline__ bool y_below_zero(double y) {
+  const long long b = __double_as_longlong(y), m = b & 0x7fffffffffffffffLL;
+  return b < 0 && m != 0 && m < 0x7fefffffffffffffLL;
+}
+__device__ __forceinline__ bool y_in_unit(double y) {
+  const long long b = __double_as_longlong(y);
+  return (b >= 0 && b <= 0x3ff0000000000000LL) || b == (long long)0x8000000000000000ULL;
+}
 __device__ __forceinline__ double changeover_K(const FU& U, double y) {
-  if (y > 1.0 && y < 1.7976931348623157e308) return 1.0;
-  if (y < 0.0 && y > -1.7976931348623157e308) return 0.0;
+  if (y_above_one(y)) return 1.0;
+  if (y_below_zero(y)) return 0.0;
   const double y2 = fmul(U, fmul(U, 2.0, y), y), d = fadd(U, fsub(U, y2, fmul(U, 2.0, y)), 1.0);
   double K = fmul(U, y, y) / d;
-  if (y >= 0.0 && y <= 1.0) return K;
+  if (y_in_unit(y)) return K;
   double gtz = (double)(y > 0.0), gto = (double)(y > 1.0), valid = (double)(y <= 1.0 && y >= 0.0);
   return K * gtz * valid + gto;
 }

@@ -90,10 +90,10 @@ __device__ __forceinline__ double div_seeded(double x, double y) {
 // the finite range its form is kept; selects rather than products with 0/1
 // factors, whose conversions and multiplications each take an FP64 slot)
 __device__ __forceinline__ double changeover_K_seeded(double y) {
-  if (y > 1.0 && y < 1.7976931348623157e308) return 1.0;
-  if (y < 0.0 && y > -1.7976931348623157e308) return 0.0;
+  if (y_above_one(y)) return 1.0;
+  if (y_below_zero(y)) return 0.0;
   const double K = div_seeded(y * y, 2.0 * y * y - 2.0 * y + 1.0);
-  if (y >= 0.0 && y <= 1.0) return K;
+  if (y_in_unit(y)) return K;
   double gtz = (double)(y > 0.0), gto = (double)(y > 1.0), valid = (double)(y <= 1.0 && y >= 0.0);
   return K * gtz * valid + gto;
 }
@@ -115,7 +115,7 @@ __device__ __forceinline__ double pair_exact_w(const d3& pos, int self, int i, c
   if (BS) w = r <= S.rc ? 1.0 - K : K;
   if (other) r_sq += soft2;
   const double den = r_sq * r;
-  return w * (den != 0.0 ? div_seeded(S.m, den) : stable_div(S.m, den));
+  return w * ((__double_as_longlong(den) << 1) != 0 ? div_seeded(S.m, den) : stable_div(S.m, den));
 }
 template <bool BS>
 __device__ __forceinline__ void pair_exact(const d3& pos, int self, int i, const FastSrc& S, double soft2, d3& acc) {

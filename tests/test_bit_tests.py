@@ -111,3 +111,26 @@ def test_k_one_shortcut_implies_quotient_above_one():
     with np.errstate(over="ignore", invalid="ignore"):
         y = t[taken] / b[taken]
     assert np.all(y > 1.0) and np.all(np.isfinite(y))
+
+
+def changeover_ranges(y):
+    """The changeover weight's three range tests on the bit patterns:
+    1 < y < DBL_MAX, -DBL_MAX < y < 0, and 0 <= y <= 1 (changeover_K,
+    changeover_K_seeded)."""
+    yb = bits(y)
+    one, big = int(bits(1.0)), int(bits(np.finfo(np.float64).max))
+    above = (yb > one) & (yb < big)
+    mag = yb & 0x7FFFFFFFFFFFFFFF
+    below = (yb < 0) & (mag != 0) & (mag < big)
+    unit = ((yb >= 0) & (yb <= one)) | (yb == SIGN)
+    return above, below, unit
+
+
+def test_changeover_range_tests():
+    dmax = np.finfo(np.float64).max
+    y = np.concatenate([_edges(1.0, dmax, 0.5), _random(300000, 8)])
+    above, below, unit = changeover_ranges(y)
+    with np.errstate(invalid="ignore"):
+        assert np.array_equal(above, (y > 1.0) & (y < dmax))
+        assert np.array_equal(below, (y < 0.0) & (y > -dmax))
+        assert np.array_equal(unit, (y >= 0.0) & (y <= 1.0))
