@@ -30,7 +30,8 @@ def _edges(*thresholds):
             for direction in (np.inf, -np.inf):
                 w = v
                 for _ in range(4):
-                    w = np.nextafter(w, direction)
+                    with np.errstate(over="ignore"):  # stepping past the largest double
+                        w = np.nextafter(w, direction)
                     out.append(float(w))
     return np.array(out, dtype=np.float64)
 
